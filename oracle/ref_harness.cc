@@ -1,0 +1,132 @@
+// Oracle harness: drives the UNMODIFIED reference sdhash library (compiled
+// from its own sources by oracle/Makefile.ref) through its public C++ API,
+// the same calls the reference CLI makes:
+//   * stream / block digests:  new sdbf(name, istream*, dd_block, size, NULL)
+//     as in sdhash-src/sdhash_threads.cc:258 (stream, -p 1) and :358 (block,
+//     files below the 128 MiB segment size);
+//   * buffer digests:          new sdbf(name, char*, dd_block, len, NULL)
+//     (sdbf/sdbf_class.cc:115, used by the stdin path sdhash_threads.cc:220);
+//   * all-pairs / query-target: sdbf_set::compare_all_quiet /
+//     compare_to_quiet (sdbf/sdbf_set.cc:278, :360) with one thread so the
+//     output order is the set order.
+// Test infrastructure only: nothing in the product links or calls this.
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+#include <vector>
+#include <cstring>
+#include <cstdlib>
+#include <sys/stat.h>
+
+#include "sdbf_class.h"
+#include "sdbf_set.h"
+#include "sdbf_defines.h"
+
+extern "C" {
+
+// Digest `len` bytes; returns a malloc'd SDBF text line (with trailing '\n')
+// or NULL when the reference constructor throws (status in *err).
+char *ref_digest_buffer(const char *name, const unsigned char *buf,
+                        unsigned long long len, unsigned dd_block_size,
+                        int *err) {
+    *err = 0;
+    std::vector<char> copy(buf, buf + len);
+    try {
+        sdbf *s = new sdbf(name, copy.empty() ? (char *)"" : &copy[0],
+                           dd_block_size, len, NULL);
+        std::string t = s->to_string();
+        delete s;
+        char *out = (char *)malloc(t.size() + 1);
+        memcpy(out, t.c_str(), t.size() + 1);
+        return out;
+    } catch (int e) {
+        *err = e;
+        return NULL;
+    }
+}
+
+// Score two SDBF text lines with sdbf::compare (sdbf_class.cc:266).
+int ref_compare_text(const char *a, const char *b, unsigned sample) {
+    try {
+        sdbf x((std::string(a))), y((std::string(b)));
+        return x.compare(&y, sample);
+    } catch (int e) {
+        return -1000 + e;
+    }
+}
+
+// compare_all_quiet over a file of SDBF lines; returns malloc'd result text.
+char *ref_compare_all_file(const char *fname, int threshold) {
+    sdbf_set set(fname);
+    std::string r = set.compare_all_quiet(threshold, 1, false);
+    for (uint32_t i = 0; i < set.size(); i++) delete set.at(i);
+    char *out = (char *)malloc(r.size() + 1);
+    memcpy(out, r.c_str(), r.size() + 1);
+    return out;
+}
+
+// compare_to_quiet(query set, target set); returns malloc'd result text.
+char *ref_compare_to_files(const char *qname, const char *tname,
+                           int threshold, unsigned sample) {
+    sdbf_set q(qname), t(tname);
+    std::string r = q.compare_to_quiet(&t, threshold, sample, 1, false);
+    for (uint32_t i = 0; i < q.size(); i++) delete q.at(i);
+    for (uint32_t i = 0; i < t.size(); i++) delete t.at(i);
+    char *out = (char *)malloc(r.size() + 1);
+    memcpy(out, r.c_str(), r.size() + 1);
+    return out;
+}
+
+void ref_free(void *p) { free(p); }
+
+}  // extern "C"
+
+#ifdef ORACLE_REF_MAIN
+static int usage() {
+    std::cerr << "usage: sdhash_ref digest [-b KB] files... | "
+                 "compare_all set.sdbf [threshold] | "
+                 "compare_to q.sdbf t.sdbf [threshold]\n";
+    return 2;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) return usage();
+    std::string cmd = argv[1];
+    if (cmd == "digest") {
+        int i = 2;
+        uint32_t dd = 0;
+        if (argc > 3 && std::string(argv[2]) == "-b") {
+            dd = (uint32_t)atoi(argv[3]) * 1024;
+            i = 4;
+        }
+        for (; i < argc; i++) {
+            struct stat st;
+            if (stat(argv[i], &st)) continue;
+            std::ifstream is(argv[i], std::ios::binary);
+            try {
+                sdbf *s = new sdbf(argv[i], &is, dd, st.st_size, NULL);
+                std::cout << s;
+                delete s;
+            } catch (int e) {
+                std::cerr << "skip " << argv[i] << " (" << e << ")\n";
+            }
+        }
+        return 0;
+    }
+    if (cmd == "compare_all" && argc >= 3) {
+        char *r = ref_compare_all_file(argv[2], argc > 3 ? atoi(argv[3]) : 1);
+        std::cout << r;
+        free(r);
+        return 0;
+    }
+    if (cmd == "compare_to" && argc >= 4) {
+        char *r = ref_compare_to_files(argv[2], argv[3],
+                                       argc > 4 ? atoi(argv[4]) : 1, 0);
+        std::cout << r;
+        free(r);
+        return 0;
+    }
+    return usage();
+}
+#endif
