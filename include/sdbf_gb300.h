@@ -1,0 +1,151 @@
+/*
+ * sdbf_gb300.h -- C ABI of the GB300 SDBF engine (libsdbf_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every entry point names the reference
+ * sdhash interface (file:line in the sdhash source tree) whose work it
+ * performs; the C++ compatibility classes (sdbf / sdbf_set with the
+ * reference's signatures) and the Python binding sit on top of this ABI.
+ *
+ * Results are bit-exact with sdhash 4.0: digests byte-identical (SDBF v3
+ * text), scores integer-identical.
+ *
+ * Error convention: functions return SDBFG_OK (0) or a negative status;
+ * sdbfg_last_error() describes the last failure on that context.  Nothing
+ * here exits the process (the reference exits on allocation failure,
+ * sdbf/error.cc:33-39).
+ */
+#ifndef SDBF_GB300_H
+#define SDBF_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDBFG_OK 0
+#define SDBFG_ERR_ARG -1        /* bad argument */
+#define SDBFG_ERR_CUDA -2       /* CUDA runtime error (see sdbfg_last_error) */
+#define SDBFG_ERR_NOMEM -3      /* device or host allocation failed */
+#define SDBFG_ERR_FORMAT -4     /* malformed SDBF text */
+#define SDBFG_ERR_CAPACITY -5   /* output buffer too small */
+
+/* Per-input digest status, mirroring the reference constructors' throws
+ * (sdbf/sdbf_class.cc:37,81,117). */
+#define SDBFG_DIGEST_OK 0
+#define SDBFG_DIGEST_TOO_SMALL -3 /* fewer than 512 bytes (MIN_FILE_SIZE) */
+
+typedef struct sdbfg_ctx sdbfg_ctx;
+typedef struct sdbfg_set sdbfg_set;
+
+/* ---------------------------------------------------------------- context
+ * One context = one device + one CUDA stream + reusable device buffers.
+ * Replaces the process-global `sdbf::config` (sdbf/sdbf_class.cc:25) for the
+ * GPU path.  A context is not thread-safe; use one per host thread. */
+int sdbfg_ctx_create(int device, sdbfg_ctx **out);
+void sdbfg_ctx_destroy(sdbfg_ctx *ctx);
+const char *sdbfg_last_error(const sdbfg_ctx *ctx);
+/* Launch on a caller-owned cudaStream_t (NULL = the context's own stream). */
+int sdbfg_ctx_set_stream(sdbfg_ctx *ctx, void *cuda_stream);
+int sdbfg_ctx_synchronize(sdbfg_ctx *ctx);
+/* Kernel launches issued on this context so far (instrumentation). */
+uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx *ctx);
+/* Speculative lead-in of the parallel popularity-score walk, in window steps
+ * (default and maximum 128).  Results are exact for every value -- shorter
+ * lead-ins only make the re-walk path run more often; tests use this to
+ * exercise it.  No counterpart in the reference (its walk is sequential). */
+int sdbfg_ctx_set_lead(sdbfg_ctx *ctx, uint32_t steps);
+/* Tiles whose speculative popularity chain was re-walked (instrumentation). */
+uint64_t sdbfg_ctx_relinked_tiles(sdbfg_ctx *ctx);
+
+/* ----------------------------------------------------- digest generation */
+typedef struct {
+    uint32_t bf_count;      /* filters in the digest */
+    uint32_t last_count;    /* stream: elements in the last filter; block: 0 */
+    int32_t status;         /* SDBFG_DIGEST_OK or SDBFG_DIGEST_TOO_SMALL */
+    uint32_t reserved;
+    uint64_t filter_offset; /* index of the digest's first filter in out_filters */
+} sdbfg_digest_result;
+
+/* Filter slots a batch needs in out_filters: per input (len>>11)+1 for stream
+ * mode (the reference's own allocation bound, sdbf/sdbf_core.cc:202-204) or
+ * len/B + (len%B >= 512) for block mode. */
+uint64_t sdbfg_digest_capacity(const uint64_t *lens, uint32_t n, uint32_t dd_block_size);
+
+/* Digest n inputs.  dd_block_size == 0: stream mode, as
+ *   sdbf::sdbf(name, char *str, 0, length, NULL)        sdbf/sdbf_class.cc:115
+ *   -> gen_chunk_sdbf                                      sdbf/sdbf_core.cc:196
+ * dd_block_size > 0 (<= 16384): block mode, as the same constructor with
+ * dd_block_size -> gen_block_sdbf_mt (sdbf/sdbf_core.cc:287).
+ * The file / istream constructors (sdbf_class.cc:34,71) read the bytes and
+ * then do exactly this.
+ * host_data + offsets[i] holds input i (lens[i] bytes) in HOST memory
+ * (pinned memory is copied directly, pageable memory through a staging
+ * buffer).  Filters land in out_filters (host, 256 bytes per slot,
+ * capacity out_cap filter slots, see sdbfg_digest_capacity); block-mode
+ * element counts in out_elem_counts (one uint16 per slot; may be NULL for
+ * stream mode). */
+int sdbfg_digest_batch(sdbfg_ctx *ctx, const uint8_t *host_data, const uint64_t *offsets, const uint64_t *lens,
+                       uint32_t n, uint32_t dd_block_size, uint8_t *out_filters, uint64_t out_cap,
+                       uint16_t *out_elem_counts, sdbfg_digest_result *results);
+
+/* Same with inputs already in DEVICE memory (offsets must be multiples of
+ * 16) and outputs written to DEVICE memory; results[] is host memory. */
+int sdbfg_digest_batch_device(sdbfg_ctx *ctx, const uint8_t *dev_data, const uint64_t *offsets,
+                              const uint64_t *lens, uint32_t n, uint32_t dd_block_size, uint8_t *dev_out_filters,
+                              uint64_t out_cap, uint16_t *dev_out_elem_counts, sdbfg_digest_result *results);
+
+/* ------------------------------------------------------------ comparison */
+/* A digest as the reference's sdbf object holds it (sdbf/sdbf_class.h:95-119). */
+typedef struct {
+    const char *name;             /* hashname; used by the swap tie-break */
+    const uint8_t *filters;       /* bf_count * 256 bytes (host) */
+    const uint16_t *elem_counts;  /* block digests: per filter; NULL for stream */
+    uint32_t bf_count;
+    uint32_t last_count;          /* stream digests */
+    uint32_t max_elem;            /* 160 stream / 192 block */
+    uint32_t dd_block_size;       /* 0 for stream digests */
+    uint64_t orig_size;
+} sdbfg_digest_desc;
+
+/* Upload digests to the device once (the resident form of sdbf_set,
+ * sdbf/sdbf_set.h:15-96); hamming weights are computed on upload
+ * (sdbf::compute_hamming, sdbf_class.cc:388-401). */
+int sdbfg_set_upload(sdbfg_ctx *ctx, const sdbfg_digest_desc *digests, uint32_t n, sdbfg_set **out);
+void sdbfg_set_free(sdbfg_set *set);
+uint32_t sdbfg_set_size(const sdbfg_set *set);
+
+/* Scores of explicit pairs (a[ia[k]], b[ib[k]]) as sdbf::compare(other, 0)
+ * (sdbf/sdbf_class.cc:266 -> sdbf_score, sdbf/sdbf_core.cc:330-389),
+ * including the swap rule and the -1 result.  b may equal a. */
+int sdbfg_score_pairs(sdbfg_ctx *ctx, const sdbfg_set *a, const sdbfg_set *b, const uint32_t *ia,
+                      const uint32_t *ib, uint64_t npairs, int32_t *out_scores);
+
+/* All pairs i<j of one set in set order (sdbf_set::compare_all /
+ * compare_all_quiet, sdbf/sdbf_set.cc:239-308): out has n*(n-1)/2 scores in
+ * row order (0,1),(0,2),...,(1,2),... */
+int sdbfg_compare_all(sdbfg_ctx *ctx, const sdbfg_set *set, int32_t *out_scores);
+
+/* Every query against every target (sdbf_set::compare_to /
+ * compare_to_quiet with sample_size 0, sdbf/sdbf_set.cc:317-394):
+ * out[i*nt + j] = score(query i, target j). */
+int sdbfg_compare_to(sdbfg_ctx *ctx, const sdbfg_set *queries, const sdbfg_set *targets, int32_t *out_scores);
+
+/* ------------------------------------------------------------ SDBF text */
+/* sdbf::to_string (sdbf/sdbf_class.cc:293-334): one SDBF v3 line with
+ * trailing newline.  Writes at most cap bytes (NUL-terminated); returns the
+ * length needed (excluding NUL) or a negative status. */
+int64_t sdbfg_to_string(const sdbfg_digest_desc *d, char *out, uint64_t cap);
+
+/* sdbf::sdbf(const std::string&) (sdbf/sdbf_class.cc:144-215).  Parses one
+ * line into caller-provided buffers (filters: bf_count*256 bytes, elem_counts:
+ * bf_count entries for sdbf-dd).  Call first with filters == NULL to learn
+ * bf_count / name length via *d.  name_buf receives the NUL-terminated name.
+ * Returns SDBFG_OK, -1 (shorter than 344 chars) or SDBFG_ERR_FORMAT. */
+int sdbfg_parse(const char *line, uint64_t len, sdbfg_digest_desc *d, char *name_buf, uint64_t name_cap,
+                uint8_t *filters, uint16_t *elem_counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -123,8 +123,8 @@ class Oracle:
                                              i32p, C.c_int]
         L.orc_score_pairs.argtypes = [C.POINTER(_Digest), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                       C.c_uint64, i32p, C.c_int]
-        L.orc_digest_many.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_uint32, C.c_uint32,
-                                      C.c_int, C.POINTER(_Digest), C.POINTER(C.c_int)]
+        L.orc_digest_many.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.POINTER(C.c_char_p),
+                                      C.c_uint32, C.c_uint32, C.c_int, C.POINTER(_Digest), C.POINTER(C.c_int)]
         L.orc_b64_encode.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p]
         L.orc_b64_encode.restype = C.c_size_t
 
@@ -211,9 +211,12 @@ class Oracle:
                                       out.ctypes.data_as(C.POINTER(C.c_int32)), nthreads)
         return out
 
-    def digest_many(self, bufs, dd_block_size: int = 0, nthreads: int = 0):
+    def digest_many(self, bufs, dd_block_size: int = 0, nthreads: int = 0, names=None):
         """Digest a list of bytes-like buffers on nthreads threads (file-parallel)."""
         n = len(bufs)
+        cnames = None
+        if names is not None:
+            cnames = (C.c_char_p * n)(*[x.encode() for x in names])
         ptrs = (C.c_void_p * n)()
         lens = (C.c_uint64 * n)()
         keep = []
@@ -227,7 +230,7 @@ class Oracle:
             lens[i] = len(b)
         outs = (_Digest * n)()
         status = (C.c_int * n)()
-        self.L.orc_digest_many(ptrs, lens, n, dd_block_size, nthreads, outs, status)
+        self.L.orc_digest_many(ptrs, lens, cnames, n, dd_block_size, nthreads, outs, status)
         res = []
         for i in range(n):
             res.append(OracleDigest(self.L, outs[i]) if status[i] == 0 else None)

@@ -691,6 +691,7 @@ typedef struct {
     int tid, nt;
     const uint8_t *const *bufs;
     const uint64_t *lens;
+    const char *const *names;
     uint32_t n, dd;
     orc_digest *outs;
     int *status;
@@ -701,19 +702,20 @@ static void *digest_worker(void *arg) {
     char name[32];
     for (uint32_t i = (uint32_t)t->tid; i < t->n; i += (uint32_t)t->nt) {
         snprintf(name, sizeof name, "f%u", i);
-        t->status[i] = t->dd ? orc_digest_block(name, t->bufs[i], t->lens[i], t->dd, &t->outs[i])
-                             : orc_digest_stream(name, t->bufs[i], t->lens[i], &t->outs[i]);
+        const char *nm = t->names ? t->names[i] : name;
+        t->status[i] = t->dd ? orc_digest_block(nm, t->bufs[i], t->lens[i], t->dd, &t->outs[i])
+                             : orc_digest_stream(nm, t->bufs[i], t->lens[i], &t->outs[i]);
     }
     return NULL;
 }
 
-void orc_digest_many(const uint8_t *const *bufs, const uint64_t *lens, uint32_t n, uint32_t dd,
-                     int nthreads, orc_digest *outs, int *status) {
+void orc_digest_many(const uint8_t *const *bufs, const uint64_t *lens, const char *const *names, uint32_t n,
+                     uint32_t dd, int nthreads, orc_digest *outs, int *status) {
     int nt = resolve_threads(nthreads);
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nt);
     digest_task *ts = (digest_task *)malloc(sizeof(digest_task) * (size_t)nt);
     for (int i = 0; i < nt; i++) {
-        digest_task d = {i, nt, bufs, lens, n, dd, outs, status};
+        digest_task d = {i, nt, bufs, lens, names, n, dd, outs, status};
         ts[i] = d;
         pthread_create(&th[i], NULL, digest_worker, &ts[i]);
     }

@@ -92,7 +92,7 @@ void orc_score_pairs(const orc_digest *set, const uint32_t *pi, const uint32_t *
 
 /* Digest many buffers on nthreads host threads (file-parallel, as
  * sdhash-src/sdhash_threads.cc:152-186 assigns files round-robin). */
-void orc_digest_many(const uint8_t *const *bufs, const uint64_t *lens, uint32_t n,
+void orc_digest_many(const uint8_t *const *bufs, const uint64_t *lens, const char *const *names, uint32_t n,
                      uint32_t dd_block_size, int nthreads, orc_digest *outs, int *status);
 
 /* Base64 (RFC 4648, '=' padding) as produced by base64/modp_b64.cc. */

@@ -1,0 +1,511 @@
+"""sdhash_gb300 -- GB300-native SDBF digest generation and comparison.
+
+Python binding over the C ABI of libsdbf_gb300.so (include/sdbf_gb300.h).
+The compute runs in hand-written sm_103a CUDA kernels; this module only
+marshals arguments.  There is no CPU fallback: if the native library is
+missing, every entry point raises.
+
+Two layers:
+* ``Context`` -- batched calls (digest many inputs, upload digest sets,
+  all-pairs / query-target comparison).
+* ``sdbf`` / ``sdbf_set`` -- the reference's object API (sdbf/sdbf_class.h,
+  sdbf/sdbf_set.h) with the same method names, argument meaning, result text
+  and error behaviour (constructors raise ``SdbfError`` carrying the
+  reference's throw codes -1 / -2 / -3).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsdbf_gb300.so")
+SYNTH_PATH = os.path.join(HERE, "libsdbf_synth.so")
+
+MIN_FILE_SIZE = 512
+STREAM_MAX_ELEM = 160
+BLOCK_MAX_ELEM = 192
+
+
+class SdbfError(Exception):
+    """Raised where the reference throws an int (its value is ``code``)."""
+
+    def __init__(self, code: int, msg: str = ""):
+        super().__init__(f"sdbf error {code}: {msg}" if msg else f"sdbf error {code}")
+        self.code = code
+
+
+class DigestResult(C.Structure):
+    _fields_ = [("bf_count", C.c_uint32), ("last_count", C.c_uint32), ("status", C.c_int32),
+                ("reserved", C.c_uint32), ("filter_offset", C.c_uint64)]
+
+
+class DigestDesc(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("filters", C.c_void_p), ("elem_counts", C.c_void_p),
+                ("bf_count", C.c_uint32), ("last_count", C.c_uint32), ("max_elem", C.c_uint32),
+                ("dd_block_size", C.c_uint32), ("orig_size", C.c_uint64)]
+
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def lib() -> C.CDLL:
+    """Load libsdbf_gb300.so (raises if it was not built)."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} not built: run `python -m sdhash_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp, u64p, u32p, i32p = C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32), C.POINTER(C.c_int32)
+        L.sdbfg_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+        L.sdbfg_ctx_destroy.argtypes = [vp]
+        L.sdbfg_last_error.argtypes = [vp]
+        L.sdbfg_last_error.restype = C.c_char_p
+        L.sdbfg_ctx_set_stream.argtypes = [vp, vp]
+        L.sdbfg_ctx_synchronize.argtypes = [vp]
+        L.sdbfg_ctx_launch_count.argtypes = [vp]
+        L.sdbfg_ctx_launch_count.restype = C.c_uint64
+        L.sdbfg_ctx_set_lead.argtypes = [vp, C.c_uint32]
+        L.sdbfg_ctx_relinked_tiles.argtypes = [vp]
+        L.sdbfg_ctx_relinked_tiles.restype = C.c_uint64
+        L.sdbfg_digest_capacity.argtypes = [u64p, C.c_uint32, C.c_uint32]
+        L.sdbfg_digest_capacity.restype = C.c_uint64
+        L.sdbfg_digest_batch.argtypes = [vp, vp, u64p, u64p, C.c_uint32, C.c_uint32, vp, C.c_uint64, vp,
+                                         C.POINTER(DigestResult)]
+        L.sdbfg_digest_batch_device.argtypes = [vp, vp, u64p, u64p, C.c_uint32, C.c_uint32, vp, C.c_uint64, vp,
+                                                C.POINTER(DigestResult)]
+        L.sdbfg_set_upload.argtypes = [vp, C.POINTER(DigestDesc), C.c_uint32, C.POINTER(vp)]
+        L.sdbfg_set_free.argtypes = [vp]
+        L.sdbfg_set_size.argtypes = [vp]
+        L.sdbfg_set_size.restype = C.c_uint32
+        L.sdbfg_score_pairs.argtypes = [vp, vp, vp, u32p, u32p, C.c_uint64, i32p]
+        L.sdbfg_compare_all.argtypes = [vp, vp, i32p]
+        L.sdbfg_compare_to.argtypes = [vp, vp, vp, i32p]
+        L.sdbfg_to_string.argtypes = [C.POINTER(DigestDesc), C.c_char_p, C.c_uint64]
+        L.sdbfg_to_string.restype = C.c_int64
+        L.sdbfg_parse.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(DigestDesc), C.c_char_p, C.c_uint64, vp, vp]
+        _lib = L
+        return L
+
+
+def _u64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+def _ptr(a: np.ndarray, t=C.c_uint64):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class Digest:
+    """A similarity digest: the data fields of the reference's sdbf object."""
+
+    __slots__ = ("name", "orig_size", "bf_count", "last_count", "max_elem", "dd_block_size", "filters",
+                 "elem_counts")
+
+    def __init__(self, name: str, orig_size: int, bf_count: int, last_count: int, max_elem: int,
+                 dd_block_size: int, filters: np.ndarray, elem_counts: np.ndarray | None):
+        self.name = name
+        self.orig_size = orig_size
+        self.bf_count = bf_count
+        self.last_count = last_count
+        self.max_elem = max_elem
+        self.dd_block_size = dd_block_size
+        self.filters = np.ascontiguousarray(filters, dtype=np.uint8).reshape(-1)
+        self.elem_counts = None if elem_counts is None else np.ascontiguousarray(elem_counts, dtype=np.uint16)
+
+    def _desc(self, keep: list) -> DigestDesc:
+        name = self.name.encode()
+        keep.append(name)
+        d = DigestDesc()
+        d.name = name
+        d.filters = self.filters.ctypes.data
+        d.elem_counts = self.elem_counts.ctypes.data if self.elem_counts is not None else None
+        d.bf_count = self.bf_count
+        d.last_count = self.last_count
+        d.max_elem = self.max_elem
+        d.dd_block_size = self.dd_block_size
+        d.orig_size = self.orig_size
+        return d
+
+    def to_string(self) -> str:
+        """SDBF v3 text line (sdbf::to_string, sdbf/sdbf_class.cc:293-334)."""
+        keep: list = []
+        d = self._desc(keep)
+        n = lib().sdbfg_to_string(C.byref(d), None, 0)
+        if n < 0:
+            raise SdbfError(int(n), "to_string")
+        buf = C.create_string_buffer(int(n) + 1)
+        lib().sdbfg_to_string(C.byref(d), buf, n + 1)
+        return buf.raw[:n].decode()
+
+    @staticmethod
+    def from_string(line: str) -> "Digest":
+        """Parse one SDBF line (sdbf(const std::string&), sdbf_class.cc:144-215)."""
+        b = line.encode()
+        d = DigestDesc()
+        rc = lib().sdbfg_parse(b, len(b), C.byref(d), None, 0, None, None)
+        if rc != 0:
+            raise SdbfError(-1 if rc == -1 else -2, "parse")
+        n = d.bf_count
+        filters = np.zeros(n * 256, dtype=np.uint8)
+        counts = np.zeros(n, dtype=np.uint16) if d.dd_block_size else None
+        name = C.create_string_buffer(len(b) + 1)
+        rc = lib().sdbfg_parse(b, len(b), C.byref(d), name, len(b) + 1, filters.ctypes.data,
+                               counts.ctypes.data if counts is not None else None)
+        if rc != 0:
+            raise SdbfError(-2, "parse")
+        return Digest(name.value.decode(), d.orig_size, d.bf_count, d.last_count, d.max_elem, d.dd_block_size,
+                      filters, counts)
+
+    def elem_count(self, i: int) -> int:
+        """get_elem_count (sdbf/sdbf_class.cc:406-415)."""
+        if self.elem_counts is not None:
+            return int(self.elem_counts[i])
+        return self.max_elem if i < self.bf_count - 1 else self.last_count
+
+
+class DeviceSet:
+    """Digests resident in device memory (sdbfg_set)."""
+
+    def __init__(self, ctx: "Context", digests: list[Digest]):
+        self.ctx = ctx
+        self.digests = digests
+        keep: list = []
+        arr = (DigestDesc * max(1, len(digests)))()
+        for i, d in enumerate(digests):
+            arr[i] = d._desc(keep)
+        h = C.c_void_p()
+        rc = lib().sdbfg_set_upload(ctx.h, arr, len(digests), C.byref(h))
+        ctx._check(rc)
+        self.h = h
+
+    def __len__(self):
+        return len(self.digests)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sdbfg_set_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One device, one stream, reusable device buffers (sdbfg_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        rc = lib().sdbfg_ctx_create(device, C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"sdbfg_ctx_create failed ({rc}): no usable CUDA device {device}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sdbfg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise RuntimeError(f"sdbf_gb300 error {rc}: {lib().sdbfg_last_error(self.h).decode()}")
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(lib().sdbfg_ctx_set_stream(self.h, stream_handle or None))
+
+    def synchronize(self):
+        self._check(lib().sdbfg_ctx_synchronize(self.h))
+
+    def set_lead(self, steps: int):
+        """Speculative lead-in of the parallel score walk (exact for any value)."""
+        self._check(lib().sdbfg_ctx_set_lead(self.h, steps))
+
+    @property
+    def launch_count(self) -> int:
+        return int(lib().sdbfg_ctx_launch_count(self.h))
+
+    @property
+    def relinked_tiles(self) -> int:
+        return int(lib().sdbfg_ctx_relinked_tiles(self.h))
+
+    # ------------------------------------------------------------ digests
+    @staticmethod
+    def capacity(lens, dd_block_size: int = 0) -> int:
+        lens = _u64(lens)
+        return int(lib().sdbfg_digest_capacity(_ptr(lens), len(lens), dd_block_size))
+
+    def digest_packed(self, data: np.ndarray, offsets, lens, dd_block_size: int = 0, names=None,
+                      out_filters: np.ndarray | None = None):
+        """Digest inputs packed in one host buffer (input i = data[offsets[i]:offsets[i]+lens[i]]).
+        Returns a list of Digest (None for inputs below 512 bytes)."""
+        data = np.ascontiguousarray(data, dtype=np.uint8)
+        offsets, lens = _u64(offsets), _u64(lens)
+        n = len(lens)
+        cap = self.capacity(lens, dd_block_size)
+        if out_filters is None or out_filters.size < cap * 256:
+            out_filters = np.zeros(max(1, cap) * 256, dtype=np.uint8)
+        counts = np.zeros(max(1, cap), dtype=np.uint16)
+        res = (DigestResult * max(1, n))()
+        rc = lib().sdbfg_digest_batch(self.h, data.ctypes.data, _ptr(offsets), _ptr(lens), n, dd_block_size,
+                                      out_filters.ctypes.data, cap, counts.ctypes.data if dd_block_size else None,
+                                      res)
+        self._check(rc)
+        out = []
+        for i in range(n):
+            r = res[i]
+            if r.status != 0:
+                out.append(None)
+                continue
+            o, k = int(r.filter_offset), int(r.bf_count)
+            name = names[i] if names is not None else f"f{i}"
+            filt = out_filters[o * 256:(o + k) * 256].copy()
+            if dd_block_size:
+                out.append(Digest(name, int(lens[i]), k, 0, BLOCK_MAX_ELEM, dd_block_size, filt,
+                                  counts[o:o + k].copy()))
+            else:
+                out.append(Digest(name, int(lens[i]), k, int(r.last_count), STREAM_MAX_ELEM, 0, filt, None))
+        return out
+
+    def digest_buffers(self, buffers, names=None, dd_block_size: int = 0):
+        """Digest a list of bytes-like inputs."""
+        lens = np.array([len(b) for b in buffers], dtype=np.uint64)
+        offs = np.zeros(len(buffers), dtype=np.uint64)
+        tot = 0
+        for i, b in enumerate(buffers):
+            offs[i] = tot
+            tot += (len(b) + 15) & ~15
+        data = np.zeros(max(16, tot), dtype=np.uint8)
+        for i, b in enumerate(buffers):
+            data[int(offs[i]):int(offs[i]) + len(b)] = np.frombuffer(bytes(b), dtype=np.uint8)
+        return self.digest_packed(data, offs, lens, dd_block_size, names)
+
+    def digest_device(self, dev_data: int, offsets, lens, dd_block_size: int, dev_out_filters: int, out_cap: int,
+                      dev_out_counts: int | None = None):
+        """Digest inputs already in device memory; returns (bf_count, last_count, status, filter_offset) arrays."""
+        offsets, lens = _u64(offsets), _u64(lens)
+        n = len(lens)
+        res = (DigestResult * max(1, n))()
+        rc = lib().sdbfg_digest_batch_device(self.h, dev_data, _ptr(offsets), _ptr(lens), n, dd_block_size,
+                                             dev_out_filters, out_cap, dev_out_counts, res)
+        self._check(rc)
+        return res
+
+    # ---------------------------------------------------------- compare
+    def upload(self, digests: list[Digest]) -> DeviceSet:
+        return DeviceSet(self, digests)
+
+    def compare_all(self, s: DeviceSet) -> np.ndarray:
+        n = len(s)
+        out = np.zeros(max(1, n * (n - 1) // 2), dtype=np.int32)
+        if n > 1:
+            self._check(lib().sdbfg_compare_all(self.h, s.h, _ptr(out, C.c_int32)))
+        return out[: n * (n - 1) // 2]
+
+    def compare_to(self, q: DeviceSet, t: DeviceSet) -> np.ndarray:
+        out = np.zeros(max(1, len(q) * len(t)), dtype=np.int32)
+        if len(q) and len(t):
+            self._check(lib().sdbfg_compare_to(self.h, q.h, t.h, _ptr(out, C.c_int32)))
+        return out[: len(q) * len(t)].reshape(len(q), len(t))
+
+    def score_pairs(self, a: DeviceSet, b: DeviceSet, ia, ib) -> np.ndarray:
+        ia = np.ascontiguousarray(ia, dtype=np.uint32)
+        ib = np.ascontiguousarray(ib, dtype=np.uint32)
+        out = np.zeros(max(1, len(ia)), dtype=np.int32)
+        if len(ia):
+            self._check(lib().sdbfg_score_pairs(self.h, a.h, b.h, _ptr(ia, C.c_uint32), _ptr(ib, C.c_uint32),
+                                                len(ia), _ptr(out, C.c_int32)))
+        return out[: len(ia)]
+
+
+# ----------------------------------------------------- reference object API
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(int(os.environ.get("SDBFG_DEVICE", "0")))
+    return _default_ctx
+
+
+class sdbf:  # noqa: N801 -- the reference's class name
+    """Mirror of the reference's ``class sdbf`` (sdbf/sdbf_class.h:23-121).
+
+    sdbf(name, data, dd_block_size=0)   -- sdbf(const char*, char*, uint32_t, uint64_t, index_info*)
+    sdbf.from_file(path, dd_block_size) -- sdbf(const char *filename, uint32_t dd_block_size)
+    sdbf.from_string(line)              -- sdbf(const std::string&)
+    """
+
+    def __init__(self, name: str | None = None, data=None, dd_block_size: int = 0, *, _digest: Digest | None = None):
+        if _digest is not None:
+            self._d = _digest
+            return
+        if data is None or len(data) < MIN_FILE_SIZE:
+            raise SdbfError(-3, "input too small")  # sdbf_class.cc:116-117
+        d = default_context().digest_buffers([data], [name], dd_block_size)[0]
+        if d is None:
+            raise SdbfError(-3, "input too small")
+        self._d = d
+
+    @classmethod
+    def from_file(cls, path: str, dd_block_size: int = 0) -> "sdbf":
+        try:
+            with open(path, "rb") as f:
+                data = f.read()
+        except OSError:
+            raise SdbfError(-1, "cannot read file")  # sdbf_class.cc:36-37
+        if len(data) < MIN_FILE_SIZE:
+            raise SdbfError(-1, "file too small")
+        return cls(path, data, dd_block_size)
+
+    @classmethod
+    def from_string(cls, line: str) -> "sdbf":
+        return cls(_digest=Digest.from_string(line))
+
+    @property
+    def digest(self) -> Digest:
+        return self._d
+
+    def name(self) -> str:
+        return self._d.name
+
+    def size(self) -> int:
+        return self._d.bf_count * 256
+
+    def input_size(self) -> int:
+        return self._d.orig_size
+
+    def filter_count(self) -> int:
+        return self._d.bf_count
+
+    def clone_filter(self, pos: int) -> bytes | None:
+        if pos >= self._d.bf_count:
+            return None
+        return self._d.filters[pos * 256:(pos + 1) * 256].tobytes()
+
+    @staticmethod
+    def get_elem_count(s: "sdbf", index: int) -> int:
+        return s._d.elem_count(index)
+
+    def compare(self, other: "sdbf", sample: int = 0) -> int:
+        """sdbf::compare (sdbf/sdbf_class.cc:266); sample must be 0."""
+        if sample:
+            raise NotImplementedError("filter sampling (random, unpinned in the reference) is not supported")
+        ctx = default_context()
+        s = ctx.upload([self._d, other._d])
+        return int(ctx.score_pairs(s, s, [0], [1])[0])
+
+    def to_string(self) -> str:
+        return self._d.to_string()
+
+    def __str__(self):
+        return self.to_string()
+
+
+def _result_lines(names_a, names_b, pairs, scores, threshold: int, sep: str) -> str:
+    # sdbf_set.cc:254-262: "a|b|%03d", -1 unpadded, only scores >= threshold
+    out = []
+    for (i, j), s in zip(pairs, scores):
+        s = int(s)
+        if s >= threshold:
+            out.append(f"{names_a[i]}{sep}{names_b[j]}{sep}{s:03d}\n" if s != -1
+                       else f"{names_a[i]}{sep}{names_b[j]}{sep}{s}\n")
+    return "".join(out)
+
+
+class sdbf_set:  # noqa: N801
+    """Mirror of the reference's ``class sdbf_set`` (sdbf/sdbf_set.h:15-96)."""
+
+    def __init__(self, fname: str | None = None):
+        self.items: list[sdbf] = []
+        self.setname = "default"
+        self.sep = "|"
+        self._lock = threading.Lock()
+        if fname is not None and os.path.isfile(fname):
+            with open(fname) as f:
+                for line in f:
+                    if not line.strip():
+                        break
+                    self.items.append(sdbf.from_string(line))
+            self.setname = fname
+
+    def at(self, pos: int):
+        return self.items[pos] if pos < len(self.items) else None
+
+    def add(self, item):
+        with self._lock:
+            if isinstance(item, sdbf_set):
+                self.items.extend(item.items)
+            else:
+                self.items.append(item)
+
+    def size(self) -> int:
+        return len(self.items)
+
+    def input_size(self) -> int:
+        return sum(s.input_size() for s in self.items)
+
+    def empty(self) -> int:
+        return 1 if not self.items else 0
+
+    def name(self) -> str:
+        return self.setname
+
+    def set_name(self, name: str):
+        self.setname = name
+
+    def set_separator(self, sep: str):
+        self.sep = sep
+
+    def to_string(self) -> str:
+        return "".join(s.to_string() for s in self.items)
+
+    def compare_all_quiet(self, threshold: int = 1, thread_count: int = 0, fast: bool = False) -> str:
+        """sdbf_set::compare_all_quiet (sdbf/sdbf_set.cc:278-308), in set order."""
+        if fast:
+            raise NotImplementedError("--fast folding is not supported")
+        n = len(self.items)
+        if n < 2:
+            return ""
+        ctx = default_context()
+        ds = ctx.upload([s.digest for s in self.items])
+        scores = ctx.compare_all(ds)
+        pairs = [(i, j) for i in range(n) for j in range(i + 1, n)]
+        names = [s.name() for s in self.items]
+        return _result_lines(names, names, pairs, scores, threshold, self.sep)
+
+    def compare_all(self, threshold: int = 1, fast: bool = False) -> None:
+        print(self.compare_all_quiet(threshold, 0, fast), end="")
+
+    def compare_to_quiet(self, other: "sdbf_set", threshold: int = 1, sample_size: int = 0, thread_count: int = 0,
+                         fast: bool = False) -> str:
+        """sdbf_set::compare_to_quiet (sdbf/sdbf_set.cc:360-394), in set order."""
+        if sample_size or fast:
+            raise NotImplementedError("sampling / --fast are not supported")
+        if not self.items or not other.items:
+            return ""
+        ctx = default_context()
+        q = ctx.upload([s.digest for s in self.items])
+        t = ctx.upload([s.digest for s in other.items])
+        scores = ctx.compare_to(q, t)
+        pairs = [(i, j) for i in range(len(self.items)) for j in range(len(other.items))]
+        return _result_lines([s.name() for s in self.items], [s.name() for s in other.items], pairs,
+                             scores.reshape(-1), threshold, self.sep)
+
+    def compare_to(self, other: "sdbf_set", threshold: int = 1, sample_size: int = 0, fast: bool = False) -> None:
+        print(self.compare_to_quiet(other, threshold, sample_size, 0, fast), end="")

@@ -1,0 +1,823 @@
+// gen_kernels.cu -- SDBF digest generation on sm_103a.
+//
+// Restates sdhash's generation path (sdbf/sdbf_core.cc:21-324) as three
+// kernels over a batch of files resident in HBM:
+//
+//  k_stream_tiles   one CTA per tile of kTileL window steps of a 32 MiB
+//                   stream chunk: bytes -> ranks (rolling 64-byte entropy,
+//                   gen_chunk_ranks :21-45) -> popularity scores
+//                   (gen_chunk_scores :50-89, parallelised below) ->
+//                   selection score > 16 -> SHA-1 of every selected 64-byte
+//                   feature.  Writes the ordered feature digests of the tile.
+//  k_stream_verify  one CTA per chunk: checks that each tile's speculative
+//                   entry state matches its predecessor's exit state and
+//                   recomputes a tile in place when it does not.
+//  k_stream_commit  one warp per file: the ordered filter fill of
+//                   gen_chunk_hash (:93-136) -- 256-byte filter insert with
+//                   zero-new-bit suppression, the 16 KiB "big filter"
+//                   dedupe (bloom_filter.cc:333-359), roll-over at 160
+//                   elements, big-filter roll-over at 8738 per chunk, and the
+//                   final chop (:235-238).
+//  k_block_digest   one CTA per dd block (gen_block_sdbf_mt :251-324,
+//                   gen_block_hash :141-191): histogram threshold, <=192
+//                   ordered inserts.
+//
+// Popularity scores in parallel.  gen_chunk_scores is a sequential state
+// machine over window steps i with state (P, M) = (min_pos, min_rank).  A
+// step is either a "cheap slide" (depends on (P, M) and rank[i+64]) or a full
+// rescan of window [i, i+63], whose result depends on i only.  Hence two
+// walks that reach the same state at the same step agree from then on.  Each
+// thread walks one segment of steps, starting kLead steps early with an
+// assumed full rescan; the state it reaches at its segment start is compared
+// with the state its left neighbour reaches at the same step.  Equal states
+// prove the segment exact (induction from step 0, which is always a full
+// rescan); a mismatch is re-walked from the neighbour's state.  The same
+// check links consecutive tiles of a chunk (k_stream_verify).
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gen_kernels.h"
+#include "sdbf_device.cuh"
+
+namespace sdbfg {
+
+// ------------------------------------------------------------ smem layout
+struct TileGeom {
+    uint32_t n;      // chunk length
+    uint32_t t0;     // first step owned by the tile
+    uint32_t S0;     // first step whose credits the tile needs (t0-64, or 0)
+    uint32_t SE;     // end of steps (exclusive), <= n-64
+    uint32_t Q0;     // first step simulated (lead-in), multiple of 64 rel. chunk
+    uint32_t RE;     // end of rank positions (exclusive)
+    uint32_t BE;     // end of bytes (exclusive)
+    uint32_t L;      // positions owned: [t0, t0+L)
+};
+
+// Shared-memory carve-up for a tile of at most Lmax owned positions.
+struct TileSmem {
+    uint32_t* bytes32;     // chunk bytes [Q0, BE) (+pad)
+    uint16_t* ranks;       // ranks [Q0, RE)
+    uint8_t* hist;         // per-thread byte histograms (phase 2 only)
+    uint16_t* fres;        // full-rescan result per step [Q0, SE)
+    uint32_t* eqw;         // run bits: bit o = rank[o]==rank[o+1]
+    uint32_t* score32;     // u8 scores of [t0, t0+L) packed 4 per word
+    uint32_t* list;        // selected positions (relative to t0)
+    uint64_t* sig;         // per-segment entry state
+    uint64_t* tau;         // per-segment exit state
+    uint32_t* misc;        // scalars
+};
+
+__host__ __device__ constexpr uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
+
+__host__ __device__ inline uint32_t tile_smem_bytes(uint32_t Lmax) {
+    const uint32_t span = Lmax + 64 + kLead + 64;           // rank positions
+    uint32_t b = 0;
+    b += align_up(span + 64 + 16, 16);                       // bytes
+    b += align_up(span * 2, 16);                             // ranks
+    const uint32_t hist = 256 * kGenThreads;
+    const uint32_t phase3 = align_up((Lmax + 64 + kLead) * 2, 16) + align_up((span / 32 + 4) * 4, 16) +
+                            align_up(Lmax + 16, 16);
+    b += hist > phase3 ? hist : phase3;                      // union
+    b += align_up(((Lmax + 64) / 15 + 8) * 4, 16);           // selected / candidate positions
+    b += 2 * kSegs * 8;                                      // sig, tau
+    b += 64 * 4;                                             // misc
+    return b;
+}
+
+__device__ inline TileSmem carve(uint8_t* base, uint32_t Lmax) {
+    TileSmem s;
+    const uint32_t span = Lmax + 64 + kLead + 64;
+    uint8_t* p = base;
+    s.bytes32 = reinterpret_cast<uint32_t*>(p); p += align_up(span + 64 + 16, 16);
+    s.ranks = reinterpret_cast<uint16_t*>(p); p += align_up(span * 2, 16);
+    uint8_t* u = p;
+    s.hist = u;
+    s.fres = reinterpret_cast<uint16_t*>(u); u += align_up((Lmax + 64 + kLead) * 2, 16);
+    s.eqw = reinterpret_cast<uint32_t*>(u); u += align_up((span / 32 + 4) * 4, 16);
+    s.score32 = reinterpret_cast<uint32_t*>(u); u += align_up(Lmax + 16, 16);
+    const uint32_t hist = 256 * kGenThreads;
+    const uint32_t phase3 = (uint32_t)(u - p);
+    p += hist > phase3 ? hist : phase3;
+    s.list = reinterpret_cast<uint32_t*>(p); p += align_up(((Lmax + 64) / 15 + 8) * 4, 16);
+    s.sig = reinterpret_cast<uint64_t*>(p); p += kSegs * 8;
+    s.tau = reinterpret_cast<uint64_t*>(p); p += kSegs * 8;
+    s.misc = reinterpret_cast<uint32_t*>(p);
+    return s;
+}
+
+// ------------------------------------------------------- phase 1: bytes
+__device__ inline void load_bytes(const uint8_t* __restrict__ chunk, const TileGeom& g, uint32_t* dst32) {
+    // [Q0, BE) -> dst; Q0 is a multiple of 64 relative to the chunk start and
+    // chunks start 16-byte aligned, so the bulk moves as 16-byte vectors.
+    const uint32_t nbytes = g.BE - g.Q0;
+    const uint8_t* src = chunk + g.Q0;
+    // dd blocks of a size that is not a multiple of 16 start unaligned
+    const uint32_t nvec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0) ? nbytes / 16 : 0;
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst32);
+    for (uint32_t i = threadIdx.x; i < nvec; i += blockDim.x) d4[i] = __ldg(s4 + i);
+    uint8_t* d8 = reinterpret_cast<uint8_t*>(dst32);
+    for (uint32_t i = nvec * 16 + threadIdx.x; i < nbytes + 8; i += blockDim.x)
+        d8[i] = (i < nbytes) ? src[i] : 0;
+}
+
+// ------------------------------------------------------- phase 2: ranks
+__device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const uint16_t* rank_tab,
+                                     const uint32_t* ent_tab) {
+    const uint8_t* b8 = reinterpret_cast<const uint8_t*>(s.bytes32);
+    const uint32_t np = g.RE - g.Q0;
+    const uint32_t per = (np + kGenThreads - 1) / kGenThreads;
+    const uint32_t tid = threadIdx.x;
+    uint8_t* h = s.hist + tid;  // counts of value v at h[v * kGenThreads]
+    // clear own histogram
+    for (int v = 0; v < 256; v++) h[v * kGenThreads] = 0;
+    const uint32_t lo = tid * per, hi = min(np, lo + per);
+    const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
+    uint32_t e = 0;
+    for (uint32_t r = lo; r < hi; r++) {
+        const uint32_t o = g.Q0 + r;
+        if (o >= last) {
+            s.ranks[r] = 0;
+            continue;
+        }
+        if (r == lo) {
+            // entr64_init_int (entr64.cc:27-41) built incrementally
+            for (int k = 0; k < kWin; k++) {
+                const uint32_t v = b8[r + k];
+                const uint32_t c = h[v * kGenThreads];
+                e += ent_tab[c + 1] - ent_tab[c];
+                h[v * kGenThreads] = (uint8_t)(c + 1);
+            }
+        } else {
+            // entr64_inc_int (entr64.cc:47-71): byte r-1 leaves, r+63 enters
+            const uint32_t a = b8[r - 1], b = b8[r + 63];
+            if (a != b) {
+                const uint32_t ca = h[a * kGenThreads], cb = h[b * kGenThreads];
+                h[a * kGenThreads] = (uint8_t)(ca - 1);
+                h[b * kGenThreads] = (uint8_t)(cb + 1);
+                e = e - (ent_tab[ca] - ent_tab[ca - 1]) + (ent_tab[cb + 1] - ent_tab[cb]);
+            }
+        }
+        s.ranks[r] = rank_tab[e >> 10];
+    }
+}
+
+// ------------------------------------- phase 3: full-rescan result per step
+// For step k with rank[k] > 0 the full rescan of gen_chunk_scores picks the
+// smallest non-zero rank m of window [k, k+63], at its leftmost position f,
+// extended right over the run of equal ranks (capped at k+63).  Stored as
+// (m << 6) | (p - k); 0 when rank[k] == 0 (no credit, next step rescans).
+__device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
+    const uint32_t np = g.RE - g.Q0;
+    // run bits
+    const uint32_t nw = (np + 31) / 32;
+    for (uint32_t w = threadIdx.x / 32; w < nw; w += blockDim.x / 32) {
+        const uint32_t o = w * 32 + (threadIdx.x & 31);
+        const bool eq = (o + 1 < np) && s.ranks[o] == s.ranks[o + 1];
+        const uint32_t bits = __ballot_sync(0xffffffffu, eq);
+        if ((threadIdx.x & 31) == 0) s.eqw[w] = bits;
+    }
+    if (threadIdx.x < 4) s.eqw[nw + threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t nsteps = g.SE - g.Q0;
+    const uint32_t nblk = (nsteps + 63) / 64;
+    for (uint32_t j = threadIdx.x; j < nblk; j += blockDim.x) {
+        const uint32_t base = j * 64;
+        // prefix minima of the next aligned block (keys: rank<<6 | offset;
+        // rank 0 is "infinite" = 1023)
+        uint16_t pre[64];
+        uint32_t run = 0xFFFFu;
+#pragma unroll
+        for (int u = 0; u < 64; u++) {
+            const uint32_t o = base + 64 + u;
+            uint32_t r = (o < np) ? s.ranks[o] : 0;
+            const uint32_t key = ((r == 0 ? 1023u : r) << 6) | (uint32_t)u;
+            run = min(run, key);
+            pre[u] = (uint16_t)run;
+        }
+        uint32_t suf = 0xFFFFu;
+#pragma unroll
+        for (int u = 63; u >= 0; u--) {
+            const uint32_t k = base + u;
+            const uint32_t rk = (k < np) ? s.ranks[k] : 0;
+            suf = min(suf, ((rk == 0 ? 1023u : rk) << 6) | (uint32_t)u);
+            if (k < nsteps) {
+                uint16_t out = 0;
+                if (rk != 0) {
+                    uint32_t f, m;
+                    if (u == 0) {
+                        f = base + (suf & 63);
+                        m = suf >> 6;
+                    } else {
+                        const uint32_t pk = pre[u - 1];
+                        if ((suf >> 6) <= (pk >> 6)) {
+                            f = base + (suf & 63);
+                            m = suf >> 6;
+                        } else {
+                            f = base + 64 + (pk & 63);
+                            m = pk >> 6;
+                        }
+                    }
+                    // count trailing ones of the run bits starting at f
+                    const uint32_t w = f >> 5, sh = f & 31;
+                    const uint32_t b0 = s.eqw[w], b1 = s.eqw[w + 1], b2 = s.eqw[w + 2];
+                    const uint32_t lo32 = __funnelshift_r(b0, b1, sh);
+                    const uint32_t hi32 = __funnelshift_r(b1, b2, sh);
+                    const uint64_t bits = ((uint64_t)hi32 << 32) | lo32;
+                    const uint32_t runlen = (~bits == 0ull) ? 64u : (uint32_t)__ffsll((long long)~bits) - 1;
+                    uint32_t p = f + runlen;
+                    if (p > k + 63) p = k + 63;
+                    out = (uint16_t)((m << 6) | (p - k));
+                }
+                s.fres[k] = out;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------ phase 4: chains
+struct Credit {
+    uint32_t* score32;
+    uint32_t lo, hi;  // credited positions [lo, hi) (chunk-relative)
+    uint32_t cur, cnt;
+    int sign;
+    __device__ void flush() {
+        if (cnt && cur >= lo && cur < hi) {
+            const uint32_t o = cur - lo;
+            const uint32_t inc = cnt << (8 * (o & 3));
+            if (sign > 0) atomicAdd(&score32[o >> 2], inc);
+            else atomicSub(&score32[o >> 2], inc);
+        }
+        cnt = 0;
+    }
+    __device__ void add(uint32_t p) {
+        if (p != cur) {
+            flush();
+            cur = p;
+        }
+        cnt++;
+    }
+};
+
+// Walk steps [a, b).  If force_full, step a is a full rescan (speculative
+// start, or exact when a == 0).  Credits go to `cr` when non-null.
+__device__ inline ChainState walk(const TileGeom& g, const TileSmem& s, uint32_t a, uint32_t b, ChainState st,
+                                  bool force_full, Credit* cr) {
+    for (uint32_t i = a; i < b; i++) {
+        const uint32_t r64 = s.ranks[i + 64 - g.Q0];
+        const bool cheap = !(force_full && i == a) && i > 0 && st.M > 0 && r64 >= st.M && i < st.P;
+        if (cheap) {
+            if (r64 == st.M) st.P = i + 64;
+            if (cr) cr->add(st.P);
+        } else {
+            const uint32_t f = s.fres[i - g.Q0];
+            st.M = f >> 6;
+            st.P = i + (f & 63);
+            if (st.M && cr) cr->add(st.P);
+        }
+    }
+    return st;
+}
+
+__device__ inline bool same_state(uint64_t a, uint64_t b) { return a == b; }
+
+// Runs all phases for one tile.  entry != nullptr: the state entering step
+// S0 is known (re-computation after a failed link check); otherwise thread 0
+// starts speculatively kLead steps early.  Returns (in misc[0]) the number
+// of features, and writes sig_in / tau_out for the tile.
+__device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom& g, const TileSmem& s,
+                              const uint16_t* rank_tab, const uint32_t* ent_tab, const uint64_t* entry,
+                              uint64_t* sig_in, uint64_t* tau_out, uint32_t lead) {
+    load_bytes(chunk, g, s.bytes32);
+    __syncthreads();
+    compute_ranks(g, s, rank_tab, ent_tab);
+    __syncthreads();
+    compute_fres(g, s);
+    // clear scores (aliases the histogram area, free after phase 2)
+    for (uint32_t i = threadIdx.x; i < (g.L + 3) / 4 + 1; i += blockDim.x) s.score32[i] = 0;
+    __syncthreads();
+
+    if (threadIdx.x == 0) {
+        s.misc[9] = 0;
+        s.misc[10] = 0;
+        s.misc[11] = 0;
+    }
+    __syncthreads();
+    // segments over steps [S0, SE)
+    const uint32_t total = g.SE > g.S0 ? g.SE - g.S0 : 0;
+    const uint32_t SL = (total + kSegs - 1) / kSegs;
+    const uint32_t chk = g.t0 + g.L - 64;  // next tile's S0
+    const uint32_t t = threadIdx.x;
+    if (t < kSegs) {
+        const uint32_t St = g.S0 + t * SL;
+        const uint32_t Et = min(St + SL, g.SE);
+        if (SL > 0 && St < g.SE) {
+            ChainState st{0, 0};
+            bool force = true;
+            uint32_t start = St;
+            if (t == 0 && entry) {
+                st = unpack_state(*entry);
+                force = false;
+            } else {
+                // lead-in of `lead` steps (never below Q0, since lead <= kLead);
+                // starting at step 0 makes the walk exact
+                const uint32_t Ls = St > lead ? St - lead : 0;
+                st = walk(g, s, Ls, St, st, true, nullptr);
+                force = (Ls == St);
+                start = St;
+            }
+            s.sig[t] = pack_state(st);
+            Credit cr{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0, 1};
+            if (chk >= St && chk < Et) {
+                st = walk(g, s, start, chk, st, force, &cr);
+                s.misc[8] = (uint32_t)t;
+                *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(st);
+                st = walk(g, s, chk, Et, st, force && chk == start, &cr);
+            } else {
+                st = walk(g, s, start, Et, st, force, &cr);
+            }
+            cr.flush();
+            s.tau[t] = pack_state(st);
+        } else {
+            s.sig[t] = ~0ull;
+            s.tau[t] = ~0ull;
+        }
+    }
+    __syncthreads();
+    // phase 5: link segments inside the tile (serial, normally no work)
+    if (t == 0 && SL > 0) {
+        for (uint32_t q = 1; q < kSegs; q++) {
+            const uint32_t St = g.S0 + q * SL;
+            if (St >= g.SE) break;
+            const uint32_t Et = min(St + SL, g.SE);
+            if (same_state(s.sig[q], s.tau[q - 1])) continue;
+            // undo the speculative credits, redo from the true state
+            Credit un{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0, -1};
+            walk(g, s, St, Et, unpack_state(s.sig[q]), false, &un);
+            un.flush();
+            Credit re{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0, 1};
+            ChainState st = unpack_state(s.tau[q - 1]);
+            if (chk >= St && chk < Et) {
+                st = walk(g, s, St, chk, st, false, &re);
+                *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(st);
+                st = walk(g, s, chk, Et, st, false, &re);
+            } else {
+                st = walk(g, s, St, Et, st, false, &re);
+            }
+            re.flush();
+            s.sig[q] = s.tau[q - 1];
+            s.tau[q] = pack_state(st);
+            s.misc[9]++;
+        }
+        if (sig_in) *sig_in = s.sig[0];
+        if (tau_out) *tau_out = *reinterpret_cast<uint64_t*>(&s.misc[10]);
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------- phase 6: ordered compaction
+// Writes the positions (relative to t0) with score > thr (or >= thr when
+// ge) among [t0, t0+nown) into s.list in ascending order; returns count.
+__device__ uint32_t compact(const TileSmem& s, uint32_t nown, uint32_t thr, bool ge, uint32_t* tmp_counts) {
+    const uint32_t per = (nown + blockDim.x - 1) / blockDim.x;
+    const uint32_t lo = threadIdx.x * per, hi = min(nown, lo + per);
+    const uint8_t* sc = reinterpret_cast<const uint8_t*>(s.score32);
+    uint32_t c = 0;
+    for (uint32_t o = lo; o < hi; o++) {
+        const uint32_t v = sc[o];
+        c += ge ? (v >= thr) : (v > thr);
+    }
+    // block exclusive scan of c
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= (uint32_t)d) incl += y;
+    }
+    if (lane == 31) tmp_counts[wid] = incl;
+    __syncthreads();
+    uint32_t woff = 0, total = 0;
+    for (uint32_t w = 0; w < blockDim.x / 32; w++) {
+        if (w < wid) woff += tmp_counts[w];
+        total += tmp_counts[w];
+    }
+    uint32_t pos = woff + incl - c;
+    for (uint32_t o = lo; o < hi; o++) {
+        const uint32_t v = sc[o];
+        if (ge ? (v >= thr) : (v > thr)) s.list[pos++] = o;
+    }
+    __syncthreads();
+    return total;
+}
+
+// ---------------------------------------------------------- stream tiles
+__device__ inline TileGeom stream_geom(uint32_t n, uint32_t t0) {
+    TileGeom g;
+    g.n = n;
+    g.t0 = t0;
+    g.L = kTileL;
+    g.S0 = t0 >= 64 ? t0 - 64 : 0;
+    const uint32_t last = n - kWin;
+    g.SE = min(t0 + kTileL, last);
+    g.Q0 = g.S0 > kLead ? g.S0 - kLead : 0;
+    g.RE = min(g.SE + 64, n);
+    g.BE = min(g.RE + 63, n);
+    return g;
+}
+
+__device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64_t* entry, uint8_t* smem) {
+    const GenTile T = P.tiles[tile];
+    const GenChunk C = P.chunks[T.chunk];
+    const TileGeom g = stream_geom(C.n, T.t0);
+    TileSmem s = carve(smem, kTileL);
+    __shared__ uint16_t rank_tab[SDBF_RANK_BINS];
+    __shared__ uint32_t ent_tab[66];
+    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) rank_tab[i] = P.rank_tab[i];
+    for (uint32_t i = threadIdx.x; i < 66; i += blockDim.x) ent_tab[i] = i < 65 ? P.ent_tab[i] : 0;
+    __syncthreads();
+    TileOut* out = P.tile_out + tile;
+    tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, entry, &out->sig_in, &out->tau_out, P.lead);
+    const uint32_t nown = g.SE > g.t0 ? g.SE - g.t0 : 0;
+    __shared__ uint32_t counts[kGenThreads / 32];
+    const uint32_t nf = compact(s, nown, kThreshold, false, counts);
+    // SHA-1 of each selected feature (sdbf_core.cc:103-105)
+    uint32_t* feat = P.features + (size_t)tile * 5 * kTileCap;
+    const uint32_t off = g.t0 - g.Q0;
+    for (uint32_t f = threadIdx.x; f < nf; f += blockDim.x) {
+        const uint32_t p = s.list[f] + off;
+        uint32_t w[16], h[5];
+        load_be16(s.bytes32, p, w);
+        sha1_feature(w, h);
+#pragma unroll
+        for (int k = 0; k < 5; k++) feat[k * kTileCap + f] = h[k];
+    }
+    if (threadIdx.x == 0) {
+        out->count = nf;
+        out->fixups = s.misc[9];
+    }
+}
+
+__global__ void __launch_bounds__(kGenThreads) k_stream_tiles(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    for (uint32_t tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+        stream_tile_body(P, tile, nullptr, smem);
+        __syncthreads();
+    }
+}
+
+// One CTA per chunk: link tiles; recompute a tile whose speculative entry
+// state differs from its predecessor's exit state.
+__global__ void __launch_bounds__(kGenThreads) k_stream_verify(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint64_t entry;
+    __shared__ int redo;
+    for (uint32_t c = blockIdx.x; c < P.nchunks; c += gridDim.x) {
+        const GenChunk C = P.chunks[c];
+        for (uint32_t j = 1; j < C.ntiles; j++) {
+            const uint32_t tile = C.first_tile + j;
+            if (threadIdx.x == 0) {
+                const uint64_t prev = P.tile_out[tile - 1].tau_out;
+                const uint64_t mine = P.tile_out[tile].sig_in;
+                // a tile whose lead-in reaches step 0 is exact by construction
+                const TileGeom g = stream_geom(C.n, P.tiles[tile].t0);
+                redo = (g.S0 > P.lead) && (prev != mine);
+                entry = prev;
+            }
+            __syncthreads();
+            if (redo) {
+                stream_tile_body(P, tile, &entry, smem);
+                if (threadIdx.x == 0) atomicAdd(P.counters + 0, 1u);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ------------------------------------------------------- ordered commit
+// Per-warp shared state for the stream commit.
+struct CommitSmem {
+    uint32_t F[64];        // current 256-byte filter
+    uint32_t G[kBigBytes / 4];  // current 16 KiB big filter
+    uint32_t dup[2][192];  // values seen twice in a group (F, G)
+    uint32_t ndup[2];
+};
+
+__device__ inline uint32_t lanemask_le() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_le;" : "=r"(m));
+    return m;
+}
+
+// Insert the group's bits into bitmap `bm` for lanes in `act`; returns for
+// each lane a mask over its 5 values of "new relative to everything before
+// this lane in lane order".  flipped[k] records bits this lane turned on.
+template <int kKind>
+__device__ inline uint32_t group_insert(uint32_t* bm, uint32_t* dup, uint32_t* ndup, bool act, const uint32_t (&idx)[5],
+                                        uint32_t& flipped) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t pre = 0;  // bit k: value k was already set before the group
+    if (act) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) pre |= ((bm[idx[k] >> 5] >> (idx[k] & 31)) & 1u) << k;
+    }
+    __syncwarp();
+    flipped = 0;
+    if (act) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            if (!((pre >> k) & 1u)) {
+                const uint32_t bit = 1u << (idx[k] & 31);
+                const uint32_t old = atomicOr(&bm[idx[k] >> 5], bit);
+                if (old & bit) {
+                    // set earlier within this group (by another lane or by an
+                    // equal value of this lane): resolve order below
+                    const uint32_t slot = atomicAdd(ndup, 1u);
+                    if (slot < 192) dup[slot] = idx[k];
+                } else {
+                    flipped |= 1u << k;
+                }
+            }
+        }
+    }
+    __syncwarp();
+    uint32_t fresh = act ? (~pre & 31u) : 0u;  // candidates for "new"
+    const uint32_t nd = min(*ndup, 192u);
+    for (uint32_t e = 0; e < nd; e++) {
+        const uint32_t v = dup[e];
+        uint32_t mine = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) mine |= ((fresh >> k) & 1u && idx[k] == v) ? (1u << k) : 0u;
+        const uint32_t holders = __ballot_sync(0xffffffffu, mine != 0);
+        const uint32_t first = __ffs(holders) - 1;
+        if (mine) {
+            // the first lane (in lane order) owns v at its lowest k; every
+            // other occurrence of v is not new
+            if (lane == first) {
+                const uint32_t keep = mine & (~mine + 1u);  // lowest set bit
+                fresh &= ~(mine & ~keep);
+            } else {
+                fresh &= ~mine;
+            }
+        }
+    }
+    __syncwarp();
+    if (lane == 0) *ndup = 0;
+    __syncwarp();
+    (void)kKind;
+    return fresh;
+}
+
+__device__ inline void undo_bits(uint32_t* bm, const uint32_t (&idx)[5], uint32_t flipped) {
+#pragma unroll
+    for (int k = 0; k < 5; k++)
+        if ((flipped >> k) & 1u) atomicAnd(&bm[idx[k] >> 5], ~(1u << (idx[k] & 31)));
+}
+
+__device__ inline void set_bits(uint32_t* bm, const uint32_t (&idx)[5]) {
+#pragma unroll
+    for (int k = 0; k < 5; k++) atomicOr(&bm[idx[k] >> 5], 1u << (idx[k] & 31));
+}
+
+__global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    CommitSmem& S = reinterpret_cast<CommitSmem*>(smem)[wid];
+    for (uint32_t fi = blockIdx.x * kCommitWarps + wid; fi < P.nfiles; fi += gridDim.x * kCommitWarps) {
+        const uint32_t file = P.file_order[fi];
+        const GenFile Fd = P.files[file];
+        if (Fd.nchunks == 0) continue;
+        uint32_t* out = P.out_filters + (size_t)Fd.filter_base * 64;
+        for (uint32_t i = lane; i < 64; i += 32) S.F[i] = 0;
+        for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
+        if (lane == 0) S.ndup[0] = S.ndup[1] = 0;
+        __syncwarp();
+        uint32_t bf_count = 1, last_count = 0;
+        for (uint32_t c = Fd.first_chunk; c < Fd.first_chunk + Fd.nchunks; c++) {
+            const GenChunk C = P.chunks[c];
+            uint32_t bigfi = 0;  // local to each chunk (sdbf_core.cc:100)
+            for (uint32_t tj = 0; tj < C.ntiles; tj++) {
+                const uint32_t tile = C.first_tile + tj;
+                const uint32_t nf = P.tile_out[tile].count;
+                const uint32_t* feat = P.features + (size_t)tile * 5 * kTileCap;
+                for (uint32_t g0 = 0; g0 < nf; g0 += 32) {
+                    const uint32_t gi = g0 + lane;
+                    const bool have = gi < nf;
+                    uint32_t hw[5], a[5], b[5];
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        hw[k] = have ? feat[k * kTileCap + gi] : 0;
+                        a[k] = hw[k] & kBfMask;
+                        b[k] = hw[k] & kBigMask;
+                    }
+                    uint32_t start = 0;
+                    while (true) {
+                        const bool act = have && lane >= start;
+                        if (!__any_sync(0xffffffffu, act)) break;
+                        uint32_t flF, flG;
+                        const uint32_t fnew = group_insert<0>(S.F, S.dup[0], &S.ndup[0], act, a, flF);
+                        const bool fpass = act && fnew != 0;
+                        const uint32_t gnew = group_insert<1>(S.G, S.dup[1], &S.ndup[1], fpass, b, flG);
+                        const bool counted = fpass && gnew != 0;
+                        const uint32_t cm = __ballot_sync(0xffffffffu, counted);
+                        const uint32_t before = __popc(cm & lanemask_le());
+                        // first lane at which a counter reaches its cap
+                        const bool hit_small = counted && (last_count + before == (uint32_t)kMaxElem);
+                        const bool hit_big = counted && (bigfi + before == (uint32_t)kBigElem);
+                        const uint32_t hm = __ballot_sync(0xffffffffu, hit_small || hit_big);
+                        if (hm == 0) {
+                            last_count += __popc(cm);
+                            bigfi += __popc(cm);
+                            break;
+                        }
+                        const uint32_t r = __ffs(hm) - 1;
+                        const bool roll_small = __shfl_sync(0xffffffffu, hit_small, r);
+                        const bool roll_big = __shfl_sync(0xffffffffu, hit_big, r);
+                        // lanes after r are re-processed: take their bits back,
+                        // then restore bits of lanes <= r that share them
+                        if (act && lane > r) {
+                            undo_bits(S.F, a, flF);
+                            if (fpass) undo_bits(S.G, b, flG);
+                        }
+                        __syncwarp();
+                        if (act && lane <= r) {
+                            set_bits(S.F, a);
+                            if (fpass) set_bits(S.G, b);
+                        }
+                        __syncwarp();
+                        const uint32_t ncnt = __popc(cm & ((2u << r) - 1u));
+                        last_count += ncnt;
+                        bigfi += ncnt;
+                        if (roll_small) {
+                            // filter full: emit and start the next one
+                            const bool fits = bf_count <= Fd.filter_cap;
+                            for (uint32_t i = lane; i < 64; i += 32) {
+                                if (fits) out[(size_t)(bf_count - 1) * 64 + i] = S.F[i];
+                                S.F[i] = 0;
+                            }
+                            if (!fits && lane == 0) atomicAdd(P.counters + 1, 1u);
+                            bf_count++;
+                            last_count = 0;
+                        }
+                        if (roll_big) {
+                            for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
+                            bigfi = 0;
+                        }
+                        __syncwarp();
+                        start = r + 1;
+                    }
+                }
+            }
+        }
+        // emit the current (last) filter, then the chop of sdbf_core.cc:235-238
+        if (bf_count <= Fd.filter_cap) {
+            for (uint32_t i = lane; i < 64; i += 32) out[(size_t)(bf_count - 1) * 64 + i] = S.F[i];
+        } else if (lane == 0) {
+            atomicAdd(P.counters + 1, 1u);
+        }
+        if (bf_count > 1 && last_count < (uint32_t)kMaxElem / 8) {
+            bf_count--;
+            last_count = kMaxElem;
+        }
+        if (lane == 0) {
+            P.out_info[file].bf_count = bf_count;
+            P.out_info[file].last_count = last_count;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------ block mode
+__device__ inline TileGeom block_geom(uint32_t n) {
+    TileGeom g;
+    g.n = n;
+    g.t0 = 0;
+    g.S0 = 0;
+    g.Q0 = 0;
+    g.SE = n - kWin;
+    g.L = n - kWin;
+    g.RE = n;
+    g.BE = n;
+    return g;
+}
+
+__global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint16_t rank_tab[SDBF_RANK_BINS];
+    __shared__ uint32_t ent_tab[66];
+    __shared__ uint32_t histo[66];
+    __shared__ uint32_t counts[kGenThreads / 32];
+    __shared__ uint32_t filt[64];
+    __shared__ uint32_t hsh[kGenThreads][5];
+    __shared__ int state[4];  // k, allowed, hashed, done
+    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) rank_tab[i] = P.rank_tab[i];
+    for (uint32_t i = threadIdx.x; i < 66; i += blockDim.x) ent_tab[i] = i < 65 ? P.ent_tab[i] : 0;
+    __syncthreads();
+    TileSmem s = carve(smem, P.block_lmax);
+    for (uint32_t b = blockIdx.x; b < P.nchunks; b += gridDim.x) {
+        const GenChunk C = P.chunks[b];
+        const TileGeom g = block_geom(C.n);
+        tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, nullptr, nullptr, nullptr, P.lead);
+        const uint8_t* sc = reinterpret_cast<const uint8_t*>(s.score32);
+        const uint32_t nown = g.SE;
+        if (threadIdx.x < 66) histo[threadIdx.x] = 0;
+        if (threadIdx.x < 64) filt[threadIdx.x] = 0;
+        __syncthreads();
+        if (C.kind == 0) {
+            for (uint32_t o = threadIdx.x; o < nown; o += blockDim.x) atomicAdd(&histo[sc[o]], 1u);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                // thresholding of thread_gen_block_sdbf (sdbf_core.cc:271-276);
+                // k may end at 15 when the loop does not break
+                int k = 65;
+                uint32_t sum = 0;
+                for (; k >= kThreshold; k--) {
+                    if (sum <= (uint32_t)kMaxElemDD && sum + histo[k] > (uint32_t)kMaxElemDD) break;
+                    sum += histo[k];
+                }
+                state[0] = k;
+                state[1] = kMaxElemDD - (int)sum;
+            }
+        } else if (threadIdx.x == 0) {
+            state[0] = kThreshold;  // tail block (sdbf_core.cc:315)
+            state[1] = kMaxElemDD;
+        }
+        if (threadIdx.x == 0) {
+            state[2] = 0;
+            state[3] = 0;
+        }
+        __syncthreads();
+        const uint32_t k = (uint32_t)state[0];
+        const uint32_t ncand = compact(s, nown, k, true, counts);
+        for (uint32_t base = 0; base < ncand; base += blockDim.x) {
+            if (state[3]) break;
+            const uint32_t ci = base + threadIdx.x;
+            if (ci < ncand) {
+                const uint32_t p = s.list[ci];
+                uint32_t w[16], h[5];
+                load_be16(s.bytes32, p, w);
+                sha1_feature(w, h);
+#pragma unroll
+                for (int q = 0; q < 5; q++) hsh[threadIdx.x][q] = h[q];
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                // gen_block_hash ordered insert (sdbf_core.cc:157-183)
+                int allowed = state[1];
+                int hashed = state[2];
+                const uint32_t lim = min(ncand - base, (uint32_t)blockDim.x);
+                for (uint32_t q = 0; q < lim && hashed < kMaxElemDD; q++) {
+                    const uint32_t v = sc[s.list[base + q]];
+                    if (!(v > k || (v == k && allowed > 0))) continue;
+                    uint32_t added = 0;
+                    for (int z = 0; z < 5; z++) {
+                        const uint32_t idx = hsh[q][z] & kBfMask;
+                        const uint32_t bit = 1u << (idx & 31);
+                        if (!(filt[idx >> 5] & bit)) added++;
+                        filt[idx >> 5] |= bit;
+                    }
+                    if (!added) continue;
+                    hashed++;
+                    if (v == k) allowed--;
+                }
+                state[1] = allowed;
+                state[2] = hashed;
+                if (hashed >= kMaxElemDD) state[3] = 1;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x < 64) P.out_filters[(size_t)C.filter * 64 + threadIdx.x] = filt[threadIdx.x];
+        if (threadIdx.x == 0) P.out_counts[C.filter] = (uint16_t)state[2];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- launch
+size_t stream_tile_smem() { return tile_smem_bytes(kTileL); }
+size_t block_smem(uint32_t lmax) { return tile_smem_bytes(lmax); }
+
+cudaError_t launch_stream(const GenParams& P, uint32_t grid_tiles, uint32_t grid_chunks, uint32_t grid_commit,
+                          cudaStream_t st) {
+    static bool attr = false;
+    const size_t sm = stream_tile_smem();
+    if (!attr) {
+        cudaFuncSetAttribute(k_stream_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_stream_verify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_stream_commit, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(CommitSmem) * kCommitWarps));
+        attr = true;
+    }
+    if (P.ntiles) k_stream_tiles<<<grid_tiles, kGenThreads, sm, st>>>(P);
+    if (P.nchunks) k_stream_verify<<<grid_chunks, kGenThreads, sm, st>>>(P);
+    if (P.nfiles) k_stream_commit<<<grid_commit, kCommitWarps * 32, sizeof(CommitSmem) * kCommitWarps, st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    const size_t sm = block_smem(P.block_lmax);
+    cudaFuncSetAttribute(k_block_digest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (P.nchunks) k_block_digest<<<grid, kGenThreads, sm, st>>>(P);
+    return cudaGetLastError();
+}
+
+}  // namespace sdbfg

@@ -1,0 +1,83 @@
+// gen_kernels.h -- work descriptors shared by the host orchestration
+// (sdbf_api.cu) and the generation kernels (gen_kernels.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sdbfg {
+
+constexpr int kGenThreads = 128;     // CTA size of the tile / block kernels
+constexpr int kSegs = 64;            // popularity-chain segments per tile
+constexpr uint32_t kLead = 128;      // speculative lead-in steps per segment
+constexpr uint32_t kTileL = 8192;    // window steps owned by a stream tile
+// at most one selected feature per 17 credited steps (score > 16), and a
+// tile's positions are credited by kTileL + 64 steps
+constexpr uint32_t kTileCap = (kTileL + 64) / 17 + 2;
+constexpr int kCommitWarps = 4;      // files per commit CTA
+constexpr uint32_t kMaxBlockBytes = 16384;  // dd block size limit (sdhash.cc:215-219)
+constexpr uint64_t kChunkBytes = 32ull << 20;  // stream chunk (sdbf_class.cc:43)
+
+// One 32 MiB stream chunk (or the tail of a file), or one dd block.
+struct GenChunk {
+    uint64_t data_off;    // byte offset of the chunk in the batch buffer (16-aligned for stream)
+    uint32_t n;           // bytes
+    uint32_t file;        // owning file
+    uint32_t first_tile;  // stream: first tile id
+    uint32_t ntiles;      // stream: tiles of this chunk
+    uint32_t filter;      // block: output filter index
+    uint32_t kind;        // block: 0 full block (histogram threshold), 1 tail (16 / 192)
+};
+
+struct GenTile {
+    uint32_t chunk;
+    uint32_t t0;  // first owned step (multiple of kTileL)
+};
+
+struct GenFile {
+    uint32_t first_chunk;
+    uint32_t nchunks;
+    uint64_t filter_base;  // first output filter slot of this file
+    uint64_t filter_cap;   // slots reserved for it ((len >> 11) + 1)
+};
+
+struct TileOut {
+    uint64_t sig_in;   // speculative chain state entering step t0-64
+    uint64_t tau_out;  // chain state entering step t0+kTileL-64
+    uint32_t count;    // features selected in the tile
+    uint32_t fixups;   // segments re-walked inside the tile
+};
+
+struct FileInfoDev {
+    uint32_t bf_count;
+    uint32_t last_count;
+};
+
+struct GenParams {
+    const uint8_t* data;
+    const GenChunk* chunks;
+    uint32_t nchunks;
+    const GenTile* tiles;
+    uint32_t ntiles;
+    const GenFile* files;
+    const uint32_t* file_order;  // commit order (largest first)
+    uint32_t nfiles;
+    TileOut* tile_out;
+    uint32_t* features;          // [tile][5][kTileCap]
+    uint32_t* out_filters;       // 64 words per filter
+    uint16_t* out_counts;        // block mode: elements per filter
+    FileInfoDev* out_info;       // stream mode: per file
+    uint32_t* counters;          // [0] tiles recomputed by the link check, [1] capacity overflows
+    const uint16_t* rank_tab;    // device copy of SDBF_ENTR64_RANKS
+    const uint32_t* ent_tab;     // device copy of SDBF_ENTROPY64
+    uint32_t block_lmax;         // block mode: max window steps per block
+    uint32_t lead;               // speculative lead-in steps (<= kLead)
+};
+
+size_t stream_tile_smem();
+size_t block_smem(uint32_t lmax);
+cudaError_t launch_stream(const GenParams& P, uint32_t grid_tiles, uint32_t grid_chunks, uint32_t grid_commit,
+                          cudaStream_t st);
+cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st);
+
+}  // namespace sdbfg

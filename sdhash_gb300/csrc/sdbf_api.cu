@@ -1,0 +1,716 @@
+// sdbf_api.cu -- host orchestration behind the C ABI (include/sdbf_gb300.h).
+//
+// Owns device memory, builds the chunk / tile / file work lists for a batch,
+// launches the generation and comparison kernels and moves results back.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sdbf_gb300.h"
+#include "compare_kernels.h"
+#include "gen_kernels.h"
+#include "sdbf_tables.h"
+
+using namespace sdbfg;
+
+namespace {
+
+constexpr uint32_t kMaxTilesPerLaunch = 1u << 18;  // 2 GiB of stream input per launch group
+constexpr uint64_t kMaxBytesPerLaunch = 2ull << 30;
+constexpr uint32_t kMinFile = 512;                 // MIN_FILE_SIZE (sdbf_defines.h:56)
+constexpr uint64_t kPairsPerLaunch = 1ull << 22;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        const size_t want = std::max(bytes, cap + cap / 2);
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+struct HostBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMallocHost(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct sdbfg_ctx {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t launches = 0;
+    int sms = 152;
+    uint32_t lead = kLead;
+    // constant tables
+    DevBuf d_rank, d_ent, d_cut;
+    // generation buffers
+    DevBuf d_data, d_chunks, d_tiles, d_files, d_order, d_tile_out, d_features, d_work_filters, d_info, d_counters,
+        d_pack_src, d_pack_dst_off, d_out_filters, d_out_counts;
+    HostBuf h_stage;
+    // comparison buffers
+    DevBuf d_pairs, d_scores;
+};
+
+struct sdbfg_set {
+    sdbfg_ctx* ctx = nullptr;
+    uint32_t n = 0;
+    std::vector<std::string> names;
+    std::vector<uint32_t> bf_count;
+    std::vector<uint32_t> last_elem;  // element count of the last filter (swap rule)
+    DevBuf d_filters, d_meta, d_digests;
+};
+
+static int fail(sdbfg_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                       \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? SDBFG_ERR_NOMEM : SDBFG_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);    \
+    } while (0)
+
+// ------------------------------------------------------------------ context
+extern "C" int sdbfg_ctx_create(int device, sdbfg_ctx** out) {
+    if (!out) return SDBFG_ERR_ARG;
+    *out = nullptr;
+    auto* c = new sdbfg_ctx();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        delete c;
+        return SDBFG_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return SDBFG_ERR_CUDA;
+    }
+    c->stream = c->own;
+    uint32_t ent[65];
+    for (int i = 0; i < 65; i++) ent[i] = SDBF_ENTROPY64[i];
+    if (c->d_rank.ensure(sizeof(SDBF_ENTR64_RANKS)) || c->d_ent.ensure(sizeof(ent)) ||
+        c->d_cut.ensure(sizeof(SDBF_CUTOFFS256)) || c->d_counters.ensure(64)) {
+        sdbfg_ctx_destroy(c);
+        return SDBFG_ERR_NOMEM;
+    }
+    cudaMemcpy(c->d_rank.p, SDBF_ENTR64_RANKS, sizeof(SDBF_ENTR64_RANKS), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_ent.p, ent, sizeof(ent), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_cut.p, SDBF_CUTOFFS256, sizeof(SDBF_CUTOFFS256), cudaMemcpyHostToDevice);
+    cudaMemset(c->d_counters.p, 0, 64);
+    *out = c;
+    return SDBFG_OK;
+}
+
+extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    for (DevBuf* b : {&c->d_rank, &c->d_ent, &c->d_cut, &c->d_data, &c->d_chunks, &c->d_tiles, &c->d_files,
+                      &c->d_order, &c->d_tile_out, &c->d_features, &c->d_work_filters, &c->d_info,
+                      &c->d_counters, &c->d_pack_src, &c->d_pack_dst_off, &c->d_out_filters, &c->d_out_counts,
+                      &c->d_pairs, &c->d_scores})
+        b->release();
+    c->h_stage.release();
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+}
+
+extern "C" const char* sdbfg_last_error(const sdbfg_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+extern "C" int sdbfg_ctx_set_stream(sdbfg_ctx* c, void* s) {
+    if (!c) return SDBFG_ERR_ARG;
+    c->stream = s ? static_cast<cudaStream_t>(s) : c->own;
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_ctx_synchronize(sdbfg_ctx* c) {
+    if (!c) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return SDBFG_OK;
+}
+
+extern "C" uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx* c) { return c ? c->launches : 0; }
+
+extern "C" int sdbfg_ctx_set_lead(sdbfg_ctx* c, uint32_t steps) {
+    if (!c || steps > kLead) return SDBFG_ERR_ARG;
+    c->lead = steps;
+    return SDBFG_OK;
+}
+
+extern "C" uint64_t sdbfg_ctx_relinked_tiles(sdbfg_ctx* c) {
+    if (!c) return 0;
+    uint32_t v = 0;
+    cudaMemcpy(&v, c->d_counters.p, 4, cudaMemcpyDeviceToHost);
+    return v;
+}
+
+// ------------------------------------------------------------- generation
+static uint64_t stream_cap(uint64_t len) { return (len >> 11) + 1; }
+static uint64_t block_count(uint64_t len, uint32_t B) { return len / B + ((len % B) >= kMinFile ? 1 : 0); }
+
+extern "C" uint64_t sdbfg_digest_capacity(const uint64_t* lens, uint32_t n, uint32_t dd) {
+    uint64_t s = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        if (lens[i] < kMinFile) continue;
+        s += dd ? block_count(lens[i], dd) : stream_cap(lens[i]);
+    }
+    return s;
+}
+
+// Packs each file's filters from the generation workspace to its final slot.
+__global__ void k_pack_filters(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                               const uint64_t* __restrict__ src_off, const uint64_t* __restrict__ dst_off,
+                               const FileInfoDev* __restrict__ info, const uint32_t* __restrict__ ids, uint32_t n) {
+    for (uint32_t f = blockIdx.x; f < n; f += gridDim.x) {
+        const uint32_t id = ids[f];
+        const uint64_t words = (uint64_t)info[id].bf_count * 64;
+        const uint4* s = reinterpret_cast<const uint4*>(src + src_off[f] * 64);
+        uint4* d = reinterpret_cast<uint4*>(dst + dst_off[f] * 64);
+        for (uint64_t q = threadIdx.x; q < words / 4; q += blockDim.x) d[q] = s[q];
+    }
+}
+
+namespace {
+
+struct Group {  // consecutive inputs processed by one launch sequence
+    uint32_t first, count;
+};
+
+// Splits inputs into launch groups bounded by tiles (stream) or bytes.
+std::vector<Group> make_groups(const uint64_t* lens, uint32_t n, uint32_t dd) {
+    std::vector<Group> gs;
+    uint32_t start = 0;
+    uint64_t tiles = 0, bytes = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        uint64_t t = 0;
+        if (!dd && lens[i] >= kMinFile) {
+            for (uint64_t pos = 0; pos < lens[i]; pos += kChunkBytes) {
+                const uint64_t m = std::min<uint64_t>(kChunkBytes, lens[i] - pos);
+                if (m > 64) t += (m - 64 + kTileL - 1) / kTileL;
+            }
+        }
+        const uint64_t b = (lens[i] + 15) & ~15ull;
+        if (i > start && (tiles + t > kMaxTilesPerLaunch || bytes + b > kMaxBytesPerLaunch)) {
+            gs.push_back({start, i - start});
+            start = i;
+            tiles = 0;
+            bytes = 0;
+        }
+        tiles += t;
+        bytes += b;
+    }
+    if (n > start) gs.push_back({start, n - start});
+    return gs;
+}
+
+}  // namespace
+
+// Core: inputs for files [g.first, g.first+g.count) are in device memory at
+// dev_base + dev_off[i].  Writes packed filters to dev_out (+ counts) at the
+// offsets in results[] (already assigned for block mode, assigned here for
+// stream mode starting at *next_slot).
+static int digest_group_device(sdbfg_ctx* c, const uint8_t* dev_base, const std::vector<uint64_t>& dev_off,
+                               const uint64_t* lens, const Group& g, uint32_t dd, uint32_t* dev_out,
+                               uint16_t* dev_counts, sdbfg_digest_result* res, uint64_t* next_slot,
+                               uint64_t out_cap) {
+    cudaStream_t st = c->stream;
+    GenParams P{};
+    P.data = dev_base;
+    P.rank_tab = c->d_rank.as<uint16_t>();
+    P.ent_tab = c->d_ent.as<uint32_t>();
+    P.counters = c->d_counters.as<uint32_t>();
+    P.lead = c->lead;
+    if (dd) {
+        std::vector<GenChunk> chunks;
+        uint32_t lmax = 0;
+        for (uint32_t k = 0; k < g.count; k++) {
+            const uint32_t i = g.first + k;
+            if (lens[i] < kMinFile) continue;
+            const uint64_t qt = lens[i] / dd, rem = lens[i] % dd;
+            uint64_t slot = res[i].filter_offset;
+            for (uint64_t b = 0; b < qt; b++) {
+                chunks.push_back({dev_off[k] + b * dd, dd, i, 0, 0, (uint32_t)(slot + b), 0});
+                lmax = std::max<uint32_t>(lmax, dd - 64);
+            }
+            if (rem >= kMinFile) {
+                chunks.push_back({dev_off[k] + qt * dd, (uint32_t)rem, i, 0, 0, (uint32_t)(slot + qt), 1});
+                lmax = std::max<uint32_t>(lmax, (uint32_t)rem - 64);
+            }
+        }
+        if (chunks.empty()) return SDBFG_OK;
+        CUDA_TRY(c, c->d_chunks.ensure(chunks.size() * sizeof(GenChunk)));
+        CUDA_TRY(c, cudaMemcpyAsync(c->d_chunks.p, chunks.data(), chunks.size() * sizeof(GenChunk),
+                                    cudaMemcpyHostToDevice, st));
+        P.chunks = c->d_chunks.as<GenChunk>();
+        P.nchunks = (uint32_t)chunks.size();
+        P.out_filters = dev_out;
+        P.out_counts = dev_counts;
+        P.block_lmax = (lmax + 63) / 64 * 64;
+        const uint32_t grid = (uint32_t)std::min<size_t>(chunks.size(), (size_t)c->sms * 2 * 8);
+        CUDA_TRY(c, launch_block(P, grid, st));
+        c->launches += 1;
+        // the chunk table must outlive the async copy
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        return SDBFG_OK;
+    }
+    // ---- stream mode
+    std::vector<GenChunk> chunks;
+    std::vector<GenTile> tiles;
+    std::vector<GenFile> files(g.count);
+    std::vector<uint64_t> work_base(g.count);
+    uint64_t work_slots = 0;
+    for (uint32_t k = 0; k < g.count; k++) {
+        const uint32_t i = g.first + k;
+        GenFile f{(uint32_t)chunks.size(), 0, work_slots, 0};
+        if (lens[i] >= kMinFile) {
+            for (uint64_t pos = 0; pos < lens[i]; pos += kChunkBytes) {
+                const uint32_t m = (uint32_t)std::min<uint64_t>(kChunkBytes, lens[i] - pos);
+                GenChunk ch{dev_off[k] + pos, m, k, (uint32_t)tiles.size(), 0, 0, 0};
+                if (m > 64) {
+                    for (uint32_t t0 = 0; t0 < m - 64; t0 += kTileL) tiles.push_back({(uint32_t)chunks.size(), t0});
+                }
+                ch.ntiles = (uint32_t)tiles.size() - ch.first_tile;
+                chunks.push_back(ch);
+                f.nchunks++;
+            }
+            work_base[k] = work_slots;
+            f.filter_cap = stream_cap(lens[i]);
+            work_slots += f.filter_cap;
+        }
+        files[k] = f;
+    }
+    std::vector<uint32_t> order(g.count);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return lens[g.first + a] > lens[g.first + b]; });
+    CUDA_TRY(c, c->d_chunks.ensure(std::max<size_t>(1, chunks.size()) * sizeof(GenChunk)));
+    CUDA_TRY(c, c->d_tiles.ensure(std::max<size_t>(1, tiles.size()) * sizeof(GenTile)));
+    CUDA_TRY(c, c->d_files.ensure(files.size() * sizeof(GenFile)));
+    CUDA_TRY(c, c->d_order.ensure(order.size() * sizeof(uint32_t) * 2));
+    CUDA_TRY(c, c->d_tile_out.ensure(std::max<size_t>(1, tiles.size()) * sizeof(TileOut)));
+    CUDA_TRY(c, c->d_features.ensure(std::max<size_t>(1, tiles.size()) * 5ull * kTileCap * 4));
+    CUDA_TRY(c, c->d_work_filters.ensure(std::max<uint64_t>(1, work_slots) * 256));
+    CUDA_TRY(c, c->d_info.ensure(files.size() * sizeof(FileInfoDev)));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_chunks.p, chunks.data(), chunks.size() * sizeof(GenChunk),
+                                cudaMemcpyHostToDevice, st));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_tiles.p, tiles.data(), tiles.size() * sizeof(GenTile), cudaMemcpyHostToDevice,
+                                st));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_files.p, files.data(), files.size() * sizeof(GenFile), cudaMemcpyHostToDevice,
+                                st));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_order.p, order.data(), order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                st));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_info.p, 0, files.size() * sizeof(FileInfoDev), st));
+    P.chunks = c->d_chunks.as<GenChunk>();
+    P.nchunks = (uint32_t)chunks.size();
+    P.tiles = c->d_tiles.as<GenTile>();
+    P.ntiles = (uint32_t)tiles.size();
+    P.files = c->d_files.as<GenFile>();
+    P.file_order = c->d_order.as<uint32_t>();
+    P.nfiles = g.count;
+    P.tile_out = c->d_tile_out.as<TileOut>();
+    P.features = c->d_features.as<uint32_t>();
+    P.out_filters = c->d_work_filters.as<uint32_t>();
+    P.out_info = c->d_info.as<FileInfoDev>();
+    const uint32_t grid_tiles = (uint32_t)std::min<size_t>(tiles.size(), (size_t)c->sms * 3 * 16);
+    const uint32_t grid_chunks = (uint32_t)std::min<size_t>(chunks.size(), (size_t)c->sms * 3 * 16);
+    const uint32_t grid_commit =
+        (uint32_t)std::min<size_t>((g.count + kCommitWarps - 1) / kCommitWarps, (size_t)c->sms * 3 * 16);
+    CUDA_TRY(c, launch_stream(P, std::max(1u, grid_tiles), std::max(1u, grid_chunks), std::max(1u, grid_commit), st));
+    c->launches += (P.ntiles ? 1 : 0) + (P.nchunks ? 1 : 0) + (P.nfiles ? 1 : 0);
+    // per-file results
+    std::vector<FileInfoDev> info(g.count);
+    CUDA_TRY(c, cudaMemcpyAsync(info.data(), c->d_info.p, info.size() * sizeof(FileInfoDev), cudaMemcpyDeviceToHost,
+                                st));
+    uint32_t flags[2] = {0, 0};
+    CUDA_TRY(c, cudaMemcpyAsync(flags, c->d_counters.p, sizeof flags, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (flags[1]) return fail(c, SDBFG_ERR_CUDA, "internal error: stream digest exceeded its filter bound");
+    std::vector<uint64_t> src_off, dst_off;
+    std::vector<uint32_t> ids;
+    for (uint32_t k = 0; k < g.count; k++) {
+        const uint32_t i = g.first + k;
+        if (lens[i] < kMinFile) continue;
+        res[i].bf_count = info[k].bf_count;
+        res[i].last_count = info[k].last_count;
+        res[i].filter_offset = *next_slot;
+        src_off.push_back(work_base[k]);
+        dst_off.push_back(*next_slot);
+        ids.push_back(k);
+        *next_slot += info[k].bf_count;
+    }
+    if (*next_slot > out_cap) return fail(c, SDBFG_ERR_CAPACITY, "output capacity %llu filters < %llu needed",
+                                          (unsigned long long)out_cap, (unsigned long long)*next_slot);
+    if (!ids.empty()) {
+        CUDA_TRY(c, c->d_pack_src.ensure(ids.size() * 8 * 2 + ids.size() * 4));
+        uint64_t* d_src = c->d_pack_src.as<uint64_t>();
+        uint64_t* d_dst = d_src + ids.size();
+        uint32_t* d_ids = reinterpret_cast<uint32_t*>(d_dst + ids.size());
+        CUDA_TRY(c, cudaMemcpyAsync(d_src, src_off.data(), ids.size() * 8, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(d_dst, dst_off.data(), ids.size() * 8, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(d_ids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, st));
+        const uint32_t grid = (uint32_t)std::min<size_t>(ids.size(), (size_t)c->sms * 8);
+        k_pack_filters<<<grid, 256, 0, st>>>(c->d_work_filters.as<uint32_t>(), dev_out, d_src, d_dst,
+                                              c->d_info.as<FileInfoDev>(), d_ids, (uint32_t)ids.size());
+        CUDA_TRY(c, cudaGetLastError());
+        c->launches += 1;
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+    }
+    return SDBFG_OK;
+}
+
+static int validate_batch(sdbfg_ctx* c, const uint64_t* offsets, const uint64_t* lens, uint32_t n, uint32_t dd,
+                          sdbfg_digest_result* res) {
+    if (!c || (!offsets && n) || (!lens && n) || (!res && n)) return SDBFG_ERR_ARG;
+    if (dd > kMaxBlockBytes || (dd && dd < kMinFile))
+        return fail(c, SDBFG_ERR_ARG, "dd_block_size %u outside [512, 16384]", dd);
+    for (uint32_t i = 0; i < n; i++) {
+        res[i] = sdbfg_digest_result{};
+        if (lens[i] < kMinFile) res[i].status = SDBFG_DIGEST_TOO_SMALL;
+        if (lens[i] >= (1ull << 40)) return fail(c, SDBFG_ERR_ARG, "input %u too large", i);
+    }
+    return SDBFG_OK;
+}
+
+// block mode: slots are known up front
+static uint64_t assign_block_slots(const uint64_t* lens, uint32_t n, uint32_t dd, sdbfg_digest_result* res) {
+    uint64_t slot = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        if (lens[i] < kMinFile) continue;
+        res[i].filter_offset = slot;
+        res[i].bf_count = (uint32_t)block_count(lens[i], dd);
+        slot += res[i].bf_count;
+    }
+    return slot;
+}
+
+extern "C" int sdbfg_digest_batch_device(sdbfg_ctx* c, const uint8_t* dev_data, const uint64_t* offsets,
+                                         const uint64_t* lens, uint32_t n, uint32_t dd, uint8_t* dev_out,
+                                         uint64_t out_cap, uint16_t* dev_counts, sdbfg_digest_result* res) {
+    int rc = validate_batch(c, offsets, lens, n, dd, res);
+    if (rc) return rc;
+    for (uint32_t i = 0; i < n; i++)
+        if (offsets[i] % 16) return fail(c, SDBFG_ERR_ARG, "device input %u not 16-byte aligned", i);
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    uint64_t next = 0;
+    if (dd) {
+        const uint64_t need = assign_block_slots(lens, n, dd, res);
+        if (need > out_cap) return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)need);
+        if (need && !dev_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
+    }
+    for (const Group& g : make_groups(lens, n, dd)) {
+        std::vector<uint64_t> off(offsets + g.first, offsets + g.first + g.count);
+        rc = digest_group_device(c, dev_data, off, lens, g, dd, reinterpret_cast<uint32_t*>(dev_out), dev_counts, res,
+                                 &next, out_cap);
+        if (rc) return rc;
+    }
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets,
+                                  const uint64_t* lens, uint32_t n, uint32_t dd, uint8_t* out_filters,
+                                  uint64_t out_cap, uint16_t* out_counts, sdbfg_digest_result* res) {
+    int rc = validate_batch(c, offsets, lens, n, dd, res);
+    if (rc) return rc;
+    if (n && !host_data) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    uint64_t total_slots = 0;
+    if (dd) {
+        total_slots = assign_block_slots(lens, n, dd, res);
+        if (total_slots > out_cap)
+            return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)total_slots);
+        if (total_slots && !out_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
+    }
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, host_data) == cudaSuccess &&
+                        (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    uint64_t next = 0;
+    for (const Group& g : make_groups(lens, n, dd)) {
+        // lay the group's inputs out 16-byte aligned on the device
+        std::vector<uint64_t> off(g.count);
+        uint64_t bytes = 0;
+        for (uint32_t k = 0; k < g.count; k++) {
+            off[k] = bytes;
+            bytes += (lens[g.first + k] + 15) & ~15ull;
+        }
+        CUDA_TRY(c, c->d_data.ensure(std::max<uint64_t>(bytes, 16)));
+        uint8_t* d = c->d_data.as<uint8_t>();
+        // contiguous source range with the same layout -> one copy
+        bool contiguous = true;
+        for (uint32_t k = 0; k < g.count && contiguous; k++)
+            contiguous = offsets[g.first + k] - offsets[g.first] == off[k];
+        if (contiguous && pinned) {
+            CUDA_TRY(c, cudaMemcpyAsync(d, host_data + offsets[g.first], bytes, cudaMemcpyHostToDevice, st));
+        } else {
+            for (uint32_t k = 0; k < g.count; k++) {
+                const uint32_t i = g.first + k;
+                if (lens[i] < kMinFile) continue;
+                CUDA_TRY(c, cudaMemcpyAsync(d + off[k], host_data + offsets[i], lens[i], cudaMemcpyHostToDevice, st));
+            }
+        }
+        uint64_t group_slots = 0, group_first_slot = 0;
+        if (dd) {
+            // block mode writes its slots directly; copy back this group's range
+            bool first = true;
+            for (uint32_t k = 0; k < g.count; k++) {
+                const uint32_t i = g.first + k;
+                if (lens[i] < kMinFile) continue;
+                if (first) {
+                    group_first_slot = res[i].filter_offset;
+                    first = false;
+                }
+                group_slots = res[i].filter_offset + res[i].bf_count - group_first_slot;
+            }
+            CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, group_slots) * 256));
+            CUDA_TRY(c, c->d_out_counts.ensure(std::max<uint64_t>(1, group_slots) * 2));
+            // shift slots into the group-local output buffer
+            std::vector<uint64_t> saved(g.count);
+            for (uint32_t k = 0; k < g.count; k++) {
+                saved[k] = res[g.first + k].filter_offset;
+                res[g.first + k].filter_offset -= group_first_slot;
+            }
+            rc = digest_group_device(c, d, off, lens, g, dd, c->d_out_filters.as<uint32_t>(),
+                                     c->d_out_counts.as<uint16_t>(), res, &next, out_cap);
+            for (uint32_t k = 0; k < g.count; k++) res[g.first + k].filter_offset = saved[k];
+            if (rc) return rc;
+            if (group_slots) {
+                CUDA_TRY(c, cudaMemcpyAsync(out_filters + group_first_slot * 256, c->d_out_filters.p,
+                                            group_slots * 256, cudaMemcpyDeviceToHost, st));
+                CUDA_TRY(c, cudaMemcpyAsync(out_counts + group_first_slot, c->d_out_counts.p, group_slots * 2,
+                                            cudaMemcpyDeviceToHost, st));
+            }
+        } else {
+            const uint64_t before = next;
+            uint64_t cap_needed = 0;
+            for (uint32_t k = 0; k < g.count; k++)
+                if (lens[g.first + k] >= kMinFile) cap_needed += stream_cap(lens[g.first + k]);
+            CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, cap_needed) * 256));
+            uint64_t local = 0;
+            rc = digest_group_device(c, d, off, lens, g, 0, c->d_out_filters.as<uint32_t>(), nullptr, res, &local,
+                                     cap_needed);
+            if (rc) return rc;
+            for (uint32_t k = 0; k < g.count; k++)
+                if (lens[g.first + k] >= kMinFile) res[g.first + k].filter_offset += before;
+            next = before + local;
+            if (next > out_cap) return fail(c, SDBFG_ERR_CAPACITY, "output capacity too small");
+            if (local)
+                CUDA_TRY(c, cudaMemcpyAsync(out_filters + before * 256, c->d_out_filters.p, local * 256,
+                                            cudaMemcpyDeviceToHost, st));
+        }
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+    }
+    return SDBFG_OK;
+}
+
+// -------------------------------------------------------------- comparison
+extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint32_t n, sdbfg_set** out) {
+    if (!c || !out || (n && !ds)) return SDBFG_ERR_ARG;
+    *out = nullptr;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    auto* s = new sdbfg_set();
+    s->ctx = c;
+    s->n = n;
+    uint64_t total = 0;
+    std::vector<CmpDigest> dig(n);
+    for (uint32_t i = 0; i < n; i++) {
+        if (ds[i].bf_count == 0 || !ds[i].filters) {
+            delete s;
+            return fail(c, SDBFG_ERR_ARG, "digest %u has no filters", i);
+        }
+        dig[i] = {(uint32_t)total, ds[i].bf_count};
+        total += ds[i].bf_count;
+    }
+    if (total >= (1ull << 32)) {
+        delete s;
+        return fail(c, SDBFG_ERR_ARG, "set too large");
+    }
+    std::vector<uint32_t> meta(total);
+    std::vector<uint8_t> filt(total * 256);
+    s->names.resize(n);
+    s->bf_count.resize(n);
+    s->last_elem.resize(n);
+    for (uint32_t i = 0; i < n; i++) {
+        const sdbfg_digest_desc& d = ds[i];
+        s->names[i] = d.name ? d.name : "";
+        s->bf_count[i] = d.bf_count;
+        memcpy(&filt[(uint64_t)dig[i].first * 256], d.filters, (uint64_t)d.bf_count * 256);
+        for (uint32_t f = 0; f < d.bf_count; f++) {
+            // get_elem_count (sdbf_class.cc:406-415)
+            uint32_t e = d.elem_counts ? d.elem_counts[f] : (f + 1 < d.bf_count ? d.max_elem : d.last_count);
+            uint32_t h = 0;
+            const uint8_t* p = d.filters + (uint64_t)f * 256;
+            for (int b = 0; b < 256; b += 8) {
+                uint64_t w;
+                memcpy(&w, p + b, 8);
+                h += (uint32_t)__builtin_popcountll(w);
+            }
+            meta[dig[i].first + f] = (h << 16) | (e & 0xFFFFu);
+            if (f + 1 == d.bf_count) s->last_elem[i] = e;
+        }
+    }
+    if (s->d_filters.ensure(std::max<uint64_t>(1, total) * 256) || s->d_meta.ensure(std::max<uint64_t>(1, total) * 4) ||
+        s->d_digests.ensure(std::max<uint32_t>(1, n) * sizeof(CmpDigest))) {
+        s->d_filters.release();
+        s->d_meta.release();
+        s->d_digests.release();
+        delete s;
+        return fail(c, SDBFG_ERR_NOMEM, "set upload: out of device memory");
+    }
+    cudaMemcpy(s->d_filters.p, filt.data(), total * 256, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_meta.p, meta.data(), total * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->d_digests.p, dig.data(), n * sizeof(CmpDigest), cudaMemcpyHostToDevice);
+    *out = s;
+    return SDBFG_OK;
+}
+
+extern "C" void sdbfg_set_free(sdbfg_set* s) {
+    if (!s) return;
+    cudaSetDevice(s->ctx->device);
+    s->d_filters.release();
+    s->d_meta.release();
+    s->d_digests.release();
+    delete s;
+}
+
+extern "C" uint32_t sdbfg_set_size(const sdbfg_set* s) { return s ? s->n : 0; }
+
+// Orientation of a pair: sdbf_score's swap rule (sdbf_core.cc:351-359).
+static CmpPair orient(const sdbfg_set* a, uint32_t i, const sdbfg_set* b, uint32_t j) {
+    const uint32_t n1 = a->bf_count[i], n2 = b->bf_count[j];
+    const bool swap = n1 > n2 || (n1 == n2 && (a->last_elem[i] > b->last_elem[j] ||
+                                               strcmp(a->names[i].c_str(), b->names[j].c_str()) > 0));
+    if (swap) return CmpPair{j, i, n2, 1u | 0u};  // ref from b (side 1), tgt from a (side 0)
+    return CmpPair{i, j, n1, 2u};                  // ref from a (side 0), tgt from b (side 1)
+}
+
+static int run_pairs(sdbfg_ctx* c, const sdbfg_set* a, const sdbfg_set* b, const std::vector<CmpPair>& pairs,
+                     int32_t* out) {
+    cudaStream_t st = c->stream;
+    CUDA_TRY(c, c->d_pairs.ensure(std::max<size_t>(1, pairs.size()) * sizeof(CmpPair)));
+    CUDA_TRY(c, c->d_scores.ensure(std::max<size_t>(1, pairs.size()) * 4));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_pairs.p, pairs.data(), pairs.size() * sizeof(CmpPair), cudaMemcpyHostToDevice,
+                                st));
+    CmpParams P{};
+    P.filters[0] = a->d_filters.as<uint32_t>();
+    P.meta[0] = a->d_meta.as<uint32_t>();
+    P.digests[0] = a->d_digests.as<CmpDigest>();
+    P.filters[1] = b->d_filters.as<uint32_t>();
+    P.meta[1] = b->d_meta.as<uint32_t>();
+    P.digests[1] = b->d_digests.as<CmpDigest>();
+    P.pairs = c->d_pairs.as<CmpPair>();
+    P.npairs = pairs.size();
+    P.scores = c->d_scores.as<int32_t>();
+    P.cutoffs = c->d_cut.as<uint16_t>();
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(pairs.size(), (uint64_t)c->sms * 16);
+    CUDA_TRY(c, launch_compare_pairs(P, std::max(1u, grid), st));
+    c->launches += 1;
+    CUDA_TRY(c, cudaMemcpyAsync(out, c->d_scores.p, pairs.size() * 4, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_score_pairs(sdbfg_ctx* c, const sdbfg_set* a, const sdbfg_set* b, const uint32_t* ia,
+                                 const uint32_t* ib, uint64_t npairs, int32_t* out) {
+    if (!c || !a || !b || (npairs && (!ia || !ib || !out))) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    for (uint64_t base = 0; base < npairs; base += kPairsPerLaunch) {
+        const uint64_t m = std::min<uint64_t>(kPairsPerLaunch, npairs - base);
+        std::vector<CmpPair> pairs(m);
+        for (uint64_t k = 0; k < m; k++) {
+            const uint32_t i = ia[base + k], j = ib[base + k];
+            if (i >= a->n || j >= b->n) return fail(c, SDBFG_ERR_ARG, "pair %llu out of range", (unsigned long long)k);
+            pairs[k] = orient(a, i, b, j);
+        }
+        int rc = run_pairs(c, a, b, pairs, out + base);
+        if (rc) return rc;
+    }
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_compare_all(sdbfg_ctx* c, const sdbfg_set* s, int32_t* out) {
+    if (!c || !s || !out) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    std::vector<CmpPair> pairs;
+    uint64_t done = 0;
+    for (uint32_t i = 0; i < s->n; i++) {
+        for (uint32_t j = i + 1; j < s->n; j++) {
+            pairs.push_back(orient(s, i, s, j));
+            if (pairs.size() == kPairsPerLaunch) {
+                int rc = run_pairs(c, s, s, pairs, out + done);
+                if (rc) return rc;
+                done += pairs.size();
+                pairs.clear();
+            }
+        }
+    }
+    if (!pairs.empty()) return run_pairs(c, s, s, pairs, out + done);
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_compare_to(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_set* t, int32_t* out) {
+    if (!c || !q || !t || !out) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    std::vector<CmpPair> pairs;
+    uint64_t done = 0;
+    for (uint32_t i = 0; i < q->n; i++) {
+        for (uint32_t j = 0; j < t->n; j++) {
+            pairs.push_back(orient(q, i, t, j));
+            if (pairs.size() == kPairsPerLaunch) {
+                int rc = run_pairs(c, q, t, pairs, out + done);
+                if (rc) return rc;
+                done += pairs.size();
+                pairs.clear();
+            }
+        }
+    }
+    if (!pairs.empty()) return run_pairs(c, q, t, pairs, out + done);
+    return SDBFG_OK;
+}
