@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark: bulk stream-mode SDBF digest generation on GB300.
+
+Workload (the configuration the headline "digest input GB/s" is quoted on):
+4096 files with sizes log-uniform over 4 KiB..64 MiB (seeded), content a
+per-file mixture of 50% uniform-random regions, 25% low-entropy runs and 25%
+order-1 Markov text, digested in stream mode (sdhash -b 0).  Synthetic,
+seeded (sdhash_gb300/csrc/synth.c); ~26 GiB, larger than L2 by 200x, so no
+L2 flush is needed between steps.
+
+One step = digest every file of the rank's shard once.
+  value -- device-resident: inputs already in HBM, digests left in HBM
+           (sdbfg_digest_batch_device), CUDA events on the launch stream.
+  e2e   -- through the public C ABI with HOST buffers (sdbfg_digest_batch):
+           host->device copy of the inputs from pinned memory, generation,
+           device->host copy of the packed filters, every step.
+
+--impl reference times the reference's CPU implementation of the path (the
+oracle port of sdhash's generation, all host threads) on the same workload.
+
+Multi-GPU (torchrun, --gpus N): files are size-balanced across ranks with no
+data-path collective (weak scaling of the total bytes); timings are max over
+ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "digest input GB/s"
+UNIT = "GB/s"
+CONFIG_BASE = {"workload": "bulk stream-mode digest generation", "files": 4096, "sizes": "log-uniform 4 KiB..64 MiB",
+               "content": "mixture: 50% random / 25% low-entropy runs / 25% order-1 Markov text",
+               "mode": "stream (-b 0)", "l2": "inputs larger than L2 (no flush needed)"}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nfiles", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
+    ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def make_workload(args, rank, world, pinned: bool):
+    """This rank's files, packed 16-byte aligned into one (pinned) host buffer."""
+    from sdhash_gb300 import shard, synth
+    sizes_all = synth.log_uniform_sizes(args.seed, args.nfiles, 4096, args.max_bytes)
+    mine = shard.shard_sizes(sizes_all, world)[rank]
+    sizes = sizes_all[mine]
+    offs, total = synth.packed_layout(sizes)
+    if pinned:
+        import torch
+        buf = torch.empty(max(16, total), dtype=torch.uint8, pin_memory=True)
+        data = buf.numpy()
+    else:
+        buf = None
+        data = np.empty(max(16, total), dtype=np.uint8)
+    # generate file by file with the global file index as the stream id, so a
+    # file's bytes do not depend on the sharding
+    import ctypes as C
+    L = synth.lib()
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(64, os.cpu_count() or 1)) as ex:
+        list(ex.map(lambda k: L.synth_fill_mixture(args.seed, int(mine[k]), data.ctypes.data + int(offs[k]),
+                                                   int(sizes[k])), range(len(mine))))
+    return buf, data, offs, sizes, sizes_all
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in self.rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str):
+    """dram bytes per input byte of `kernel` from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", f"{kernel}_ncu.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_input_byte:"):
+                return float(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(args, data, offs, sizes, nthreads=None, seed=7):
+    """The oracle port of sdhash's generation (file-parallel on all host
+    threads, as sdhash -p N) on a bounded random sample of the workload."""
+    from oracle import Oracle
+    O = Oracle()
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(len(sizes))
+    target = int(args.cpu_sample_gib * (1 << 30))
+    pick, tot = [], 0
+    for i in order:
+        if tot >= target:
+            break
+        pick.append(int(i))
+        tot += int(sizes[i])
+    nt = nthreads or (os.cpu_count() or 1)
+    bufs = [data[int(offs[i]):int(offs[i]) + int(sizes[i])] for i in pick]
+    t0 = time.perf_counter()
+    res = O.digest_many(bufs, 0, nt)
+    dt = time.perf_counter() - t0
+    assert all(r is not None or int(sizes[i]) < 512 for r, i in zip(res, pick))
+    del res
+    return {"value": tot / dt / 1e9, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": f"{len(pick)} files, {tot / (1 << 30):.2f} GiB drawn at random from the same workload",
+            "seconds": round(dt, 3)}
+
+
+def run_reference(args):
+    rank, world, local = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    _, data, offs, sizes, _ = make_workload(args, 0, 1, pinned=False)
+    nt = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(args, data, offs, sizes, nt, seed=1)
+    vals, secs = [], 0.0
+    base = None
+    for k in range(args.steps):
+        cb = cpu_baseline(args, data, offs, sizes, nt, seed=100 + k)
+        vals.append(cb["value"])
+        secs += cb["seconds"]
+        base = cb
+    v = float(np.mean(vals))
+    base["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": dict(CONFIG_BASE, sample_per_step=base["sample"]), "cpu_baseline": base,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_setup(args.gpus)
+    import torch
+    import sdhash_gb300 as g
+    torch.cuda.set_device(local)
+    buf, data, offs, sizes, sizes_all = make_workload(args, rank, world, pinned=True)
+    total_bytes = int(sizes.sum())
+    ctx = g.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    dev = torch.empty(max(16, len(data)), dtype=torch.uint8, device="cuda")
+    dev.copy_(buf, non_blocking=True)
+    cap = ctx.capacity(sizes, 0)
+    out = torch.empty(max(1, cap) * 256, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+
+    def step_device():
+        return ctx.digest_device(dev.data_ptr(), offs, sizes, 0, out.data_ptr(), cap)
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launch_count
+    ctx.profile(True)
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        res = step_device()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    barrier(world)
+    clocks.stop()
+    dev_ms = e0.elapsed_time(e1)
+    launches = ctx.launch_count - launches0
+    tiles_ms, tiles_n = ctx.kernel_time("k_stream_tiles")
+    kern = {k: ctx.kernel_time(k) for k in ("k_stream_tiles", "k_stream_verify", "k_stream_commit", "k_pack_filters")}
+    ctx.profile(False)
+    ms_per_step = allmax(world, dev_ms / args.steps)
+    bytes_all = allsum(world, total_bytes)
+    value = bytes_all / (ms_per_step / 1e3) / 1e9
+    out_filters = sum(int(r.bf_count) for r in res[: len(sizes)]) if len(sizes) else 0
+
+    # e2e through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        ctx.digest_packed(data, offs, sizes, 0)  # warm host staging
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ds = ctx.digest_packed(data, offs, sizes, 0)
+        torch.cuda.synchronize()
+        e2e_s = allmax(world, (time.perf_counter() - t0) / args.steps)
+        d2h = sum(d.bf_count for d in ds if d is not None) * 256 + 24 * len(sizes)
+        e2e = {"value": bytes_all / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(total_bytes),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+        del ds
+
+    peak, peak_kind = peaks()
+    ngroups = max(1, tiles_n // max(1, args.steps))
+    per_launch_bytes = total_bytes / ngroups
+    tile_ms = tiles_ms / max(1, tiles_n)
+    achieved = per_launch_bytes / (tile_ms / 1e3) / 1e9 if tile_ms > 0 else None
+    tpb = profiled_traffic("k_stream_tiles")
+    roofline = {"bound": "hbm", "kernel": "k_stream_tiles", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None,
+                "traffic": (tpb * per_launch_bytes) if tpb else None,
+                "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
+                "algorithmic_bytes_per_launch": per_launch_bytes,
+                "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kern.items()}}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": dict(CONFIG_BASE, total_bytes=int(bytes_all), files_per_rank=len(sizes),
+                           parallelism=f"files sharded over {world} GPU(s)", wall_s_timed=round(wall, 3),
+                           out_filters_per_step=out_filters),
+            "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e}
+    if rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline(args, data, offs, sizes)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    barrier(world)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

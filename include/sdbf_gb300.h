@@ -50,6 +50,14 @@ int sdbfg_ctx_set_stream(sdbfg_ctx *ctx, void *cuda_stream);
 int sdbfg_ctx_synchronize(sdbfg_ctx *ctx);
 /* Kernel launches issued on this context so far (instrumentation). */
 uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx *ctx);
+/* Per-kernel timing with CUDA events recorded on the launch stream around
+ * every launch (off by default; enabling clears previous totals).
+ * sdbfg_ctx_kernel_time reports the accumulated milliseconds and launch
+ * count of one kernel ("k_stream_tiles", "k_stream_verify",
+ * "k_stream_commit", "k_pack_filters", "k_block_digest", "k_compare_pairs").
+ * Instrumentation without a counterpart in the reference. */
+int sdbfg_ctx_profile(sdbfg_ctx *ctx, int enable);
+int sdbfg_ctx_kernel_time(sdbfg_ctx *ctx, const char *kernel, double *total_ms, uint64_t *launches);
 /* Speculative lead-in of the parallel popularity-score walk, in window steps
  * (default and maximum 128).  Results are exact for every value -- shorter
  * lead-ins only make the re-walk path run more often; tests use this to

@@ -72,6 +72,8 @@ def lib() -> C.CDLL:
         L.sdbfg_ctx_launch_count.argtypes = [vp]
         L.sdbfg_ctx_launch_count.restype = C.c_uint64
         L.sdbfg_ctx_set_lead.argtypes = [vp, C.c_uint32]
+        L.sdbfg_ctx_profile.argtypes = [vp, C.c_int]
+        L.sdbfg_ctx_kernel_time.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         L.sdbfg_ctx_relinked_tiles.argtypes = [vp]
         L.sdbfg_ctx_relinked_tiles.restype = C.c_uint64
         L.sdbfg_digest_capacity.argtypes = [u64p, C.c_uint32, C.c_uint32]
@@ -234,6 +236,16 @@ class Context:
     def set_lead(self, steps: int):
         """Speculative lead-in of the parallel score walk (exact for any value)."""
         self._check(lib().sdbfg_ctx_set_lead(self.h, steps))
+
+    def profile(self, enable: bool = True):
+        """Per-kernel CUDA-event timing on the launch stream."""
+        self._check(lib().sdbfg_ctx_profile(self.h, 1 if enable else 0))
+
+    def kernel_time(self, name: str) -> tuple[float, int]:
+        """(total milliseconds, launches) of one kernel since profiling was enabled."""
+        ms, n = C.c_double(), C.c_uint64()
+        self._check(lib().sdbfg_ctx_kernel_time(self.h, name.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, int(n.value)
 
     @property
     def launch_count(self) -> int:

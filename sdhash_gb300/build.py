@@ -24,8 +24,9 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = os.environ.get("SDBFG_ARCH", "-gencode=arch=compute_103a,code=sm_103a")
 CU_SOURCES = ["gen_kernels.cu", "compare_kernels.cu", "sdbf_api.cu"]
-CPP_SOURCES = ["sdbf_text.cpp"]
-HEADERS = ["gen_kernels.h", "compare_kernels.h", "sdbf_device.cuh", "sdbf_tables.h"]
+CPP_SOURCES = ["sdbf_text.cpp", "../compat/sdbf_compat.cpp"]
+HEADERS = ["gen_kernels.h", "compare_kernels.h", "sdbf_device.cuh", "sdbf_tables.h", "../compat/sdbf_class.h",
+           "../compat/sdbf_set.h", "../compat/sdbf_conf.h"]
 
 
 def _nvcc() -> str:
@@ -55,7 +56,7 @@ def build_gb300(force: bool = False, verbose: bool = False) -> str:
     objs, jobs = [], []
     for src in CU_SOURCES + CPP_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+        o = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
             if src.endswith(".cu"):

@@ -128,9 +128,7 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
     const uint32_t np = g.RE - g.Q0;
     const uint32_t per = (np + kGenThreads - 1) / kGenThreads;
     const uint32_t tid = threadIdx.x;
-    uint8_t* h = s.hist + tid;  // counts of value v at h[v * kGenThreads]
-    // clear own histogram
-    for (int v = 0; v < 256; v++) h[v * kGenThreads] = 0;
+    uint8_t* h = s.hist + tid;  // counts of value v at h[v * kGenThreads] (cleared by the caller)
     const uint32_t lo = tid * per, hi = min(np, lo + per);
     const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
     uint32_t e = 0;
@@ -289,6 +287,10 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
                               const uint16_t* rank_tab, const uint32_t* ent_tab, const uint64_t* entry,
                               uint64_t* sig_in, uint64_t* tau_out, uint32_t lead) {
     load_bytes(chunk, g, s.bytes32);
+    {
+        uint4* h4 = reinterpret_cast<uint4*>(s.hist);
+        for (uint32_t i = threadIdx.x; i < 256 * kGenThreads / 16; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
+    }
     __syncthreads();
     compute_ranks(g, s, rank_tab, ent_tab);
     __syncthreads();
@@ -796,20 +798,32 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
 size_t stream_tile_smem() { return tile_smem_bytes(kTileL); }
 size_t block_smem(uint32_t lmax) { return tile_smem_bytes(lmax); }
 
-cudaError_t launch_stream(const GenParams& P, uint32_t grid_tiles, uint32_t grid_chunks, uint32_t grid_commit,
-                          cudaStream_t st) {
-    static bool attr = false;
-    const size_t sm = stream_tile_smem();
-    if (!attr) {
-        cudaFuncSetAttribute(k_stream_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_stream_verify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_stream_commit, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(sizeof(CommitSmem) * kCommitWarps));
-        attr = true;
-    }
-    if (P.ntiles) k_stream_tiles<<<grid_tiles, kGenThreads, sm, st>>>(P);
-    if (P.nchunks) k_stream_verify<<<grid_chunks, kGenThreads, sm, st>>>(P);
-    if (P.nfiles) k_stream_commit<<<grid_commit, kCommitWarps * 32, sizeof(CommitSmem) * kCommitWarps, st>>>(P);
+static void set_stream_attrs() {
+    static bool done = false;
+    if (done) return;
+    const int sm = (int)stream_tile_smem();
+    cudaFuncSetAttribute(k_stream_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(k_stream_verify, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(k_stream_commit, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(CommitSmem) * kCommitWarps));
+    done = true;
+}
+
+cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    set_stream_attrs();
+    k_stream_tiles<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_verify(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    set_stream_attrs();
+    k_stream_verify<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_commit(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    set_stream_attrs();
+    k_stream_commit<<<grid, kCommitWarps * 32, sizeof(CommitSmem) * kCommitWarps, st>>>(P);
     return cudaGetLastError();
 }
 

@@ -76,8 +76,9 @@ struct GenParams {
 
 size_t stream_tile_smem();
 size_t block_smem(uint32_t lmax);
-cudaError_t launch_stream(const GenParams& P, uint32_t grid_tiles, uint32_t grid_chunks, uint32_t grid_commit,
-                          cudaStream_t st);
+cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t st);
+cudaError_t launch_stream_verify(const GenParams& P, uint32_t grid, cudaStream_t st);
+cudaError_t launch_stream_commit(const GenParams& P, uint32_t grid, cudaStream_t st);
 cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st);
 
 }  // namespace sdbfg

@@ -72,7 +72,21 @@ struct HostBuf {
 
 }  // namespace
 
+struct KernelTimer {
+    const char* name;
+    cudaEvent_t a, b;
+};
+
+struct KernelStat {
+    std::string name;
+    double ms = 0;
+    uint64_t launches = 0;
+};
+
 struct sdbfg_ctx {
+    bool profile = false;
+    std::vector<KernelTimer> pending;
+    std::vector<KernelStat> stats;
     int device = 0;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
@@ -98,6 +112,56 @@ struct sdbfg_set {
     std::vector<uint32_t> last_elem;  // element count of the last filter (swap rule)
     DevBuf d_filters, d_meta, d_digests;
 };
+
+// Per-kernel CUDA-event timing on the launch stream (only when enabled).
+static void timer_begin(sdbfg_ctx* c, const char* name, cudaEvent_t* a) {
+    *a = nullptr;
+    if (!c->profile) return;
+    cudaEventCreate(a);
+    cudaEventRecord(*a, c->stream);
+    (void)name;
+}
+
+static void timer_end(sdbfg_ctx* c, const char* name, cudaEvent_t a) {
+    if (!c->profile || !a) return;
+    cudaEvent_t b;
+    cudaEventCreate(&b);
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({name, a, b});
+}
+
+static void timer_collect(sdbfg_ctx* c) {
+    for (KernelTimer& t : c->pending) {
+        cudaEventSynchronize(t.b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, t.a, t.b);
+        KernelStat* st = nullptr;
+        for (KernelStat& k : c->stats)
+            if (k.name == t.name) st = &k;
+        if (!st) {
+            c->stats.push_back(KernelStat{t.name, 0, 0});
+            st = &c->stats.back();
+        }
+        st->ms += ms;
+        st->launches += 1;
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    c->pending.clear();
+}
+
+#define TIMED_LAUNCH(c, name, expr)             \
+    do {                                        \
+        cudaEvent_t ev_;                        \
+        timer_begin((c), (name), &ev_);         \
+        cudaError_t le_ = (expr);               \
+        timer_end((c), (name), ev_);            \
+        if (le_ != cudaSuccess)                 \
+            return fail((c), SDBFG_ERR_CUDA, "%s launch: %s", (name), cudaGetErrorString(le_)); \
+        (c)->launches += 1;                     \
+    } while (0)
+
+static int fail(sdbfg_ctx* c, int code, const char* fmt, ...);
 
 static int fail(sdbfg_ctx* c, int code, const char* fmt, ...) {
     char buf[512];
@@ -158,6 +222,7 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
                       &c->d_pairs, &c->d_scores})
         b->release();
     c->h_stage.release();
+    timer_collect(c);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
 }
@@ -177,6 +242,27 @@ extern "C" int sdbfg_ctx_synchronize(sdbfg_ctx* c) {
 }
 
 extern "C" uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx* c) { return c ? c->launches : 0; }
+
+extern "C" int sdbfg_ctx_profile(sdbfg_ctx* c, int enable) {
+    if (!c) return SDBFG_ERR_ARG;
+    timer_collect(c);
+    c->profile = enable != 0;
+    if (enable) c->stats.clear();
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_ctx_kernel_time(sdbfg_ctx* c, const char* name, double* total_ms, uint64_t* launches) {
+    if (!c || !name) return SDBFG_ERR_ARG;
+    timer_collect(c);
+    if (total_ms) *total_ms = 0;
+    if (launches) *launches = 0;
+    for (const KernelStat& k : c->stats)
+        if (k.name == name) {
+            if (total_ms) *total_ms = k.ms;
+            if (launches) *launches = k.launches;
+        }
+    return SDBFG_OK;
+}
 
 extern "C" int sdbfg_ctx_set_lead(sdbfg_ctx* c, uint32_t steps) {
     if (!c || steps > kLead) return SDBFG_ERR_ARG;
@@ -294,8 +380,7 @@ static int digest_group_device(sdbfg_ctx* c, const uint8_t* dev_base, const std:
         P.out_counts = dev_counts;
         P.block_lmax = (lmax + 63) / 64 * 64;
         const uint32_t grid = (uint32_t)std::min<size_t>(chunks.size(), (size_t)c->sms * 2 * 8);
-        CUDA_TRY(c, launch_block(P, grid, st));
-        c->launches += 1;
+        TIMED_LAUNCH(c, "k_block_digest", launch_block(P, grid, st));
         // the chunk table must outlive the async copy
         CUDA_TRY(c, cudaStreamSynchronize(st));
         return SDBFG_OK;
@@ -362,8 +447,9 @@ static int digest_group_device(sdbfg_ctx* c, const uint8_t* dev_base, const std:
     const uint32_t grid_chunks = (uint32_t)std::min<size_t>(chunks.size(), (size_t)c->sms * 3 * 16);
     const uint32_t grid_commit =
         (uint32_t)std::min<size_t>((g.count + kCommitWarps - 1) / kCommitWarps, (size_t)c->sms * 3 * 16);
-    CUDA_TRY(c, launch_stream(P, std::max(1u, grid_tiles), std::max(1u, grid_chunks), std::max(1u, grid_commit), st));
-    c->launches += (P.ntiles ? 1 : 0) + (P.nchunks ? 1 : 0) + (P.nfiles ? 1 : 0);
+    if (P.ntiles) TIMED_LAUNCH(c, "k_stream_tiles", launch_stream_tiles(P, std::max(1u, grid_tiles), st));
+    if (P.nchunks) TIMED_LAUNCH(c, "k_stream_verify", launch_stream_verify(P, std::max(1u, grid_chunks), st));
+    if (P.nfiles) TIMED_LAUNCH(c, "k_stream_commit", launch_stream_commit(P, std::max(1u, grid_commit), st));
     // per-file results
     std::vector<FileInfoDev> info(g.count);
     CUDA_TRY(c, cudaMemcpyAsync(info.data(), c->d_info.p, info.size() * sizeof(FileInfoDev), cudaMemcpyDeviceToHost,
@@ -396,10 +482,10 @@ static int digest_group_device(sdbfg_ctx* c, const uint8_t* dev_base, const std:
         CUDA_TRY(c, cudaMemcpyAsync(d_dst, dst_off.data(), ids.size() * 8, cudaMemcpyHostToDevice, st));
         CUDA_TRY(c, cudaMemcpyAsync(d_ids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, st));
         const uint32_t grid = (uint32_t)std::min<size_t>(ids.size(), (size_t)c->sms * 8);
-        k_pack_filters<<<grid, 256, 0, st>>>(c->d_work_filters.as<uint32_t>(), dev_out, d_src, d_dst,
-                                              c->d_info.as<FileInfoDev>(), d_ids, (uint32_t)ids.size());
-        CUDA_TRY(c, cudaGetLastError());
-        c->launches += 1;
+        TIMED_LAUNCH(c, "k_pack_filters",
+                     (k_pack_filters<<<grid, 256, 0, st>>>(c->d_work_filters.as<uint32_t>(), dev_out, d_src, d_dst,
+                                                           c->d_info.as<FileInfoDev>(), d_ids, (uint32_t)ids.size()),
+                      cudaGetLastError()));
         CUDA_TRY(c, cudaStreamSynchronize(st));
     }
     return SDBFG_OK;
@@ -650,8 +736,7 @@ static int run_pairs(sdbfg_ctx* c, const sdbfg_set* a, const sdbfg_set* b, const
     P.scores = c->d_scores.as<int32_t>();
     P.cutoffs = c->d_cut.as<uint16_t>();
     const uint32_t grid = (uint32_t)std::min<uint64_t>(pairs.size(), (uint64_t)c->sms * 16);
-    CUDA_TRY(c, launch_compare_pairs(P, std::max(1u, grid), st));
-    c->launches += 1;
+    TIMED_LAUNCH(c, "k_compare_pairs", launch_compare_pairs(P, std::max(1u, grid), st));
     CUDA_TRY(c, cudaMemcpyAsync(out, c->d_scores.p, pairs.size() * 4, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(c, cudaStreamSynchronize(st));
     return SDBFG_OK;
