@@ -103,6 +103,34 @@ int sdbfg_digest_batch_device(sdbfg_ctx *ctx, const uint8_t *dev_data, const uin
                               const uint64_t *lens, uint32_t n, uint32_t dd_block_size, uint8_t *dev_out_filters,
                               uint64_t out_cap, uint16_t *dev_out_elem_counts, sdbfg_digest_result *results);
 
+/* ------------------------------------------- digests without allocation
+ * No counterpart in the reference.  For callers that cannot allocate GPU
+ * memory -- code inside a framework that owns every device allocation, a
+ * fixed memory budget reserved up front, or a path that may not enter the
+ * allocator -- this stream-mode digest (same results as
+ * sdbfg_digest_batch_device with dd_block_size 0) allocates nothing, on the
+ * device or on the host heap.  Its scratch is one fixed device array of
+ * SDBFG_NOALLOC_SCRATCH_BYTES compiled into the library: every GPU that
+ * loads the library holds it until the process exits.
+ *   Limits: at most SDBFG_NOALLOC_MAX_INPUTS inputs and
+ *   SDBFG_NOALLOC_MAX_INPUT_BYTES input bytes per call; larger requests are
+ *   rejected with SDBFG_ERR_CAPACITY (and a message on stderr), as is an
+ *   output smaller than the digests need.
+ * Inputs: device memory, offsets multiples of 16; outputs: packed filters in
+ * dev_out_filters (out_cap filter slots), results[] in host memory.  Runs on
+ * the current device and on cuda_stream (NULL = default stream), and
+ * returns after the work is complete.
+ * The first call on a device resolves the scratch array's device address
+ * and loads the digest tables into it; make that first call before any
+ * stream capture.  All calls share the one array: calls whose work overlaps
+ * on the GPU race and corrupt each other's results -- serialise them. */
+#define SDBFG_NOALLOC_MAX_INPUTS 256u
+#define SDBFG_NOALLOC_MAX_INPUT_BYTES (8ull << 20)
+#define SDBFG_NOALLOC_SCRATCH_BYTES (14ull << 20)
+int sdbfg_digest_stream_noalloc(const uint8_t *dev_data, const uint64_t *offsets, const uint64_t *lens, uint32_t n,
+                                uint8_t *dev_out_filters, uint64_t out_cap, sdbfg_digest_result *results,
+                                void *cuda_stream);
+
 /* ------------------------------------------------------------ comparison */
 /* A digest as the reference's sdbf object holds it (sdbf/sdbf_class.h:95-119). */
 typedef struct {
