@@ -69,13 +69,25 @@ struct TileSmem {
 
 __host__ __device__ constexpr uint32_t align_up(uint32_t v, uint32_t a) { return (v + a - 1) / a * a; }
 
+// Padded index of the per-position uint16 arrays (ranks, full-rescan
+// results): one spare word after every 64 entries, so 32 lanes that each
+// scan their own aligned 64-position block address 32 different banks.
+__host__ __device__ constexpr uint32_t pidx(uint32_t o) { return o + 2 * (o >> 6); }
+__host__ __device__ constexpr uint32_t padded_len(uint32_t n) { return pidx(n) + 2; }
+
+// Byte address of thread t's counter for byte value v in the histogram area:
+// each lane's 256 counters occupy 64 words of its own bank.
+__device__ __forceinline__ uint32_t hist_off(uint32_t t, uint32_t v) {
+    return ((((t >> 5) * 64 + (v >> 2)) * 32 + (t & 31)) << 2) | (v & 3);
+}
+
 __host__ __device__ inline uint32_t tile_smem_bytes(uint32_t Lmax) {
     const uint32_t span = Lmax + 64 + kLead + 64;           // rank positions
     uint32_t b = 0;
     b += align_up(span + 64 + 16, 16);                       // bytes
-    b += align_up(span * 2, 16);                             // ranks
+    b += align_up(padded_len(span) * 2, 16);                 // ranks
     const uint32_t hist = 256 * kGenThreads;
-    const uint32_t phase3 = align_up((Lmax + 64 + kLead) * 2, 16) + align_up((span / 32 + 4) * 4, 16) +
+    const uint32_t phase3 = align_up(padded_len(Lmax + 64 + kLead) * 2, 16) + align_up((span / 32 + 4) * 4, 16) +
                             align_up(Lmax + 16, 16);
     b += hist > phase3 ? hist : phase3;                      // union
     b += align_up(((Lmax + 64) / 15 + 8) * 4, 16);           // selected / candidate positions
@@ -89,10 +101,10 @@ __device__ inline TileSmem carve(uint8_t* base, uint32_t Lmax) {
     const uint32_t span = Lmax + 64 + kLead + 64;
     uint8_t* p = base;
     s.bytes32 = reinterpret_cast<uint32_t*>(p); p += align_up(span + 64 + 16, 16);
-    s.ranks = reinterpret_cast<uint16_t*>(p); p += align_up(span * 2, 16);
+    s.ranks = reinterpret_cast<uint16_t*>(p); p += align_up(padded_len(span) * 2, 16);
     uint8_t* u = p;
     s.hist = u;
-    s.fres = reinterpret_cast<uint16_t*>(u); u += align_up((Lmax + 64 + kLead) * 2, 16);
+    s.fres = reinterpret_cast<uint16_t*>(u); u += align_up(padded_len(Lmax + 64 + kLead) * 2, 16);
     s.eqw = reinterpret_cast<uint32_t*>(u); u += align_up((span / 32 + 4) * 4, 16);
     s.score32 = reinterpret_cast<uint32_t*>(u); u += align_up(Lmax + 16, 16);
     const uint32_t hist = 256 * kGenThreads;
@@ -128,35 +140,36 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
     const uint32_t np = g.RE - g.Q0;
     const uint32_t per = (np + kGenThreads - 1) / kGenThreads;
     const uint32_t tid = threadIdx.x;
-    uint8_t* h = s.hist + tid;  // counts of value v at h[v * kGenThreads] (cleared by the caller)
+    uint8_t* h = s.hist;  // counts at hist_off(tid, v) (cleared by the caller)
     const uint32_t lo = tid * per, hi = min(np, lo + per);
     const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
     uint32_t e = 0;
     for (uint32_t r = lo; r < hi; r++) {
         const uint32_t o = g.Q0 + r;
         if (o >= last) {
-            s.ranks[r] = 0;
+            s.ranks[pidx(r)] = 0;
             continue;
         }
         if (r == lo) {
             // entr64_init_int (entr64.cc:27-41) built incrementally
             for (int k = 0; k < kWin; k++) {
                 const uint32_t v = b8[r + k];
-                const uint32_t c = h[v * kGenThreads];
+                const uint32_t c = h[hist_off(tid, v)];
                 e += ent_tab[c + 1] - ent_tab[c];
-                h[v * kGenThreads] = (uint8_t)(c + 1);
+                h[hist_off(tid, v)] = (uint8_t)(c + 1);
             }
         } else {
             // entr64_inc_int (entr64.cc:47-71): byte r-1 leaves, r+63 enters
             const uint32_t a = b8[r - 1], b = b8[r + 63];
             if (a != b) {
-                const uint32_t ca = h[a * kGenThreads], cb = h[b * kGenThreads];
-                h[a * kGenThreads] = (uint8_t)(ca - 1);
-                h[b * kGenThreads] = (uint8_t)(cb + 1);
+                const uint32_t ha = hist_off(tid, a), hb = hist_off(tid, b);
+                const uint32_t ca = h[ha], cb = h[hb];
+                h[ha] = (uint8_t)(ca - 1);
+                h[hb] = (uint8_t)(cb + 1);
                 e = e - (ent_tab[ca] - ent_tab[ca - 1]) + (ent_tab[cb + 1] - ent_tab[cb]);
             }
         }
-        s.ranks[r] = rank_tab[e >> 10];
+        s.ranks[pidx(r)] = rank_tab[e >> 10];
     }
 }
 
@@ -171,7 +184,7 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
     const uint32_t nw = (np + 31) / 32;
     for (uint32_t w = threadIdx.x / 32; w < nw; w += blockDim.x / 32) {
         const uint32_t o = w * 32 + (threadIdx.x & 31);
-        const bool eq = (o + 1 < np) && s.ranks[o] == s.ranks[o + 1];
+        const bool eq = (o + 1 < np) && s.ranks[pidx(o)] == s.ranks[pidx(o + 1)];
         const uint32_t bits = __ballot_sync(0xffffffffu, eq);
         if ((threadIdx.x & 31) == 0) s.eqw[w] = bits;
     }
@@ -188,7 +201,7 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 #pragma unroll
         for (int u = 0; u < 64; u++) {
             const uint32_t o = base + 64 + u;
-            uint32_t r = (o < np) ? s.ranks[o] : 0;
+            uint32_t r = (o < np) ? s.ranks[pidx(o)] : 0;
             const uint32_t key = ((r == 0 ? 1023u : r) << 6) | (uint32_t)u;
             run = min(run, key);
             pre[u] = (uint16_t)run;
@@ -197,7 +210,7 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 #pragma unroll
         for (int u = 63; u >= 0; u--) {
             const uint32_t k = base + u;
-            const uint32_t rk = (k < np) ? s.ranks[k] : 0;
+            const uint32_t rk = (k < np) ? s.ranks[pidx(k)] : 0;
             suf = min(suf, ((rk == 0 ? 1023u : rk) << 6) | (uint32_t)u);
             if (k < nsteps) {
                 uint16_t out = 0;
@@ -227,7 +240,7 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
                     if (p > k + 63) p = k + 63;
                     out = (uint16_t)((m << 6) | (p - k));
                 }
-                s.fres[k] = out;
+                s.fres[pidx(k)] = out;
             }
         }
     }
@@ -262,13 +275,13 @@ struct Credit {
 __device__ inline ChainState walk(const TileGeom& g, const TileSmem& s, uint32_t a, uint32_t b, ChainState st,
                                   bool force_full, Credit* cr) {
     for (uint32_t i = a; i < b; i++) {
-        const uint32_t r64 = s.ranks[i + 64 - g.Q0];
+        const uint32_t r64 = s.ranks[pidx(i + 64 - g.Q0)];
         const bool cheap = !(force_full && i == a) && i > 0 && st.M > 0 && r64 >= st.M && i < st.P;
         if (cheap) {
             if (r64 == st.M) st.P = i + 64;
             if (cr) cr->add(st.P);
         } else {
-            const uint32_t f = s.fres[i - g.Q0];
+            const uint32_t f = s.fres[pidx(i - g.Q0)];
             st.M = f >> 6;
             st.P = i + (f & 63);
             if (st.M && cr) cr->add(st.P);
@@ -380,34 +393,52 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
 // ------------------------------------------- phase 6: ordered compaction
 // Writes the positions (relative to t0) with score > thr (or >= thr when
 // ge) among [t0, t0+nown) into s.list in ascending order; returns count.
-__device__ uint32_t compact(const TileSmem& s, uint32_t nown, uint32_t thr, bool ge, uint32_t* tmp_counts) {
-    const uint32_t per = (nown + blockDim.x - 1) / blockDim.x;
-    const uint32_t lo = threadIdx.x * per, hi = min(nown, lo + per);
-    const uint8_t* sc = reinterpret_cast<const uint8_t*>(s.score32);
-    uint32_t c = 0;
-    for (uint32_t o = lo; o < hi; o++) {
-        const uint32_t v = sc[o];
-        c += ge ? (v >= thr) : (v > thr);
-    }
-    // block exclusive scan of c
-    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    uint32_t incl = c;
+// Each warp owns a contiguous run of score words; lanes read consecutive
+// 32-bit words (4 positions each), so the reads are conflict-free.
+__device__ __forceinline__ uint32_t word_flags(const uint32_t* sc32, uint32_t wd, uint32_t nown, uint32_t thr,
+                                               bool ge) {
+    const uint32_t w = sc32[wd];
+    uint32_t f = 0;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= (uint32_t)d) incl += y;
+    for (int b = 0; b < 4; b++) {
+        const uint32_t v = (w >> (8 * b)) & 0xFFu;
+        const bool sel = ge ? (v >= thr) : (v > thr);
+        if (sel && 4 * wd + b < nown) f |= 1u << b;
     }
-    if (lane == 31) tmp_counts[wid] = incl;
+    return f;
+}
+
+__device__ uint32_t compact(const TileSmem& s, uint32_t nown, uint32_t thr, bool ge, uint32_t* tmp_counts) {
+    const uint32_t nwords = (nown + 3) / 4;
+    const uint32_t nwarps = blockDim.x / 32, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t per = ((nwords + nwarps - 1) / nwarps + 31) / 32 * 32;
+    const uint32_t w0 = min(nwords, wid * per), w1 = min(nwords, w0 + per);
+    uint32_t c = 0;
+    for (uint32_t wd = w0 + lane; wd < w1; wd += 32) c += __popc(word_flags(s.score32, wd, nown, thr, ge));
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+    if (lane == 0) tmp_counts[wid] = c;
     __syncthreads();
-    uint32_t woff = 0, total = 0;
-    for (uint32_t w = 0; w < blockDim.x / 32; w++) {
-        if (w < wid) woff += tmp_counts[w];
+    uint32_t base = 0, total = 0;
+    for (uint32_t w = 0; w < nwarps; w++) {
+        if (w < wid) base += tmp_counts[w];
         total += tmp_counts[w];
     }
-    uint32_t pos = woff + incl - c;
-    for (uint32_t o = lo; o < hi; o++) {
-        const uint32_t v = sc[o];
-        if (ge ? (v >= thr) : (v > thr)) s.list[pos++] = o;
+    for (uint32_t wd0 = w0; wd0 < w1; wd0 += 32) {
+        const uint32_t wd = wd0 + lane;
+        const uint32_t f = wd < w1 ? word_flags(s.score32, wd, nown, thr, ge) : 0u;
+        const uint32_t k = __popc(f);
+        uint32_t incl = k;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        uint32_t pos = base + incl - k;
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+            if ((f >> b) & 1u) s.list[pos++] = 4 * wd + b;
+        base += __shfl_sync(0xffffffffu, incl, 31);
     }
     __syncthreads();
     return total;
@@ -499,10 +530,13 @@ __global__ void __launch_bounds__(kGenThreads) k_stream_verify(GenParams P) {
 // ------------------------------------------------------- ordered commit
 // Per-warp shared state for the stream commit.
 struct CommitSmem {
-    uint32_t F[64];        // current 256-byte filter
-    uint32_t G[kBigBytes / 4];  // current 16 KiB big filter
-    uint32_t dup[2][192];  // values seen twice in a group (F, G)
-    uint32_t ndup[2];
+    uint32_t F[64];                  // current 256-byte filter
+    uint32_t own[2048];              // lanes of the group holding each filter index
+    uint32_t G[kBigBytes / 4];       // current 16 KiB big filter
+    uint32_t dup[192];               // big-filter values set twice within a group
+    uint32_t ndup;
+    uint32_t pad[3];
+    uint32_t feat[2][5][kTileCap];   // double-buffered features of a tile
 };
 
 __device__ inline uint32_t lanemask_le() {
@@ -511,17 +545,34 @@ __device__ inline uint32_t lanemask_le() {
     return m;
 }
 
-// Insert the group's bits into bitmap `bm` for lanes in `act`; returns for
-// each lane a mask over its 5 values of "new relative to everything before
-// this lane in lane order".  flipped[k] records bits this lane turned on.
-template <int kKind>
-__device__ inline uint32_t group_insert(uint32_t* bm, uint32_t* dup, uint32_t* ndup, bool act, const uint32_t (&idx)[5],
-                                        uint32_t& flipped) {
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+// Stage the first `nf` features of a tile (5 rows of kTileCap words) into buf.
+__device__ __forceinline__ void stage_tile(uint32_t (*buf)[kTileCap], const uint32_t* feat, uint32_t nf,
+                                           uint32_t lane) {
+    const uint32_t n4 = (nf + 3) / 4;
+    for (uint32_t q = lane; q < 5 * n4; q += 32) {
+        const uint32_t k = q / n4, j = q - k * n4;
+        cp_async16(&buf[k][4 * j], feat + (size_t)k * kTileCap + 4 * j);
+    }
+    cp_async_commit();
+}
+
+// Big-filter (G) test for the lanes in `act`, in lane order: returns a mask
+// over the lane's 5 values of "not set before this lane".  Sets the bits
+// (atomicOr); `flipped` records the bits this lane turned on.
+__device__ inline uint32_t big_insert(uint32_t* G, uint32_t* dup, uint32_t* ndup, bool act, const uint32_t (&b)[5],
+                                      uint32_t& flipped) {
     const uint32_t lane = threadIdx.x & 31;
-    uint32_t pre = 0;  // bit k: value k was already set before the group
+    uint32_t pre = 0;
     if (act) {
 #pragma unroll
-        for (int k = 0; k < 5; k++) pre |= ((bm[idx[k] >> 5] >> (idx[k] & 31)) & 1u) << k;
+        for (int k = 0; k < 5; k++) pre |= ((G[b[k] >> 5] >> (b[k] & 31)) & 1u) << k;
     }
     __syncwarp();
     flipped = 0;
@@ -529,13 +580,11 @@ __device__ inline uint32_t group_insert(uint32_t* bm, uint32_t* dup, uint32_t* n
 #pragma unroll
         for (int k = 0; k < 5; k++) {
             if (!((pre >> k) & 1u)) {
-                const uint32_t bit = 1u << (idx[k] & 31);
-                const uint32_t old = atomicOr(&bm[idx[k] >> 5], bit);
+                const uint32_t bit = 1u << (b[k] & 31);
+                const uint32_t old = atomicOr(&G[b[k] >> 5], bit);
                 if (old & bit) {
-                    // set earlier within this group (by another lane or by an
-                    // equal value of this lane): resolve order below
                     const uint32_t slot = atomicAdd(ndup, 1u);
-                    if (slot < 192) dup[slot] = idx[k];
+                    if (slot < 192) dup[slot] = b[k];
                 } else {
                     flipped |= 1u << k;
                 }
@@ -543,48 +592,30 @@ __device__ inline uint32_t group_insert(uint32_t* bm, uint32_t* dup, uint32_t* n
         }
     }
     __syncwarp();
-    uint32_t fresh = act ? (~pre & 31u) : 0u;  // candidates for "new"
+    uint32_t fresh = act ? (~pre & 31u) : 0u;
     const uint32_t nd = min(*ndup, 192u);
     for (uint32_t e = 0; e < nd; e++) {
         const uint32_t v = dup[e];
         uint32_t mine = 0;
 #pragma unroll
-        for (int k = 0; k < 5; k++) mine |= ((fresh >> k) & 1u && idx[k] == v) ? (1u << k) : 0u;
+        for (int k = 0; k < 5; k++) mine |= ((fresh >> k) & 1u && b[k] == v) ? (1u << k) : 0u;
         const uint32_t holders = __ballot_sync(0xffffffffu, mine != 0);
-        const uint32_t first = __ffs(holders) - 1;
         if (mine) {
-            // the first lane (in lane order) owns v at its lowest k; every
-            // other occurrence of v is not new
-            if (lane == first) {
-                const uint32_t keep = mine & (~mine + 1u);  // lowest set bit
-                fresh &= ~(mine & ~keep);
-            } else {
-                fresh &= ~mine;
-            }
+            if (lane == (uint32_t)(__ffs(holders) - 1)) fresh &= ~(mine & ~(mine & (~mine + 1u)));
+            else fresh &= ~mine;
         }
     }
     __syncwarp();
     if (lane == 0) *ndup = 0;
     __syncwarp();
-    (void)kKind;
     return fresh;
-}
-
-__device__ inline void undo_bits(uint32_t* bm, const uint32_t (&idx)[5], uint32_t flipped) {
-#pragma unroll
-    for (int k = 0; k < 5; k++)
-        if ((flipped >> k) & 1u) atomicAnd(&bm[idx[k] >> 5], ~(1u << (idx[k] & 31)));
-}
-
-__device__ inline void set_bits(uint32_t* bm, const uint32_t (&idx)[5]) {
-#pragma unroll
-    for (int k = 0; k < 5; k++) atomicOr(&bm[idx[k] >> 5], 1u << (idx[k] & 31));
 }
 
 __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     CommitSmem& S = reinterpret_cast<CommitSmem*>(smem)[wid];
+    for (uint32_t i = lane; i < 2048; i += 32) S.own[i] = 0;
     for (uint32_t fi = blockIdx.x * kCommitWarps + wid; fi < P.nfiles; fi += gridDim.x * kCommitWarps) {
         const uint32_t file = P.file_order[fi];
         const GenFile Fd = P.files[file];
@@ -592,85 +623,127 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
         uint32_t* out = P.out_filters + (size_t)Fd.filter_base * 64;
         for (uint32_t i = lane; i < 64; i += 32) S.F[i] = 0;
         for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
-        if (lane == 0) S.ndup[0] = S.ndup[1] = 0;
+        if (lane == 0) S.ndup = 0;
+        // the file's tiles are one contiguous range
+        const GenChunk c0 = P.chunks[Fd.first_chunk];
+        const GenChunk cl = P.chunks[Fd.first_chunk + Fd.nchunks - 1];
+        const uint32_t t_first = c0.first_tile, t_end = cl.first_tile + cl.ntiles;
+        uint32_t chunk = Fd.first_chunk;
+        uint32_t next_chunk_tile = (Fd.nchunks > 1) ? P.chunks[chunk + 1].first_tile : 0xFFFFFFFFu;
+        uint32_t nf_cur = t_first < t_end ? P.tile_out[t_first].count : 0;
+        uint32_t nf_next = t_first + 1 < t_end ? P.tile_out[t_first + 1].count : 0;
+        if (t_first < t_end) stage_tile(S.feat[0], P.features + (size_t)t_first * 5 * kTileCap, nf_cur, lane);
         __syncwarp();
-        uint32_t bf_count = 1, last_count = 0;
-        for (uint32_t c = Fd.first_chunk; c < Fd.first_chunk + Fd.nchunks; c++) {
-            const GenChunk C = P.chunks[c];
-            uint32_t bigfi = 0;  // local to each chunk (sdbf_core.cc:100)
-            for (uint32_t tj = 0; tj < C.ntiles; tj++) {
-                const uint32_t tile = C.first_tile + tj;
-                const uint32_t nf = P.tile_out[tile].count;
-                const uint32_t* feat = P.features + (size_t)tile * 5 * kTileCap;
-                for (uint32_t g0 = 0; g0 < nf; g0 += 32) {
-                    const uint32_t gi = g0 + lane;
-                    const bool have = gi < nf;
-                    uint32_t hw[5], a[5], b[5];
+        uint32_t bf_count = 1, last_count = 0, bigfi = 0;
+        for (uint32_t t = t_first; t < t_end; t++) {
+            const uint32_t cur = (t - t_first) & 1u;
+            // chunk boundary: the big-filter counter is local to each chunk
+            // (sdbf_core.cc:100); the big filter itself continues
+            while (t >= next_chunk_tile) {
+                bigfi = 0;
+                chunk++;
+                next_chunk_tile = (chunk + 1 < Fd.first_chunk + Fd.nchunks) ? P.chunks[chunk + 1].first_tile
+                                                                             : 0xFFFFFFFFu;
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            const uint32_t nf = nf_cur;
+            if (t + 1 < t_end)
+                stage_tile(S.feat[cur ^ 1u], P.features + (size_t)(t + 1) * 5 * kTileCap, nf_next, lane);
+            nf_cur = nf_next;
+            nf_next = t + 2 < t_end ? P.tile_out[t + 2].count : 0;
+            for (uint32_t g0 = 0; g0 < nf; g0 += 32) {
+                const uint32_t gi = g0 + lane;
+                const bool have = gi < nf;
+                uint32_t a[5], b[5];
 #pragma unroll
-                    for (int k = 0; k < 5; k++) {
-                        hw[k] = have ? feat[k * kTileCap + gi] : 0;
-                        a[k] = hw[k] & kBfMask;
-                        b[k] = hw[k] & kBigMask;
+                for (int k = 0; k < 5; k++) {
+                    const uint32_t h = have ? S.feat[cur][k][gi] : 0u;
+                    a[k] = h & kBfMask;
+                    b[k] = h & kBigMask;
+                }
+                uint32_t start = 0;
+                while (true) {
+                    const bool act = have && lane >= start;
+                    if (!__any_sync(0xffffffffu, act)) break;
+                    // small filter: new iff some index is unset in F and no
+                    // earlier lane of the group holds it (bf_sha1_insert)
+                    uint32_t fpre = 0;
+                    if (act) {
+#pragma unroll
+                        for (int k = 0; k < 5; k++) {
+                            fpre |= ((S.F[a[k] >> 5] >> (a[k] & 31)) & 1u) << k;
+                            atomicOr(&S.own[a[k]], 1u << lane);
+                        }
                     }
-                    uint32_t start = 0;
-                    while (true) {
-                        const bool act = have && lane >= start;
-                        if (!__any_sync(0xffffffffu, act)) break;
-                        uint32_t flF, flG;
-                        const uint32_t fnew = group_insert<0>(S.F, S.dup[0], &S.ndup[0], act, a, flF);
-                        const bool fpass = act && fnew != 0;
-                        const uint32_t gnew = group_insert<1>(S.G, S.dup[1], &S.ndup[1], fpass, b, flG);
-                        const bool counted = fpass && gnew != 0;
-                        const uint32_t cm = __ballot_sync(0xffffffffu, counted);
-                        const uint32_t before = __popc(cm & lanemask_le());
-                        // first lane at which a counter reaches its cap
-                        const bool hit_small = counted && (last_count + before == (uint32_t)kMaxElem);
-                        const bool hit_big = counted && (bigfi + before == (uint32_t)kBigElem);
-                        const uint32_t hm = __ballot_sync(0xffffffffu, hit_small || hit_big);
-                        if (hm == 0) {
-                            last_count += __popc(cm);
-                            bigfi += __popc(cm);
-                            break;
-                        }
-                        const uint32_t r = __ffs(hm) - 1;
-                        const bool roll_small = __shfl_sync(0xffffffffu, hit_small, r);
-                        const bool roll_big = __shfl_sync(0xffffffffu, hit_big, r);
-                        // lanes after r are re-processed: take their bits back,
-                        // then restore bits of lanes <= r that share them
-                        if (act && lane > r) {
-                            undo_bits(S.F, a, flF);
-                            if (fpass) undo_bits(S.G, b, flG);
-                        }
-                        __syncwarp();
-                        if (act && lane <= r) {
-                            set_bits(S.F, a);
-                            if (fpass) set_bits(S.G, b);
-                        }
-                        __syncwarp();
-                        const uint32_t ncnt = __popc(cm & ((2u << r) - 1u));
-                        last_count += ncnt;
-                        bigfi += ncnt;
-                        if (roll_small) {
-                            // filter full: emit and start the next one
-                            const bool fits = bf_count <= Fd.filter_cap;
-                            for (uint32_t i = lane; i < 64; i += 32) {
-                                if (fits) out[(size_t)(bf_count - 1) * 64 + i] = S.F[i];
-                                S.F[i] = 0;
-                            }
-                            if (!fits && lane == 0) atomicAdd(P.counters + 1, 1u);
-                            bf_count++;
-                            last_count = 0;
-                        }
-                        if (roll_big) {
-                            for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
-                            bigfi = 0;
-                        }
-                        __syncwarp();
-                        start = r + 1;
+                    __syncwarp();
+                    bool fpass = false;
+                    if (act) {
+#pragma unroll
+                        for (int k = 0; k < 5; k++)
+                            if (!((fpre >> k) & 1u) && (uint32_t)(__ffs(S.own[a[k]]) - 1) == lane) fpass = true;
                     }
+                    __syncwarp();
+                    if (act) {
+#pragma unroll
+                        for (int k = 0; k < 5; k++) S.own[a[k]] = 0;
+                    }
+                    uint32_t flG;
+                    const uint32_t gnew = big_insert(S.G, S.dup, &S.ndup, fpass, b, flG);
+                    const bool counted = fpass && gnew != 0;
+                    const uint32_t cm = __ballot_sync(0xffffffffu, counted);
+                    const uint32_t before = __popc(cm & lanemask_le());
+                    const bool hit_small = counted && (last_count + before == (uint32_t)kMaxElem);
+                    const bool hit_big = counted && (bigfi + before == (uint32_t)kBigElem);
+                    const uint32_t hm = __ballot_sync(0xffffffffu, hit_small || hit_big);
+                    const uint32_t r = hm ? (uint32_t)(__ffs(hm) - 1) : 31u;
+                    // lanes after r are re-processed: take back their big-filter
+                    // bits, restore bits of lanes <= r that share them
+                    if (hm && fpass && lane > r) {
+#pragma unroll
+                        for (int k = 0; k < 5; k++)
+                            if ((flG >> k) & 1u) atomicAnd(&S.G[b[k] >> 5], ~(1u << (b[k] & 31)));
+                    }
+                    __syncwarp();
+                    if (act && lane <= r) {
+#pragma unroll
+                        for (int k = 0; k < 5; k++) {
+                            atomicOr(&S.F[a[k] >> 5], 1u << (a[k] & 31));
+                            if (hm && fpass) atomicOr(&S.G[b[k] >> 5], 1u << (b[k] & 31));
+                        }
+                    }
+                    __syncwarp();
+                    if (!hm) {
+                        last_count += __popc(cm);
+                        bigfi += __popc(cm);
+                        break;
+                    }
+                    const bool roll_small = __shfl_sync(0xffffffffu, hit_small, r);
+                    const bool roll_big = __shfl_sync(0xffffffffu, hit_big, r);
+                    const uint32_t ncnt = __popc(cm & ((2u << r) - 1u));
+                    last_count += ncnt;
+                    bigfi += ncnt;
+                    if (roll_small) {
+                        const bool fits = bf_count <= Fd.filter_cap;
+                        for (uint32_t i = lane; i < 64; i += 32) {
+                            if (fits) out[(size_t)(bf_count - 1) * 64 + i] = S.F[i];
+                            S.F[i] = 0;
+                        }
+                        if (!fits && lane == 0) atomicAdd(P.counters + 1, 1u);
+                        bf_count++;
+                        last_count = 0;
+                    }
+                    if (roll_big) {
+                        for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
+                        bigfi = 0;
+                    }
+                    __syncwarp();
+                    start = r + 1;
                 }
             }
         }
+        cp_async_wait_all();
+        __syncwarp();
         // emit the current (last) filter, then the chop of sdbf_core.cc:235-238
         if (bf_count <= Fd.filter_cap) {
             for (uint32_t i = lane; i < 64; i += 32) out[(size_t)(bf_count - 1) * 64 + i] = S.F[i];

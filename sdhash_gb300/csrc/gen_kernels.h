@@ -9,12 +9,13 @@ namespace sdbfg {
 
 constexpr int kGenThreads = 128;     // CTA size of the tile / block kernels
 constexpr int kSegs = 64;            // popularity-chain segments per tile
-constexpr uint32_t kLead = 128;      // speculative lead-in steps per segment
+constexpr uint32_t kLead = 128;      // maximum speculative lead-in steps per segment
+constexpr uint32_t kDefaultLead = 96; // default lead-in (mis-speculation ~1e-4 per segment)
 constexpr uint32_t kTileL = 8192;    // window steps owned by a stream tile
 // at most one selected feature per 17 credited steps (score > 16), and a
 // tile's positions are credited by kTileL + 64 steps
-constexpr uint32_t kTileCap = (kTileL + 64) / 17 + 2;
-constexpr int kCommitWarps = 4;      // files per commit CTA
+constexpr uint32_t kTileCap = ((kTileL + 64) / 17 + 2 + 3) / 4 * 4;  // rows 16-byte aligned
+constexpr int kCommitWarps = 2;      // files per commit CTA
 constexpr uint32_t kMaxBlockBytes = 16384;  // dd block size limit (sdhash.cc:215-219)
 constexpr uint64_t kChunkBytes = 32ull << 20;  // stream chunk (sdbf_class.cc:43)
 

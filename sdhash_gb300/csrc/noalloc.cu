@@ -201,7 +201,7 @@ extern "C" int sdbfg_digest_stream_noalloc(const uint8_t* dev_data, const uint64
     P.counters = reinterpret_cast<uint32_t*>(base + kOffCounters);
     P.rank_tab = reinterpret_cast<const uint16_t*>(base + kOffRank);
     P.ent_tab = reinterpret_cast<const uint32_t*>(base + kOffEnt);
-    P.lead = kLead;
+    P.lead = kDefaultLead;
     const uint32_t cap3 = (uint32_t)sms * 3 * 16;
     if (ntiles) NA_TRY(launch_stream_tiles(P, ntiles < cap3 ? ntiles : cap3, st));
     if (nchunks) NA_TRY(launch_stream_verify(P, nchunks < cap3 ? nchunks : cap3, st));

@@ -93,7 +93,7 @@ struct sdbfg_ctx {
     std::string err;
     uint64_t launches = 0;
     int sms = 152;
-    uint32_t lead = kLead;
+    uint32_t lead = kDefaultLead;
     // constant tables
     DevBuf d_rank, d_ent, d_cut;
     // generation buffers

@@ -51,7 +51,7 @@ def test_short_lead_in_exercises_relink(ctx, golden, lead):
     try:
         out = ctx.digest_buffers([d.tobytes() for d in datas], [r["name"] for r in recs + big], 0)
     finally:
-        ctx.set_lead(128)
+        ctx.set_lead(96)
     bad = [r["name"] for r, d in zip(recs + big, out) if sha(d.to_string()) != r["sha256"]]
     assert not bad, bad
     if lead <= 17:
@@ -131,3 +131,17 @@ def test_reference_object_api(ctx, oracle):
     assert e.value.code == -3
     back = g.sdbf.from_string(sa.to_string())
     assert back.compare(sb, 0) == sa.compare(sb, 0)
+
+
+@pytest.mark.parametrize("lead", [0, 5])
+def test_short_lead_in_block_mode(ctx, golden, lead):
+    """Block mode re-walks mis-speculated segments inside each block."""
+    recs = [r for r in _golden_by_mode(golden)[16384] if r["status"] == 0]
+    datas = [cases.make(r["spec"]) for r in recs]
+    ctx.set_lead(lead)
+    try:
+        out = ctx.digest_buffers([d.tobytes() for d in datas], [r["name"] for r in recs], 16384)
+    finally:
+        ctx.set_lead(96)
+    bad = [r["name"] for r, d in zip(recs, out) if sha(d.to_string()) != r["sha256"]]
+    assert not bad, bad
