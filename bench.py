@@ -290,7 +290,12 @@ def main():
     dev_ms = e0.elapsed_time(e1)
     launches = ctx.launch_count - launches0
     tiles_ms, tiles_n = ctx.kernel_time("k_stream_tiles")
-    kern = {k: ctx.kernel_time(k) for k in ("k_stream_tiles", "k_stream_verify", "k_stream_commit", "k_pack_filters")}
+    kern = {k: ctx.kernel_time(k) for k in ("k_stream_tiles", "k_stream_verify", "k_stream_commit", "k_pack_filters",
+                                            "k_scan_offsets")}
+    ntile_ph = ctx.kernel_time("k_stream_tiles.count")[0] or 1.0
+    phases = {k: ctx.kernel_time("k_stream_tiles." + k)[0] / ntile_ph
+              for k in ("load", "ranks", "fres", "walk", "link", "compact", "sha1")}
+    commit_ph = {k: ctx.kernel_time("k_stream_commit." + k)[0] for k in ("wait", "busy", "groups", "loops", "max_file")}
     ctx.profile(False)
     ms_per_step = allmax(world, dev_ms / args.steps)
     bytes_all = allsum(world, total_bytes)
@@ -324,7 +329,8 @@ def main():
                 "traffic": (tpb * per_launch_bytes) if tpb else None,
                 "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
                 "algorithmic_bytes_per_launch": per_launch_bytes,
-                "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kern.items()}}
+                "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kern.items()},
+                "tile_phase_cycles_per_tile": phases, "commit_phase_totals": commit_ph}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",

@@ -54,7 +54,12 @@ uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx *ctx);
  * every launch (off by default; enabling clears previous totals).
  * sdbfg_ctx_kernel_time reports the accumulated milliseconds and launch
  * count of one kernel ("k_stream_tiles", "k_stream_verify",
- * "k_stream_commit", "k_pack_filters", "k_block_digest", "k_compare_pairs").
+ * "k_stream_commit", "k_pack_filters", "k_block_digest", "k_compare_pairs",
+ * "k_scan_offsets").  While profiling, the stream kernels also count SM
+ * cycles per phase; the names "k_stream_tiles.{load,ranks,fres,walk,link,
+ * compact,sha1}" and "k_stream_commit.{wait,busy,max_file}" report those
+ * cycles in *total_ms (and the tile count in *launches); ".count",
+ * ".groups", ".loops" report counts.
  * Instrumentation without a counterpart in the reference. */
 int sdbfg_ctx_profile(sdbfg_ctx *ctx, int enable);
 int sdbfg_ctx_kernel_time(sdbfg_ctx *ctx, const char *kernel, double *total_ms, uint64_t *launches);

@@ -296,17 +296,24 @@ __device__ inline bool same_state(uint64_t a, uint64_t b) { return a == b; }
 // S0 is known (re-computation after a failed link check); otherwise thread 0
 // starts speculatively kLead steps early.  Returns (in misc[0]) the number
 // of features, and writes sig_in / tau_out for the tile.
+__device__ __forceinline__ void stamp(long long* tm, int k) {
+    if (tm && threadIdx.x == 0) tm[k] = clock64();
+}
+
 __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom& g, const TileSmem& s,
                               const uint16_t* rank_tab, const uint32_t* ent_tab, const uint64_t* entry,
-                              uint64_t* sig_in, uint64_t* tau_out, uint32_t lead) {
+                              uint64_t* sig_in, uint64_t* tau_out, uint32_t lead, long long* tm) {
+    stamp(tm, 0);
     load_bytes(chunk, g, s.bytes32);
     {
         uint4* h4 = reinterpret_cast<uint4*>(s.hist);
         for (uint32_t i = threadIdx.x; i < 256 * kGenThreads / 16; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
     }
     __syncthreads();
+    stamp(tm, 1);
     compute_ranks(g, s, rank_tab, ent_tab);
     __syncthreads();
+    stamp(tm, 2);
     compute_fres(g, s);
     // clear scores (aliases the histogram area, free after phase 2)
     for (uint32_t i = threadIdx.x; i < (g.L + 3) / 4 + 1; i += blockDim.x) s.score32[i] = 0;
@@ -318,6 +325,7 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
         s.misc[11] = 0;
     }
     __syncthreads();
+    stamp(tm, 3);
     // segments over steps [S0, SE)
     const uint32_t total = g.SE > g.S0 ? g.SE - g.S0 : 0;
     const uint32_t SL = (total + kSegs - 1) / kSegs;
@@ -359,6 +367,7 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
         }
     }
     __syncthreads();
+    stamp(tm, 4);
     // phase 5: link segments inside the tile (serial, normally no work)
     if (t == 0 && SL > 0) {
         for (uint32_t q = 1; q < kSegs; q++) {
@@ -388,6 +397,7 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
         if (tau_out) *tau_out = *reinterpret_cast<uint64_t*>(&s.misc[10]);
     }
     __syncthreads();
+    stamp(tm, 5);
 }
 
 // ------------------------------------------- phase 6: ordered compaction
@@ -470,10 +480,13 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
     for (uint32_t i = threadIdx.x; i < 66; i += blockDim.x) ent_tab[i] = i < 65 ? P.ent_tab[i] : 0;
     __syncthreads();
     TileOut* out = P.tile_out + tile;
-    tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, entry, &out->sig_in, &out->tau_out, P.lead);
+    long long tm[9];
+    tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, entry, &out->sig_in, &out->tau_out, P.lead,
+                  P.phase ? tm : nullptr);
     const uint32_t nown = g.SE > g.t0 ? g.SE - g.t0 : 0;
     __shared__ uint32_t counts[kGenThreads / 32];
     const uint32_t nf = compact(s, nown, kThreshold, false, counts);
+    stamp(P.phase ? tm : nullptr, 6);
     // SHA-1 of each selected feature (sdbf_core.cc:103-105)
     uint32_t* feat = P.features + (size_t)tile * 5 * kTileCap;
     const uint32_t off = g.t0 - g.Q0;
@@ -488,6 +501,14 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
     if (threadIdx.x == 0) {
         out->count = nf;
         out->fixups = s.misc[9];
+    }
+    if (P.phase) {
+        __syncthreads();
+        stamp(tm, 7);
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < 7; k++) atomicAdd(P.phase + k, (unsigned long long)(tm[k + 1] - tm[k]));
+            atomicAdd(P.phase + kPhTiles, 1ull);
+        }
     }
 }
 
@@ -635,6 +656,8 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
         if (t_first < t_end) stage_tile(S.feat[0], P.features + (size_t)t_first * 5 * kTileCap, nf_cur, lane);
         __syncwarp();
         uint32_t bf_count = 1, last_count = 0, bigfi = 0;
+        long long t_file = clock64(), t_wait = 0;
+        uint32_t n_groups = 0, n_loops = 0;
         for (uint32_t t = t_first; t < t_end; t++) {
             const uint32_t cur = (t - t_first) & 1u;
             // chunk boundary: the big-filter counter is local to each chunk
@@ -645,8 +668,10 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                 next_chunk_tile = (chunk + 1 < Fd.first_chunk + Fd.nchunks) ? P.chunks[chunk + 1].first_tile
                                                                              : 0xFFFFFFFFu;
             }
+            const long long w0 = clock64();
             cp_async_wait_all();
             __syncwarp();
+            t_wait += clock64() - w0;
             const uint32_t nf = nf_cur;
             if (t + 1 < t_end)
                 stage_tile(S.feat[cur ^ 1u], P.features + (size_t)(t + 1) * 5 * kTileCap, nf_next, lane);
@@ -663,9 +688,11 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                     b[k] = h & kBigMask;
                 }
                 uint32_t start = 0;
+                n_groups++;
                 while (true) {
                     const bool act = have && lane >= start;
                     if (!__any_sync(0xffffffffu, act)) break;
+                    n_loops++;
                     // small filter: new iff some index is unset in F and no
                     // earlier lane of the group holds it (bf_sha1_insert)
                     uint32_t fpre = 0;
@@ -757,6 +784,14 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
         if (lane == 0) {
             P.out_info[file].bf_count = bf_count;
             P.out_info[file].last_count = last_count;
+            if (P.phase) {
+                const long long busy = clock64() - t_file;
+                atomicAdd(P.phase + kPhCommitWait, (unsigned long long)t_wait);
+                atomicAdd(P.phase + kPhCommitBusy, (unsigned long long)busy);
+                atomicAdd(P.phase + kPhCommitGroups, (unsigned long long)n_groups);
+                atomicAdd(P.phase + kPhCommitLoops, (unsigned long long)n_loops);
+                atomicMax(P.phase + kPhCommitMaxFile, (unsigned long long)busy);
+            }
         }
         __syncwarp();
     }
@@ -792,7 +827,7 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
     for (uint32_t b = blockIdx.x; b < P.nchunks; b += gridDim.x) {
         const GenChunk C = P.chunks[b];
         const TileGeom g = block_geom(C.n);
-        tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, nullptr, nullptr, nullptr, P.lead);
+        tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, nullptr, nullptr, nullptr, P.lead, nullptr);
         const uint8_t* sc = reinterpret_cast<const uint8_t*>(s.score32);
         const uint32_t nown = g.SE;
         if (threadIdx.x < 66) histo[threadIdx.x] = 0;

@@ -11,7 +11,10 @@ constexpr int kGenThreads = 128;     // CTA size of the tile / block kernels
 constexpr int kSegs = 64;            // popularity-chain segments per tile
 constexpr uint32_t kLead = 128;      // maximum speculative lead-in steps per segment
 constexpr uint32_t kDefaultLead = 96; // default lead-in (mis-speculation ~1e-4 per segment)
-constexpr uint32_t kTileL = 8192;    // window steps owned by a stream tile
+// window steps owned by a stream tile: with the 64-step credit halo and the
+// 128-step maximum lead-in a tile simulates 8192 steps = 128 aligned
+// 64-step blocks, one per thread of the full-rescan table
+constexpr uint32_t kTileL = 8000;
 // at most one selected feature per 17 credited steps (score > 16), and a
 // tile's positions are credited by kTileL + 64 steps
 constexpr uint32_t kTileCap = ((kTileL + 64) / 17 + 2 + 3) / 4 * 4;  // rows 16-byte aligned
@@ -73,6 +76,13 @@ struct GenParams {
     const uint32_t* ent_tab;     // device copy of SDBF_ENTROPY64
     uint32_t block_lmax;         // block mode: max window steps per block
     uint32_t lead;               // speculative lead-in steps (<= kLead)
+    unsigned long long* phase;   // optional phase cycle counters (kPhase*), null = off
+};
+
+// Phase counters (cycles summed over CTAs / warps) when GenParams::phase is set.
+enum : int {
+    kPhLoad = 0, kPhRanks, kPhFres, kPhWalk, kPhLink, kPhCompact, kPhSha, kPhTiles,
+    kPhCommitWait, kPhCommitBusy, kPhCommitGroups, kPhCommitLoops, kPhCommitMaxFile, kPhCount
 };
 
 size_t stream_tile_smem();

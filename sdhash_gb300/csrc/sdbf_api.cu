@@ -102,6 +102,17 @@ struct sdbfg_ctx {
     HostBuf h_stage;
     // comparison buffers
     DevBuf d_pairs, d_scores;
+    // stream-mode pipeline: two launch-group slots on their own streams
+    struct Slot {
+        cudaStream_t stream = nullptr;
+        cudaEvent_t done = nullptr;
+        bool used = false;
+        DevBuf data, chunks, tiles, files, order, tile_out, features, work;
+        HostBuf h_tables;
+    } slot[2];
+    DevBuf d_binfo, d_boff, d_total, d_phase;
+    cudaEvent_t ev_scan[2] = {nullptr, nullptr};
+    cudaEvent_t ev_start = nullptr;
 };
 
 struct sdbfg_set {
@@ -114,19 +125,19 @@ struct sdbfg_set {
 };
 
 // Per-kernel CUDA-event timing on the launch stream (only when enabled).
-static void timer_begin(sdbfg_ctx* c, const char* name, cudaEvent_t* a) {
+static void timer_begin(sdbfg_ctx* c, const char* name, cudaEvent_t* a, cudaStream_t st) {
     *a = nullptr;
     if (!c->profile) return;
     cudaEventCreate(a);
-    cudaEventRecord(*a, c->stream);
+    cudaEventRecord(*a, st);
     (void)name;
 }
 
-static void timer_end(sdbfg_ctx* c, const char* name, cudaEvent_t a) {
+static void timer_end(sdbfg_ctx* c, const char* name, cudaEvent_t a, cudaStream_t st) {
     if (!c->profile || !a) return;
     cudaEvent_t b;
     cudaEventCreate(&b);
-    cudaEventRecord(b, c->stream);
+    cudaEventRecord(b, st);
     c->pending.push_back({name, a, b});
 }
 
@@ -150,16 +161,17 @@ static void timer_collect(sdbfg_ctx* c) {
     c->pending.clear();
 }
 
-#define TIMED_LAUNCH(c, name, expr)             \
+#define TIMED_LAUNCH_ON(c, name, st_, expr)     \
     do {                                        \
         cudaEvent_t ev_;                        \
-        timer_begin((c), (name), &ev_);         \
+        timer_begin((c), (name), &ev_, (st_));  \
         cudaError_t le_ = (expr);               \
-        timer_end((c), (name), ev_);            \
+        timer_end((c), (name), ev_, (st_));     \
         if (le_ != cudaSuccess)                 \
             return fail((c), SDBFG_ERR_CUDA, "%s launch: %s", (name), cudaGetErrorString(le_)); \
         (c)->launches += 1;                     \
     } while (0)
+#define TIMED_LAUNCH(c, name, expr) TIMED_LAUNCH_ON(c, name, (c)->stream, expr)
 
 static int fail(sdbfg_ctx* c, int code, const char* fmt, ...);
 
@@ -219,8 +231,18 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
     for (DevBuf* b : {&c->d_rank, &c->d_ent, &c->d_cut, &c->d_data, &c->d_chunks, &c->d_tiles, &c->d_files,
                       &c->d_order, &c->d_tile_out, &c->d_features, &c->d_work_filters, &c->d_info,
                       &c->d_counters, &c->d_pack_src, &c->d_pack_dst_off, &c->d_out_filters, &c->d_out_counts,
-                      &c->d_pairs, &c->d_scores})
+                      &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase})
         b->release();
+    for (auto& S : c->slot) {
+        for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work})
+            b->release();
+        S.h_tables.release();
+        if (S.stream) cudaStreamDestroy(S.stream);
+        if (S.done) cudaEventDestroy(S.done);
+    }
+    for (cudaEvent_t e : c->ev_scan)
+        if (e) cudaEventDestroy(e);
+    if (c->ev_start) cudaEventDestroy(c->ev_start);
     c->h_stage.release();
     timer_collect(c);
     if (c->own) cudaStreamDestroy(c->own);
@@ -247,15 +269,33 @@ extern "C" int sdbfg_ctx_profile(sdbfg_ctx* c, int enable) {
     if (!c) return SDBFG_ERR_ARG;
     timer_collect(c);
     c->profile = enable != 0;
-    if (enable) c->stats.clear();
+    if (enable) {
+        c->stats.clear();
+        CUDA_TRY(c, c->d_phase.ensure(kPhCount * sizeof(unsigned long long)));
+        CUDA_TRY(c, cudaMemset(c->d_phase.p, 0, kPhCount * sizeof(unsigned long long)));
+    }
     return SDBFG_OK;
 }
+
+static const char* kPhaseNames[kPhCount] = {
+    "k_stream_tiles.load", "k_stream_tiles.ranks", "k_stream_tiles.fres", "k_stream_tiles.walk",
+    "k_stream_tiles.link", "k_stream_tiles.compact", "k_stream_tiles.sha1", "k_stream_tiles.count",
+    "k_stream_commit.wait", "k_stream_commit.busy", "k_stream_commit.groups", "k_stream_commit.loops",
+    "k_stream_commit.max_file"};
 
 extern "C" int sdbfg_ctx_kernel_time(sdbfg_ctx* c, const char* name, double* total_ms, uint64_t* launches) {
     if (!c || !name) return SDBFG_ERR_ARG;
     timer_collect(c);
     if (total_ms) *total_ms = 0;
     if (launches) *launches = 0;
+    for (int k = 0; k < kPhCount; k++)
+        if (!strcmp(name, kPhaseNames[k]) && c->d_phase.p) {
+            unsigned long long v[kPhCount];
+            CUDA_TRY(c, cudaMemcpy(v, c->d_phase.p, sizeof v, cudaMemcpyDeviceToHost));
+            if (total_ms) *total_ms = (double)v[k];
+            if (launches) *launches = v[kPhTiles];
+            return SDBFG_OK;
+        }
     for (const KernelStat& k : c->stats)
         if (k.name == name) {
             if (total_ms) *total_ms = k.ms;
@@ -385,109 +425,242 @@ static int digest_group_device(sdbfg_ctx* c, const uint8_t* dev_base, const std:
         CUDA_TRY(c, cudaStreamSynchronize(st));
         return SDBFG_OK;
     }
-    // ---- stream mode
-    std::vector<GenChunk> chunks;
-    std::vector<GenTile> tiles;
-    std::vector<GenFile> files(g.count);
-    std::vector<uint64_t> work_base(g.count);
-    uint64_t work_slots = 0;
-    for (uint32_t k = 0; k < g.count; k++) {
-        const uint32_t i = g.first + k;
-        GenFile f{(uint32_t)chunks.size(), 0, work_slots, 0};
-        if (lens[i] >= kMinFile) {
-            for (uint64_t pos = 0; pos < lens[i]; pos += kChunkBytes) {
-                const uint32_t m = (uint32_t)std::min<uint64_t>(kChunkBytes, lens[i] - pos);
-                GenChunk ch{dev_off[k] + pos, m, k, (uint32_t)tiles.size(), 0, 0, 0};
-                if (m > 64) {
-                    for (uint32_t t0 = 0; t0 < m - 64; t0 += kTileL) tiles.push_back({(uint32_t)chunks.size(), t0});
-                }
-                ch.ntiles = (uint32_t)tiles.size() - ch.first_tile;
-                chunks.push_back(ch);
-                f.nchunks++;
-            }
-            work_base[k] = work_slots;
-            f.filter_cap = stream_cap(lens[i]);
-            work_slots += f.filter_cap;
+    return fail(c, SDBFG_ERR_ARG, "internal: stream mode goes through the pipeline");
+}
+
+// ---------------------------------------------------- stream pipeline
+// Output slots of one launch group: exclusive scan of the files' filter
+// counts, continuing from the running total of the earlier groups
+// (*total), so the packed layout follows input order.
+__global__ void k_scan_offsets(const FileInfoDev* __restrict__ info, uint64_t* __restrict__ dst_off, uint32_t n,
+                               uint64_t* __restrict__ total) {
+    __shared__ uint64_t warp_sums[32];
+    __shared__ uint64_t carry;
+    if (threadIdx.x == 0) carry = *total;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < n; base += blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint64_t v = i < n ? info[i].bf_count : 0;
+        uint64_t incl = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
         }
-        files[k] = f;
+        if (lane == 31) warp_sums[wid] = incl;
+        __syncthreads();
+        uint64_t woff = 0, tot = 0;
+        for (uint32_t w = 0; w < blockDim.x / 32; w++) {
+            if (w < wid) woff += warp_sums[w];
+            tot += warp_sums[w];
+        }
+        if (i < n) dst_off[i] = carry + woff + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
     }
-    std::vector<uint32_t> order(g.count);
-    std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t a, uint32_t b) { return lens[g.first + a] > lens[g.first + b]; });
-    CUDA_TRY(c, c->d_chunks.ensure(std::max<size_t>(1, chunks.size()) * sizeof(GenChunk)));
-    CUDA_TRY(c, c->d_tiles.ensure(std::max<size_t>(1, tiles.size()) * sizeof(GenTile)));
-    CUDA_TRY(c, c->d_files.ensure(files.size() * sizeof(GenFile)));
-    CUDA_TRY(c, c->d_order.ensure(order.size() * sizeof(uint32_t) * 2));
-    CUDA_TRY(c, c->d_tile_out.ensure(std::max<size_t>(1, tiles.size()) * sizeof(TileOut)));
-    CUDA_TRY(c, c->d_features.ensure(std::max<size_t>(1, tiles.size()) * 5ull * kTileCap * 4));
-    CUDA_TRY(c, c->d_work_filters.ensure(std::max<uint64_t>(1, work_slots) * 256));
-    CUDA_TRY(c, c->d_info.ensure(files.size() * sizeof(FileInfoDev)));
-    CUDA_TRY(c, cudaMemcpyAsync(c->d_chunks.p, chunks.data(), chunks.size() * sizeof(GenChunk),
-                                cudaMemcpyHostToDevice, st));
-    CUDA_TRY(c, cudaMemcpyAsync(c->d_tiles.p, tiles.data(), tiles.size() * sizeof(GenTile), cudaMemcpyHostToDevice,
-                                st));
-    CUDA_TRY(c, cudaMemcpyAsync(c->d_files.p, files.data(), files.size() * sizeof(GenFile), cudaMemcpyHostToDevice,
-                                st));
-    CUDA_TRY(c, cudaMemcpyAsync(c->d_order.p, order.data(), order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                                st));
-    CUDA_TRY(c, cudaMemsetAsync(c->d_info.p, 0, files.size() * sizeof(FileInfoDev), st));
-    P.chunks = c->d_chunks.as<GenChunk>();
-    P.nchunks = (uint32_t)chunks.size();
-    P.tiles = c->d_tiles.as<GenTile>();
-    P.ntiles = (uint32_t)tiles.size();
-    P.files = c->d_files.as<GenFile>();
-    P.file_order = c->d_order.as<uint32_t>();
-    P.nfiles = g.count;
-    P.tile_out = c->d_tile_out.as<TileOut>();
-    P.features = c->d_features.as<uint32_t>();
-    P.out_filters = c->d_work_filters.as<uint32_t>();
-    P.out_info = c->d_info.as<FileInfoDev>();
-    const uint32_t grid_tiles = (uint32_t)std::min<size_t>(tiles.size(), (size_t)c->sms * 3 * 16);
-    const uint32_t grid_chunks = (uint32_t)std::min<size_t>(chunks.size(), (size_t)c->sms * 3 * 16);
-    const uint32_t grid_commit =
-        (uint32_t)std::min<size_t>((g.count + kCommitWarps - 1) / kCommitWarps, (size_t)c->sms * 3 * 16);
-    if (P.ntiles) TIMED_LAUNCH(c, "k_stream_tiles", launch_stream_tiles(P, std::max(1u, grid_tiles), st));
-    if (P.nchunks) TIMED_LAUNCH(c, "k_stream_verify", launch_stream_verify(P, std::max(1u, grid_chunks), st));
-    if (P.nfiles) TIMED_LAUNCH(c, "k_stream_commit", launch_stream_commit(P, std::max(1u, grid_commit), st));
-    // per-file results
-    std::vector<FileInfoDev> info(g.count);
-    CUDA_TRY(c, cudaMemcpyAsync(info.data(), c->d_info.p, info.size() * sizeof(FileInfoDev), cudaMemcpyDeviceToHost,
-                                st));
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_pack_group(const uint32_t* __restrict__ work, const GenFile* __restrict__ files,
+                             const FileInfoDev* __restrict__ info, const uint64_t* __restrict__ dst_off,
+                             uint32_t* __restrict__ dst, uint32_t n) {
+    for (uint32_t f = blockIdx.x; f < n; f += gridDim.x) {
+        if (files[f].nchunks == 0) continue;
+        const uint64_t words = (uint64_t)info[f].bf_count * 64;
+        const uint4* s = reinterpret_cast<const uint4*>(work + files[f].filter_base * 64);
+        uint4* d = reinterpret_cast<uint4*>(dst + dst_off[f] * 64);
+        for (uint64_t q = threadIdx.x; q < words / 4; q += blockDim.x) d[q] = s[q];
+    }
+}
+
+static int ensure_pipeline(sdbfg_ctx* c) {
+    for (int k = 0; k < 2; k++) {
+        if (!c->slot[k].stream) {
+            CUDA_TRY(c, cudaStreamCreateWithFlags(&c->slot[k].stream, cudaStreamNonBlocking));
+            CUDA_TRY(c, cudaEventCreateWithFlags(&c->slot[k].done, cudaEventDisableTiming));
+            CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_scan[k], cudaEventDisableTiming));
+        }
+    }
+    if (!c->ev_start) CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming));
+    return SDBFG_OK;
+}
+
+// Stream-mode digests of n inputs.  Inputs are either already on the device
+// (dev_data + offsets[i], 16-byte aligned) or in host memory (host_data +
+// offsets[i]) and copied per launch group.  Filters are packed in input
+// order into dev_out (device); results[] gets counts and slots.  Launch
+// groups alternate between two streams with their own workspaces, so the
+// commit of one group overlaps the tiles (and the input copy) of the next;
+// the host synchronises once, at the end.
+static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const uint8_t* dev_data,
+                                   const uint64_t* offsets, const uint64_t* lens, uint32_t n, uint32_t* dev_out,
+                                   uint64_t out_cap, sdbfg_digest_result* res, uint64_t* total_out) {
+    int rc = ensure_pipeline(c);
+    if (rc) return rc;
+    CUDA_TRY(c, c->d_binfo.ensure(std::max<size_t>(1, n) * sizeof(FileInfoDev)));
+    CUDA_TRY(c, c->d_boff.ensure(std::max<size_t>(1, n) * sizeof(uint64_t)));
+    CUDA_TRY(c, c->d_total.ensure(64));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_binfo.p, 0, std::max<size_t>(1, n) * sizeof(FileInfoDev), c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_total.p, 0, 64, c->stream));
+    CUDA_TRY(c, cudaEventRecord(c->ev_start, c->stream));
+    const std::vector<Group> groups = make_groups(lens, n, 0);
+    cudaEvent_t prev_scan = c->ev_start;
+    for (size_t gi = 0; gi < groups.size(); gi++) {
+        const Group& g = groups[gi];
+        sdbfg_ctx::Slot& S = c->slot[gi & 1];
+        cudaStream_t st = S.stream;
+        if (S.used) CUDA_TRY(c, cudaEventSynchronize(S.done));  // its pinned tables may be reused now
+        S.used = true;
+        CUDA_TRY(c, cudaStreamWaitEvent(st, c->ev_start, 0));
+        // ---- work lists (pinned host staging, copied asynchronously)
+        uint64_t nchunks = 0, ntiles = 0, bytes = 0;
+        for (uint32_t k = 0; k < g.count; k++) {
+            const uint64_t len = lens[g.first + k];
+            bytes += (len + 15) & ~15ull;
+            if (len < kMinFile) continue;
+            for (uint64_t pos = 0; pos < len; pos += kChunkBytes) {
+                const uint64_t m = std::min<uint64_t>(kChunkBytes, len - pos);
+                nchunks++;
+                if (m > 64) ntiles += (m - 64 + kTileL - 1) / kTileL;
+            }
+        }
+        const size_t tb_chunks = nchunks * sizeof(GenChunk), tb_tiles = ntiles * sizeof(GenTile);
+        const size_t tb_files = g.count * sizeof(GenFile), tb_order = g.count * sizeof(uint32_t);
+        CUDA_TRY(c, S.h_tables.ensure(tb_chunks + tb_tiles + tb_files + tb_order + 64));
+        GenChunk* hc = reinterpret_cast<GenChunk*>(S.h_tables.p);
+        GenTile* ht = reinterpret_cast<GenTile*>(reinterpret_cast<uint8_t*>(S.h_tables.p) + tb_chunks);
+        GenFile* hf = reinterpret_cast<GenFile*>(reinterpret_cast<uint8_t*>(ht) + tb_tiles);
+        uint32_t* ho = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(hf) + tb_files);
+        const uint8_t* gdata;
+        std::vector<uint64_t> doff(g.count);
+        if (dev_data) {
+            gdata = dev_data;
+            for (uint32_t k = 0; k < g.count; k++) doff[k] = offsets[g.first + k];
+        } else {
+            CUDA_TRY(c, S.data.ensure(std::max<uint64_t>(16, bytes)));
+            gdata = S.data.as<uint8_t>();
+            uint64_t b = 0;
+            for (uint32_t k = 0; k < g.count; k++) {
+                doff[k] = b;
+                b += (lens[g.first + k] + 15) & ~15ull;
+            }
+            bool contiguous = true;
+            for (uint32_t k = 0; k < g.count && contiguous; k++)
+                contiguous = offsets[g.first + k] - offsets[g.first] == doff[k];
+            if (contiguous) {
+                CUDA_TRY(c, cudaMemcpyAsync(S.data.p, host_data + offsets[g.first], bytes, cudaMemcpyHostToDevice, st));
+            } else {
+                for (uint32_t k = 0; k < g.count; k++) {
+                    const uint32_t i = g.first + k;
+                    if (lens[i] < kMinFile) continue;
+                    CUDA_TRY(c, cudaMemcpyAsync(S.data.as<uint8_t>() + doff[k], host_data + offsets[i], lens[i],
+                                                cudaMemcpyHostToDevice, st));
+                }
+            }
+        }
+        uint32_t ci = 0, ti = 0;
+        uint64_t work = 0;
+        for (uint32_t k = 0; k < g.count; k++) {
+            const uint32_t i = g.first + k;
+            GenFile f{ci, 0, work, 0};
+            if (lens[i] >= kMinFile) {
+                for (uint64_t pos = 0; pos < lens[i]; pos += kChunkBytes) {
+                    const uint32_t m = (uint32_t)std::min<uint64_t>(kChunkBytes, lens[i] - pos);
+                    GenChunk ch{doff[k] + pos, m, k, ti, 0, 0, 0};
+                    if (m > 64)
+                        for (uint32_t t0 = 0; t0 < m - 64; t0 += kTileL) ht[ti++] = GenTile{ci, t0};
+                    ch.ntiles = ti - ch.first_tile;
+                    hc[ci++] = ch;
+                    f.nchunks++;
+                }
+                f.filter_cap = stream_cap(lens[i]);
+                work += f.filter_cap;
+            }
+            hf[k] = f;
+            ho[k] = k;
+        }
+        std::stable_sort(ho, ho + g.count, [&](uint32_t a, uint32_t b) { return lens[g.first + a] > lens[g.first + b]; });
+        CUDA_TRY(c, S.chunks.ensure(std::max<size_t>(1, tb_chunks)));
+        CUDA_TRY(c, S.tiles.ensure(std::max<size_t>(1, tb_tiles)));
+        CUDA_TRY(c, S.files.ensure(std::max<size_t>(1, tb_files)));
+        CUDA_TRY(c, S.order.ensure(std::max<size_t>(1, tb_order)));
+        CUDA_TRY(c, S.tile_out.ensure(std::max<uint64_t>(1, ntiles) * sizeof(TileOut)));
+        CUDA_TRY(c, S.features.ensure(std::max<uint64_t>(1, ntiles) * 5ull * kTileCap * 4));
+        CUDA_TRY(c, S.work.ensure(std::max<uint64_t>(1, work) * 256));
+        if (tb_chunks) CUDA_TRY(c, cudaMemcpyAsync(S.chunks.p, hc, tb_chunks, cudaMemcpyHostToDevice, st));
+        if (tb_tiles) CUDA_TRY(c, cudaMemcpyAsync(S.tiles.p, ht, tb_tiles, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(S.files.p, hf, tb_files, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(c, cudaMemcpyAsync(S.order.p, ho, tb_order, cudaMemcpyHostToDevice, st));
+        GenParams P{};
+        P.data = gdata;
+        P.rank_tab = c->d_rank.as<uint16_t>();
+        P.ent_tab = c->d_ent.as<uint32_t>();
+        P.counters = c->d_counters.as<uint32_t>();
+        P.lead = c->lead;
+        P.phase = c->profile ? c->d_phase.as<unsigned long long>() : nullptr;
+        P.chunks = S.chunks.as<GenChunk>();
+        P.nchunks = (uint32_t)nchunks;
+        P.tiles = S.tiles.as<GenTile>();
+        P.ntiles = (uint32_t)ntiles;
+        P.files = S.files.as<GenFile>();
+        P.file_order = S.order.as<uint32_t>();
+        P.nfiles = g.count;
+        P.tile_out = S.tile_out.as<TileOut>();
+        P.features = S.features.as<uint32_t>();
+        P.out_filters = S.work.as<uint32_t>();
+        P.out_info = c->d_binfo.as<FileInfoDev>() + g.first;
+        const uint32_t cap_grid = (uint32_t)c->sms * 3 * 16;
+        if (P.ntiles)
+            TIMED_LAUNCH_ON(c, "k_stream_tiles", st, launch_stream_tiles(P, std::min<uint32_t>(P.ntiles, cap_grid), st));
+        if (P.nchunks)
+            TIMED_LAUNCH_ON(c, "k_stream_verify", st,
+                            launch_stream_verify(P, std::min<uint32_t>(P.nchunks, cap_grid), st));
+        TIMED_LAUNCH_ON(c, "k_stream_commit", st,
+                        launch_stream_commit(P, std::min<uint32_t>((g.count + kCommitWarps - 1) / kCommitWarps,
+                                                                   cap_grid), st));
+        // output slots follow input order: scan after the previous group's scan
+        CUDA_TRY(c, cudaStreamWaitEvent(st, prev_scan, 0));
+        TIMED_LAUNCH_ON(c, "k_scan_offsets", st,
+                        (k_scan_offsets<<<1, 1024, 0, st>>>(c->d_binfo.as<FileInfoDev>() + g.first,
+                                                             c->d_boff.as<uint64_t>() + g.first, g.count,
+                                                             c->d_total.as<uint64_t>()),
+                         cudaGetLastError()));
+        CUDA_TRY(c, cudaEventRecord(c->ev_scan[gi & 1], st));
+        prev_scan = c->ev_scan[gi & 1];
+        TIMED_LAUNCH_ON(c, "k_pack_filters", st,
+                        (k_pack_group<<<std::min<uint32_t>(g.count, (uint32_t)c->sms * 8), 256, 0, st>>>(
+                             S.work.as<uint32_t>(), S.files.as<GenFile>(), c->d_binfo.as<FileInfoDev>() + g.first,
+                             c->d_boff.as<uint64_t>() + g.first, dev_out, g.count),
+                         cudaGetLastError()));
+        CUDA_TRY(c, cudaEventRecord(S.done, st));
+    }
+    // join: the caller's stream waits for both slots, then results come back
+    for (int k = 0; k < 2; k++)
+        if (c->slot[k].used) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->slot[k].done, 0));
+    std::vector<FileInfoDev> info(n);
+    std::vector<uint64_t> off(n);
+    uint64_t flags_total[2] = {0, 0};
     uint32_t flags[2] = {0, 0};
-    CUDA_TRY(c, cudaMemcpyAsync(flags, c->d_counters.p, sizeof flags, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(c, cudaStreamSynchronize(st));
+    if (n) {
+        CUDA_TRY(c, cudaMemcpyAsync(info.data(), c->d_binfo.p, n * sizeof(FileInfoDev), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(off.data(), c->d_boff.p, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, c->stream));
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(flags_total, c->d_total.p, 8, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(flags, c->d_counters.p, sizeof flags, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     if (flags[1]) return fail(c, SDBFG_ERR_CUDA, "internal error: stream digest exceeded its filter bound");
-    std::vector<uint64_t> src_off, dst_off;
-    std::vector<uint32_t> ids;
-    for (uint32_t k = 0; k < g.count; k++) {
-        const uint32_t i = g.first + k;
+    if (flags_total[0] > out_cap)
+        return fail(c, SDBFG_ERR_CAPACITY, "output capacity %llu filters < %llu needed", (unsigned long long)out_cap,
+                    (unsigned long long)flags_total[0]);
+    for (uint32_t i = 0; i < n; i++) {
         if (lens[i] < kMinFile) continue;
-        res[i].bf_count = info[k].bf_count;
-        res[i].last_count = info[k].last_count;
-        res[i].filter_offset = *next_slot;
-        src_off.push_back(work_base[k]);
-        dst_off.push_back(*next_slot);
-        ids.push_back(k);
-        *next_slot += info[k].bf_count;
+        res[i].bf_count = info[i].bf_count;
+        res[i].last_count = info[i].last_count;
+        res[i].filter_offset = off[i];
     }
-    if (*next_slot > out_cap) return fail(c, SDBFG_ERR_CAPACITY, "output capacity %llu filters < %llu needed",
-                                          (unsigned long long)out_cap, (unsigned long long)*next_slot);
-    if (!ids.empty()) {
-        CUDA_TRY(c, c->d_pack_src.ensure(ids.size() * 8 * 2 + ids.size() * 4));
-        uint64_t* d_src = c->d_pack_src.as<uint64_t>();
-        uint64_t* d_dst = d_src + ids.size();
-        uint32_t* d_ids = reinterpret_cast<uint32_t*>(d_dst + ids.size());
-        CUDA_TRY(c, cudaMemcpyAsync(d_src, src_off.data(), ids.size() * 8, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(c, cudaMemcpyAsync(d_dst, dst_off.data(), ids.size() * 8, cudaMemcpyHostToDevice, st));
-        CUDA_TRY(c, cudaMemcpyAsync(d_ids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice, st));
-        const uint32_t grid = (uint32_t)std::min<size_t>(ids.size(), (size_t)c->sms * 8);
-        TIMED_LAUNCH(c, "k_pack_filters",
-                     (k_pack_filters<<<grid, 256, 0, st>>>(c->d_work_filters.as<uint32_t>(), dev_out, d_src, d_dst,
-                                                           c->d_info.as<FileInfoDev>(), d_ids, (uint32_t)ids.size()),
-                      cudaGetLastError()));
-        CUDA_TRY(c, cudaStreamSynchronize(st));
-    }
+    if (total_out) *total_out = flags_total[0];
     return SDBFG_OK;
 }
 
@@ -530,6 +703,8 @@ extern "C" int sdbfg_digest_batch_device(sdbfg_ctx* c, const uint8_t* dev_data, 
         if (need > out_cap) return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)need);
         if (need && !dev_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
     }
+    if (!dd) return digest_stream_pipelined(c, nullptr, dev_data, offsets, lens, n, reinterpret_cast<uint32_t*>(dev_out),
+                                            out_cap, res, nullptr);
     for (const Group& g : make_groups(lens, n, dd)) {
         std::vector<uint64_t> off(offsets + g.first, offsets + g.first + g.count);
         rc = digest_group_device(c, dev_data, off, lens, g, dd, reinterpret_cast<uint32_t*>(dev_out), dev_counts, res,
@@ -553,6 +728,19 @@ extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const 
         if (total_slots > out_cap)
             return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)total_slots);
         if (total_slots && !out_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
+    }
+    if (!dd) {
+        uint64_t cap_needed = 0;
+        for (uint32_t i = 0; i < n; i++)
+            if (lens[i] >= kMinFile) cap_needed += stream_cap(lens[i]);
+        CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, cap_needed) * 256));
+        uint64_t total = 0;
+        rc = digest_stream_pipelined(c, host_data, nullptr, offsets, lens, n, c->d_out_filters.as<uint32_t>(),
+                                     std::min(cap_needed, out_cap), res, &total);
+        if (rc) return rc;
+        if (total) CUDA_TRY(c, cudaMemcpyAsync(out_filters, c->d_out_filters.p, total * 256, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        return SDBFG_OK;
     }
     cudaPointerAttributes attr{};
     const bool pinned = cudaPointerGetAttributes(&attr, host_data) == cudaSuccess &&
@@ -613,23 +801,6 @@ extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const 
                 CUDA_TRY(c, cudaMemcpyAsync(out_counts + group_first_slot, c->d_out_counts.p, group_slots * 2,
                                             cudaMemcpyDeviceToHost, st));
             }
-        } else {
-            const uint64_t before = next;
-            uint64_t cap_needed = 0;
-            for (uint32_t k = 0; k < g.count; k++)
-                if (lens[g.first + k] >= kMinFile) cap_needed += stream_cap(lens[g.first + k]);
-            CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, cap_needed) * 256));
-            uint64_t local = 0;
-            rc = digest_group_device(c, d, off, lens, g, 0, c->d_out_filters.as<uint32_t>(), nullptr, res, &local,
-                                     cap_needed);
-            if (rc) return rc;
-            for (uint32_t k = 0; k < g.count; k++)
-                if (lens[g.first + k] >= kMinFile) res[g.first + k].filter_offset += before;
-            next = before + local;
-            if (next > out_cap) return fail(c, SDBFG_ERR_CAPACITY, "output capacity too small");
-            if (local)
-                CUDA_TRY(c, cudaMemcpyAsync(out_filters + before * 256, c->d_out_filters.p, local * 256,
-                                            cudaMemcpyDeviceToHost, st));
         }
         CUDA_TRY(c, cudaStreamSynchronize(st));
     }
