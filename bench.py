@@ -294,7 +294,7 @@ def main():
                                             "k_scan_offsets")}
     ntile_ph = ctx.kernel_time("k_stream_tiles.count")[0] or 1.0
     phases = {k: ctx.kernel_time("k_stream_tiles." + k)[0] / ntile_ph
-              for k in ("load", "ranks", "fres", "walk", "link", "compact", "sha1")}
+              for k in ("load", "ranks", "fres", "walk", "link", "compact", "sha1", "fixups")}
     commit_ph = {k: ctx.kernel_time("k_stream_commit." + k)[0] for k in ("wait", "busy", "groups", "loops", "max_file")}
     ctx.profile(False)
     ms_per_step = allmax(world, dev_ms / args.steps)

@@ -508,6 +508,7 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
         if (threadIdx.x == 0) {
             for (int k = 0; k < 7; k++) atomicAdd(P.phase + k, (unsigned long long)(tm[k + 1] - tm[k]));
             atomicAdd(P.phase + kPhTiles, 1ull);
+            atomicAdd(P.phase + kPhFixups, (unsigned long long)s.misc[9]);
         }
     }
 }
@@ -554,15 +555,17 @@ struct CommitSmem {
     uint32_t F[64];                  // current 256-byte filter
     uint32_t own[2048];              // lanes of the group holding each filter index
     uint32_t G[kBigBytes / 4];       // current 16 KiB big filter
-    uint32_t dup[192];               // big-filter values set twice within a group
-    uint32_t ndup;
-    uint32_t pad[3];
     uint32_t feat[2][5][kTileCap];   // double-buffered features of a tile
 };
 
 __device__ inline uint32_t lanemask_le() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_le;" : "=r"(m));
+    return m;
+}
+__device__ inline uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
 }
 
@@ -584,54 +587,20 @@ __device__ __forceinline__ void stage_tile(uint32_t (*buf)[kTileCap], const uint
     cp_async_commit();
 }
 
-// Big-filter (G) test for the lanes in `act`, in lane order: returns a mask
-// over the lane's 5 values of "not set before this lane".  Sets the bits
-// (atomicOr); `flipped` records the bits this lane turned on.
-__device__ inline uint32_t big_insert(uint32_t* G, uint32_t* dup, uint32_t* ndup, bool act, const uint32_t (&b)[5],
-                                      uint32_t& flipped) {
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t pre = 0;
-    if (act) {
-#pragma unroll
-        for (int k = 0; k < 5; k++) pre |= ((G[b[k] >> 5] >> (b[k] & 31)) & 1u) << k;
-    }
-    __syncwarp();
-    flipped = 0;
-    if (act) {
-#pragma unroll
-        for (int k = 0; k < 5; k++) {
-            if (!((pre >> k) & 1u)) {
-                const uint32_t bit = 1u << (b[k] & 31);
-                const uint32_t old = atomicOr(&G[b[k] >> 5], bit);
-                if (old & bit) {
-                    const uint32_t slot = atomicAdd(ndup, 1u);
-                    if (slot < 192) dup[slot] = b[k];
-                } else {
-                    flipped |= 1u << k;
-                }
-            }
-        }
-    }
-    __syncwarp();
-    uint32_t fresh = act ? (~pre & 31u) : 0u;
-    const uint32_t nd = min(*ndup, 192u);
-    for (uint32_t e = 0; e < nd; e++) {
-        const uint32_t v = dup[e];
-        uint32_t mine = 0;
-#pragma unroll
-        for (int k = 0; k < 5; k++) mine |= ((fresh >> k) & 1u && b[k] == v) ? (1u << k) : 0u;
-        const uint32_t holders = __ballot_sync(0xffffffffu, mine != 0);
-        if (mine) {
-            if (lane == (uint32_t)(__ffs(holders) - 1)) fresh &= ~(mine & ~(mine & (~mine + 1u)));
-            else fresh &= ~mine;
-        }
-    }
-    __syncwarp();
-    if (lane == 0) *ndup = 0;
-    __syncwarp();
-    return fresh;
-}
-
+// The ordered filter fill for one group of up to 32 features (lane l holds
+// feature l), in feature order, with the semantics of gen_chunk_hash
+// (sdbf_core.cc:103-130): a feature is counted iff it sets a new bit in the
+// 256-byte filter F (bf_sha1_insert) and a new bit in the big filter G
+// (query_and_set); F keeps the bits of features that fail G.
+//
+// "New" means unset before this feature, i.e. unset in the state before the
+// group and not held by an earlier lane of the group.  Earlier holders of a
+// filter index come from an owner mask (bit l set for every lane holding the
+// 11-bit index).  Two big-filter indices can only be equal if their low 11
+// bits -- the filter index -- are, so the same mask names the only lanes
+// whose 17-bit values need an exact comparison (register shuffles).  Bits
+// are written only for lanes up to the first roll-over, which is found
+// before anything is written; later lanes are re-run against the new state.
 __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -644,7 +613,6 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
         uint32_t* out = P.out_filters + (size_t)Fd.filter_base * 64;
         for (uint32_t i = lane; i < 64; i += 32) S.F[i] = 0;
         for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
-        if (lane == 0) S.ndup = 0;
         // the file's tiles are one contiguous range
         const GenChunk c0 = P.chunks[Fd.first_chunk];
         const GenChunk cl = P.chunks[Fd.first_chunk + Fd.nchunks - 1];
@@ -693,30 +661,71 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                     const bool act = have && lane >= start;
                     if (!__any_sync(0xffffffffu, act)) break;
                     n_loops++;
-                    // small filter: new iff some index is unset in F and no
-                    // earlier lane of the group holds it (bf_sha1_insert)
-                    uint32_t fpre = 0;
+                    // round 1: state before the group, publish holders
+                    uint32_t fpre = 0, gpre = 0;
                     if (act) {
 #pragma unroll
                         for (int k = 0; k < 5; k++) {
                             fpre |= ((S.F[a[k] >> 5] >> (a[k] & 31)) & 1u) << k;
+                            gpre |= ((S.G[b[k] >> 5] >> (b[k] & 31)) & 1u) << k;
                             atomicOr(&S.own[a[k]], 1u << lane);
                         }
                     }
                     __syncwarp();
-                    bool fpass = false;
-                    if (act) {
+                    // round 2: holders of each index
+                    uint32_t m[5];
 #pragma unroll
-                        for (int k = 0; k < 5; k++)
-                            if (!((fpre >> k) & 1u) && (uint32_t)(__ffs(S.own[a[k]]) - 1) == lane) fpass = true;
-                    }
+                    for (int k = 0; k < 5; k++) m[k] = act ? S.own[a[k]] : 0u;
                     __syncwarp();
                     if (act) {
 #pragma unroll
                         for (int k = 0; k < 5; k++) S.own[a[k]] = 0;
                     }
-                    uint32_t flG;
-                    const uint32_t gnew = big_insert(S.G, S.dup, &S.ndup, fpass, b, flG);
+                    // 256-byte filter: new iff unset before the group and this
+                    // lane is the first holder
+                    bool fpass = false;
+#pragma unroll
+                    for (int k = 0; k < 5; k++)
+                        if (act && !((fpre >> k) & 1u) && (uint32_t)(__ffs(m[k]) - 1) == lane) fpass = true;
+                    const uint32_t fmask = __ballot_sync(0xffffffffu, fpass);
+                    // big filter: new iff unset before the group and no earlier
+                    // filter-passing lane holds the same 17-bit value
+                    uint32_t gnew = 0, pend = 0;
+                    uint32_t cand[5];
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        cand[k] = m[k] & fmask & lanemask_lt();
+                        if (fpass && !((gpre >> k) & 1u)) {
+                            if (cand[k]) pend |= 1u << k;
+                            else gnew |= 1u << k;
+                        }
+                    }
+                    while (__any_sync(0xffffffffu, pend != 0)) {
+                        // each pending lane checks one candidate lane per pass
+                        int kk = pend ? __ffs(pend) - 1 : 0;
+                        uint32_t ck = 0, vk = 0;
+#pragma unroll
+                        for (int k = 0; k < 5; k++)
+                            if (k == kk) {
+                                ck = cand[k];
+                                vk = b[k];
+                            }
+                        const uint32_t j = pend ? (uint32_t)(__ffs(ck) - 1) : lane;
+                        bool same = false;
+#pragma unroll
+                        for (int q = 0; q < 5; q++) same |= (__shfl_sync(0xffffffffu, b[q], j) == vk);
+                        if (pend) {
+                            ck &= ck - 1u;
+#pragma unroll
+                            for (int k = 0; k < 5; k++)
+                                if (k == kk) cand[k] = ck;
+                            if (same) pend &= ~(1u << kk);
+                            else if (ck == 0) {
+                                pend &= ~(1u << kk);
+                                gnew |= 1u << kk;
+                            }
+                        }
+                    }
                     const bool counted = fpass && gnew != 0;
                     const uint32_t cm = __ballot_sync(0xffffffffu, counted);
                     const uint32_t before = __popc(cm & lanemask_le());
@@ -724,19 +733,12 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                     const bool hit_big = counted && (bigfi + before == (uint32_t)kBigElem);
                     const uint32_t hm = __ballot_sync(0xffffffffu, hit_small || hit_big);
                     const uint32_t r = hm ? (uint32_t)(__ffs(hm) - 1) : 31u;
-                    // lanes after r are re-processed: take back their big-filter
-                    // bits, restore bits of lanes <= r that share them
-                    if (hm && fpass && lane > r) {
-#pragma unroll
-                        for (int k = 0; k < 5; k++)
-                            if ((flG >> k) & 1u) atomicAnd(&S.G[b[k] >> 5], ~(1u << (b[k] & 31)));
-                    }
-                    __syncwarp();
+                    // write the bits of lanes up to r (all of them without a roll-over)
                     if (act && lane <= r) {
 #pragma unroll
                         for (int k = 0; k < 5; k++) {
                             atomicOr(&S.F[a[k] >> 5], 1u << (a[k] & 31));
-                            if (hm && fpass) atomicOr(&S.G[b[k] >> 5], 1u << (b[k] & 31));
+                            if (fpass) atomicOr(&S.G[b[k] >> 5], 1u << (b[k] & 31));
                         }
                     }
                     __syncwarp();

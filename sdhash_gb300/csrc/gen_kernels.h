@@ -82,7 +82,7 @@ struct GenParams {
 // Phase counters (cycles summed over CTAs / warps) when GenParams::phase is set.
 enum : int {
     kPhLoad = 0, kPhRanks, kPhFres, kPhWalk, kPhLink, kPhCompact, kPhSha, kPhTiles,
-    kPhCommitWait, kPhCommitBusy, kPhCommitGroups, kPhCommitLoops, kPhCommitMaxFile, kPhCount
+    kPhCommitWait, kPhCommitBusy, kPhCommitGroups, kPhCommitLoops, kPhCommitMaxFile, kPhFixups, kPhCount
 };
 
 size_t stream_tile_smem();
