@@ -134,8 +134,11 @@ __device__ inline void load_bytes(const uint8_t* __restrict__ chunk, const TileG
 }
 
 // ------------------------------------------------------- phase 2: ranks
+// dtab[c] = T[c+1] - T[c] (c = 0..63): entropy change when a byte value's
+// count in the window goes from c to c+1 (entr64_inc_int, entr64.cc:47-71,
+// written as differences of the table of entr64_table_init_int).
 __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const uint16_t* rank_tab,
-                                     const uint32_t* ent_tab) {
+                                     const int32_t* dtab) {
     const uint8_t* b8 = reinterpret_cast<const uint8_t*>(s.bytes32);
     const uint32_t np = g.RE - g.Q0;
     const uint32_t per = (np + kGenThreads - 1) / kGenThreads;
@@ -143,31 +146,35 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
     uint8_t* h = s.hist;  // counts at hist_off(tid, v) (cleared by the caller)
     const uint32_t lo = tid * per, hi = min(np, lo + per);
     const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
-    uint32_t e = 0;
-    for (uint32_t r = lo; r < hi; r++) {
-        const uint32_t o = g.Q0 + r;
-        if (o >= last) {
+    const uint32_t hbase = hist_off(tid, 0);
+    int32_t e = 0;
+    uint32_t r = lo;
+    if (r < hi && g.Q0 + r < last) {
+        // entr64_init_int (entr64.cc:27-41) built incrementally
+        for (int k = 0; k < kWin; k++) {
+            const uint32_t v = b8[r + k];
+            const uint32_t off = hbase + ((v >> 2) << 7) + (v & 3);
+            const uint32_t c = h[off];
+            e += dtab[c];
+            h[off] = (uint8_t)(c + 1);
+        }
+        s.ranks[pidx(r)] = rank_tab[e >> 10];
+        r++;
+    }
+    for (; r < hi; r++) {
+        if (g.Q0 + r >= last) {
             s.ranks[pidx(r)] = 0;
             continue;
         }
-        if (r == lo) {
-            // entr64_init_int (entr64.cc:27-41) built incrementally
-            for (int k = 0; k < kWin; k++) {
-                const uint32_t v = b8[r + k];
-                const uint32_t c = h[hist_off(tid, v)];
-                e += ent_tab[c + 1] - ent_tab[c];
-                h[hist_off(tid, v)] = (uint8_t)(c + 1);
-            }
-        } else {
-            // entr64_inc_int (entr64.cc:47-71): byte r-1 leaves, r+63 enters
-            const uint32_t a = b8[r - 1], b = b8[r + 63];
-            if (a != b) {
-                const uint32_t ha = hist_off(tid, a), hb = hist_off(tid, b);
-                const uint32_t ca = h[ha], cb = h[hb];
-                h[ha] = (uint8_t)(ca - 1);
-                h[hb] = (uint8_t)(cb + 1);
-                e = e - (ent_tab[ca] - ent_tab[ca - 1]) + (ent_tab[cb + 1] - ent_tab[cb]);
-            }
+        // byte r-1 leaves, byte r+63 enters
+        const uint32_t a = b8[r - 1], b = b8[r + 63];
+        if (a != b) {
+            const uint32_t ha = hbase + ((a >> 2) << 7) + (a & 3);
+            const uint32_t hb = hbase + ((b >> 2) << 7) + (b & 3);
+            const uint32_t ca = h[ha], cb = h[hb];
+            h[ha] = (uint8_t)(ca - 1);
+            h[hb] = (uint8_t)(cb + 1);
+            e += dtab[cb] - dtab[ca - 1];
         }
         s.ranks[pidx(r)] = rank_tab[e >> 10];
     }
@@ -207,6 +214,7 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
             pre[u] = (uint16_t)run;
         }
         uint32_t suf = 0xFFFFu;
+        uint32_t last_f = 0xFFFFFFFFu, last_end = 0;
 #pragma unroll
         for (int u = 63; u >= 0; u--) {
             const uint32_t k = base + u;
@@ -229,14 +237,18 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
                             m = pk >> 6;
                         }
                     }
-                    // count trailing ones of the run bits starting at f
-                    const uint32_t w = f >> 5, sh = f & 31;
-                    const uint32_t b0 = s.eqw[w], b1 = s.eqw[w + 1], b2 = s.eqw[w + 2];
-                    const uint32_t lo32 = __funnelshift_r(b0, b1, sh);
-                    const uint32_t hi32 = __funnelshift_r(b1, b2, sh);
-                    const uint64_t bits = ((uint64_t)hi32 << 32) | lo32;
-                    const uint32_t runlen = (~bits == 0ull) ? 64u : (uint32_t)__ffsll((long long)~bits) - 1;
-                    uint32_t p = f + runlen;
+                    // end of the run of equal ranks starting at f (the run bits
+                    // are only re-read when f changes)
+                    if (f != last_f) {
+                        const uint32_t w = f >> 5, sh = f & 31;
+                        const uint32_t b0 = s.eqw[w], b1 = s.eqw[w + 1], b2 = s.eqw[w + 2];
+                        const uint32_t lo32 = __funnelshift_r(b0, b1, sh);
+                        const uint32_t hi32 = __funnelshift_r(b1, b2, sh);
+                        const uint64_t bits = ((uint64_t)hi32 << 32) | lo32;
+                        last_end = f + ((~bits == 0ull) ? 64u : (uint32_t)__ffsll((long long)~bits) - 1);
+                        last_f = f;
+                    }
+                    uint32_t p = last_end;
                     if (p > k + 63) p = k + 63;
                     out = (uint16_t)((m << 6) | (p - k));
                 }
@@ -247,21 +259,24 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 }
 
 // ------------------------------------------------------ phase 4: chains
+// Run-length credit accumulator: a cheap slide credits the same position
+// many times in a row, so credits are added to the shared score array only
+// when the credited position changes.
+template <int kSign>
 struct Credit {
     uint32_t* score32;
     uint32_t lo, hi;  // credited positions [lo, hi) (chunk-relative)
     uint32_t cur, cnt;
-    int sign;
-    __device__ void flush() {
-        if (cnt && cur >= lo && cur < hi) {
+    __device__ __forceinline__ void flush() {
+        if (cnt && cur - lo < hi - lo) {
             const uint32_t o = cur - lo;
             const uint32_t inc = cnt << (8 * (o & 3));
-            if (sign > 0) atomicAdd(&score32[o >> 2], inc);
+            if (kSign > 0) atomicAdd(&score32[o >> 2], inc);
             else atomicSub(&score32[o >> 2], inc);
         }
         cnt = 0;
     }
-    __device__ void add(uint32_t p) {
+    __device__ __forceinline__ void add(uint32_t p) {
         if (p != cur) {
             flush();
             cur = p;
@@ -270,38 +285,57 @@ struct Credit {
     }
 };
 
-// Walk steps [a, b).  If force_full, step a is a full rescan (speculative
-// start, or exact when a == 0).  Credits go to `cr` when non-null.
-__device__ inline ChainState walk(const TileGeom& g, const TileSmem& s, uint32_t a, uint32_t b, ChainState st,
-                                  bool force_full, Credit* cr) {
+// Walk steps [a, b) of gen_chunk_scores from state `st` (st.M == 0 makes step
+// a a full rescan: the speculative start, or step 0).  The operands of step
+// i+1 are loaded while step i is processed; both arrays extend past the last
+// step, so those loads stay in bounds.
+template <typename CR>
+__device__ __forceinline__ ChainState walk(const TileGeom& g, const TileSmem& s, uint32_t a, uint32_t b,
+                                           ChainState st, CR* cr) {
+    if (a >= b) return st;
+    const uint16_t* __restrict__ R = s.ranks;
+    const uint16_t* __restrict__ Fr = s.fres;
+    uint32_t r64 = R[pidx(a + 64 - g.Q0)], f = Fr[pidx(a - g.Q0)];
     for (uint32_t i = a; i < b; i++) {
-        const uint32_t r64 = s.ranks[pidx(i + 64 - g.Q0)];
-        const bool cheap = !(force_full && i == a) && i > 0 && st.M > 0 && r64 >= st.M && i < st.P;
-        if (cheap) {
-            if (r64 == st.M) st.P = i + 64;
-            if (cr) cr->add(st.P);
-        } else {
-            const uint32_t f = s.fres[pidx(i - g.Q0)];
-            st.M = f >> 6;
-            st.P = i + (f & 63);
-            if (st.M && cr) cr->add(st.P);
-        }
+        const uint32_t r64n = R[pidx(i + 65 - g.Q0)], fn = Fr[pidx(i + 1 - g.Q0)];
+        const bool cheap = (st.M != 0) & (r64 >= st.M) & (i < st.P);
+        const uint32_t cheapP = (r64 == st.M) ? i + 64 : st.P;
+        st.P = cheap ? cheapP : i + (f & 63);
+        st.M = cheap ? st.M : (f >> 6);
+        if (cr && st.M != 0) cr->add(st.P);
+        r64 = r64n;
+        f = fn;
     }
     return st;
 }
 
-__device__ inline bool same_state(uint64_t a, uint64_t b) { return a == b; }
-
-// Runs all phases for one tile.  entry != nullptr: the state entering step
-// S0 is known (re-computation after a failed link check); otherwise thread 0
-// starts speculatively kLead steps early.  Returns (in misc[0]) the number
-// of features, and writes sig_in / tau_out for the tile.
 __device__ __forceinline__ void stamp(long long* tm, int k) {
     if (tm && threadIdx.x == 0) tm[k] = clock64();
 }
 
+// Walk segment [St, Et) from `st` with credits of sign kSign; records the
+// state entering step chk (the next tile's first credited step) when the
+// segment contains it.
+template <int kSign>
+__device__ __forceinline__ ChainState walk_segment(const TileGeom& g, const TileSmem& s, uint32_t St, uint32_t Et,
+                                                   ChainState st, uint32_t chk) {
+    Credit<kSign> cr{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0};
+    if (chk >= St && chk < Et) {
+        st = walk(g, s, St, chk, st, &cr);
+        if (kSign > 0) *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(st);
+        st = walk(g, s, chk, Et, st, &cr);
+    } else {
+        st = walk(g, s, St, Et, st, &cr);
+    }
+    cr.flush();
+    return st;
+}
+
+// Runs all phases for one tile.  entry != nullptr: the state entering step
+// S0 is known (re-computation after a failed link check); otherwise thread 0
+// starts speculatively `lead` steps early.  Writes sig_in / tau_out.
 __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom& g, const TileSmem& s,
-                              const uint16_t* rank_tab, const uint32_t* ent_tab, const uint64_t* entry,
+                              const uint16_t* rank_tab, const int32_t* dtab, const uint64_t* entry,
                               uint64_t* sig_in, uint64_t* tau_out, uint32_t lead, long long* tm) {
     stamp(tm, 0);
     load_bytes(chunk, g, s.bytes32);
@@ -311,14 +345,12 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
     }
     __syncthreads();
     stamp(tm, 1);
-    compute_ranks(g, s, rank_tab, ent_tab);
+    compute_ranks(g, s, rank_tab, dtab);
     __syncthreads();
     stamp(tm, 2);
     compute_fres(g, s);
     // clear scores (aliases the histogram area, free after phase 2)
     for (uint32_t i = threadIdx.x; i < (g.L + 3) / 4 + 1; i += blockDim.x) s.score32[i] = 0;
-    __syncthreads();
-
     if (threadIdx.x == 0) {
         s.misc[9] = 0;
         s.misc[10] = 0;
@@ -331,36 +363,22 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
     const uint32_t SL = (total + kSegs - 1) / kSegs;
     const uint32_t chk = g.t0 + g.L - 64;  // next tile's S0
     const uint32_t t = threadIdx.x;
+    const uint32_t St = g.S0 + t * SL;
+    const uint32_t Et = min(St + SL, g.SE);
+    const bool has_seg = t < kSegs && SL > 0 && St < g.SE;
     if (t < kSegs) {
-        const uint32_t St = g.S0 + t * SL;
-        const uint32_t Et = min(St + SL, g.SE);
-        if (SL > 0 && St < g.SE) {
+        if (has_seg) {
             ChainState st{0, 0};
-            bool force = true;
-            uint32_t start = St;
             if (t == 0 && entry) {
                 st = unpack_state(*entry);
-                force = false;
             } else {
                 // lead-in of `lead` steps (never below Q0, since lead <= kLead);
-                // starting at step 0 makes the walk exact
+                // a lead-in from step 0 makes the walk exact
                 const uint32_t Ls = St > lead ? St - lead : 0;
-                st = walk(g, s, Ls, St, st, true, nullptr);
-                force = (Ls == St);
-                start = St;
+                st = walk(g, s, Ls, St, st, (Credit<1>*)nullptr);
             }
             s.sig[t] = pack_state(st);
-            Credit cr{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0, 1};
-            if (chk >= St && chk < Et) {
-                st = walk(g, s, start, chk, st, force, &cr);
-                s.misc[8] = (uint32_t)t;
-                *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(st);
-                st = walk(g, s, chk, Et, st, force && chk == start, &cr);
-            } else {
-                st = walk(g, s, start, Et, st, force, &cr);
-            }
-            cr.flush();
-            s.tau[t] = pack_state(st);
+            s.tau[t] = pack_state(walk_segment<1>(g, s, St, Et, st, chk));
         } else {
             s.sig[t] = ~0ull;
             s.tau[t] = ~0ull;
@@ -368,31 +386,27 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
     }
     __syncthreads();
     stamp(tm, 4);
-    // phase 5: link segments inside the tile (serial, normally no work)
-    if (t == 0 && SL > 0) {
-        for (uint32_t q = 1; q < kSegs; q++) {
-            const uint32_t St = g.S0 + q * SL;
-            if (St >= g.SE) break;
-            const uint32_t Et = min(St + SL, g.SE);
-            if (same_state(s.sig[q], s.tau[q - 1])) continue;
-            // undo the speculative credits, redo from the true state
-            Credit un{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0, -1};
-            walk(g, s, St, Et, unpack_state(s.sig[q]), false, &un);
-            un.flush();
-            Credit re{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0, 1};
-            ChainState st = unpack_state(s.tau[q - 1]);
-            if (chk >= St && chk < Et) {
-                st = walk(g, s, St, chk, st, false, &re);
-                *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(st);
-                st = walk(g, s, chk, Et, st, false, &re);
-            } else {
-                st = walk(g, s, St, Et, st, false, &re);
-            }
-            re.flush();
-            s.sig[q] = s.tau[q - 1];
-            s.tau[q] = pack_state(st);
-            s.misc[9]++;
+    // phase 5: link segments.  A segment is exact iff its entry state equals
+    // its left neighbour's exit state; mismatched segments are re-walked in
+    // parallel rounds until every link holds (normally zero rounds).
+    while (true) {
+        bool need = false;
+        uint64_t from = 0;
+        if (has_seg && t >= 1) {
+            from = s.tau[t - 1];
+            need = s.sig[t] != from;
         }
+        if (!__syncthreads_or(need)) break;
+        if (need) {
+            walk_segment<-1>(g, s, St, Et, unpack_state(s.sig[t]), chk);
+            const ChainState st = walk_segment<1>(g, s, St, Et, unpack_state(from), chk);
+            s.sig[t] = from;
+            s.tau[t] = pack_state(st);
+            atomicAdd(&s.misc[9], 1u);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
         if (sig_in) *sig_in = s.sig[0];
         if (tau_out) *tau_out = *reinterpret_cast<uint64_t*>(&s.misc[10]);
     }
@@ -475,13 +489,13 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
     const TileGeom g = stream_geom(C.n, T.t0);
     TileSmem s = carve(smem, kTileL);
     __shared__ uint16_t rank_tab[SDBF_RANK_BINS];
-    __shared__ uint32_t ent_tab[66];
+    __shared__ int32_t dtab[64];
     for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) rank_tab[i] = P.rank_tab[i];
-    for (uint32_t i = threadIdx.x; i < 66; i += blockDim.x) ent_tab[i] = i < 65 ? P.ent_tab[i] : 0;
+    for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
     __syncthreads();
     TileOut* out = P.tile_out + tile;
     long long tm[9];
-    tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, entry, &out->sig_in, &out->tau_out, P.lead,
+    tile_pipeline(P.data + C.data_off, g, s, rank_tab, dtab, entry, &out->sig_in, &out->tau_out, P.lead,
                   P.phase ? tm : nullptr);
     const uint32_t nown = g.SE > g.t0 ? g.SE - g.t0 : 0;
     __shared__ uint32_t counts[kGenThreads / 32];
@@ -513,7 +527,7 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
     }
 }
 
-__global__ void __launch_bounds__(kGenThreads) k_stream_tiles(GenParams P) {
+__global__ void __launch_bounds__(kGenThreads, 4) k_stream_tiles(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     for (uint32_t tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
         stream_tile_body(P, tile, nullptr, smem);
@@ -816,20 +830,20 @@ __device__ inline TileGeom block_geom(uint32_t n) {
 __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint16_t rank_tab[SDBF_RANK_BINS];
-    __shared__ uint32_t ent_tab[66];
+    __shared__ int32_t dtab[64];
     __shared__ uint32_t histo[66];
     __shared__ uint32_t counts[kGenThreads / 32];
     __shared__ uint32_t filt[64];
     __shared__ uint32_t hsh[kGenThreads][5];
     __shared__ int state[4];  // k, allowed, hashed, done
     for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) rank_tab[i] = P.rank_tab[i];
-    for (uint32_t i = threadIdx.x; i < 66; i += blockDim.x) ent_tab[i] = i < 65 ? P.ent_tab[i] : 0;
+    for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
     __syncthreads();
     TileSmem s = carve(smem, P.block_lmax);
     for (uint32_t b = blockIdx.x; b < P.nchunks; b += gridDim.x) {
         const GenChunk C = P.chunks[b];
         const TileGeom g = block_geom(C.n);
-        tile_pipeline(P.data + C.data_off, g, s, rank_tab, ent_tab, nullptr, nullptr, nullptr, P.lead, nullptr);
+        tile_pipeline(P.data + C.data_off, g, s, rank_tab, dtab, nullptr, nullptr, nullptr, P.lead, nullptr);
         const uint8_t* sc = reinterpret_cast<const uint8_t*>(s.score32);
         const uint32_t nown = g.SE;
         if (threadIdx.x < 66) histo[threadIdx.x] = 0;
