@@ -161,6 +161,35 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
         s.ranks[pidx(r)] = rank_tab[e >> 10];
         r++;
     }
+    // two steps per iteration: the second step's counts are loaded together
+    // with the first's and corrected for the first step's update in registers
+    // (later stores win where both steps touch the same byte value)
+    for (; r + 1 < hi && g.Q0 + r + 1 < last; r += 2) {
+        const uint32_t a0 = b8[r - 1], b0 = b8[r + 63], a1 = b8[r], b1 = b8[r + 64];
+        const uint32_t ha0 = hbase + ((a0 >> 2) << 7) + (a0 & 3), hb0 = hbase + ((b0 >> 2) << 7) + (b0 & 3);
+        const uint32_t ha1 = hbase + ((a1 >> 2) << 7) + (a1 & 3), hb1 = hbase + ((b1 >> 2) << 7) + (b1 & 3);
+        const int32_t ca0 = h[ha0], cb0 = h[hb0];
+        int32_t ca1 = h[ha1], cb1 = h[hb1];
+        const bool d0 = a0 != b0, d1 = a1 != b1;
+        if (d0) {
+            e += dtab[cb0] - dtab[ca0 - 1];
+            ca1 += (int32_t)(a1 == b0) - (int32_t)(a1 == a0);
+            cb1 += (int32_t)(b1 == b0) - (int32_t)(b1 == a0);
+        }
+        const uint16_t rk0 = rank_tab[e >> 10];
+        if (d1) e += dtab[cb1] - dtab[ca1 - 1];
+        const uint16_t rk1 = rank_tab[e >> 10];
+        if (d0) {
+            h[ha0] = (uint8_t)(ca0 - 1);
+            h[hb0] = (uint8_t)(cb0 + 1);
+        }
+        if (d1) {
+            h[ha1] = (uint8_t)(ca1 - 1);
+            h[hb1] = (uint8_t)(cb1 + 1);
+        }
+        s.ranks[pidx(r)] = rk0;
+        s.ranks[pidx(r + 1)] = rk1;
+    }
     for (; r < hi; r++) {
         if (g.Q0 + r >= last) {
             s.ranks[pidx(r)] = 0;
@@ -309,6 +338,32 @@ __device__ __forceinline__ ChainState walk(const TileGeom& g, const TileSmem& s,
     return st;
 }
 
+// Lead-in of a tile's first segment: the maximum under the default lead (a
+// failed link between tiles recomputes a whole tile), the configured lead
+// otherwise (so tests can drive the cross-tile path).
+__host__ __device__ inline uint32_t tile_lead(uint32_t lead) { return lead >= kDefaultLead ? kLead : lead; }
+
+// Re-walk segment [St, Et) from its true entry state `nw` next to the chain
+// it was credited with (`old`, from its speculative entry).  Both walks run
+// in lockstep; credits differ only until the two states coincide, after
+// which the rest of the old walk (and its exit state) stands.  Returns the
+// segment's exit state.
+__device__ uint64_t relink_segment(const TileGeom& g, const TileSmem& s, uint32_t St, uint32_t Et, ChainState old,
+                                   ChainState nw, uint32_t chk, uint64_t old_exit) {
+    Credit<-1> un{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0};
+    Credit<1> re{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0};
+    uint32_t i = St;
+    for (; i < Et; i++) {
+        if (pack_state(old) == pack_state(nw)) break;
+        if (i == chk) *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(nw);
+        old = walk(g, s, i, i + 1, old, &un);
+        nw = walk(g, s, i, i + 1, nw, &re);
+    }
+    un.flush();
+    re.flush();
+    return i < Et ? old_exit : pack_state(nw);
+}
+
 __device__ __forceinline__ void stamp(long long* tm, int k) {
     if (tm && threadIdx.x == 0) tm[k] = clock64();
 }
@@ -372,9 +427,11 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
             if (t == 0 && entry) {
                 st = unpack_state(*entry);
             } else {
-                // lead-in of `lead` steps (never below Q0, since lead <= kLead);
-                // a lead-in from step 0 makes the walk exact
-                const uint32_t Ls = St > lead ? St - lead : 0;
+                // lead-in (never below Q0, since every lead <= kLead); a lead-in
+                // from step 0 makes the walk exact.  The tile's first segment
+                // uses tile_lead: its mis-speculation costs a tile recompute.
+                const uint32_t ld = t == 0 ? tile_lead(lead) : lead;
+                const uint32_t Ls = St > ld ? St - ld : 0;
                 st = walk(g, s, Ls, St, st, (Credit<1>*)nullptr);
             }
             s.sig[t] = pack_state(st);
@@ -398,10 +455,10 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
         }
         if (!__syncthreads_or(need)) break;
         if (need) {
-            walk_segment<-1>(g, s, St, Et, unpack_state(s.sig[t]), chk);
-            const ChainState st = walk_segment<1>(g, s, St, Et, unpack_state(from), chk);
+            const uint64_t out = relink_segment(g, s, St, Et, unpack_state(s.sig[t]), unpack_state(from), chk,
+                                                s.tau[t]);
             s.sig[t] = from;
-            s.tau[t] = pack_state(st);
+            s.tau[t] = out;
             atomicAdd(&s.misc[9], 1u);
         }
         __syncthreads();
@@ -550,7 +607,7 @@ __global__ void __launch_bounds__(kGenThreads) k_stream_verify(GenParams P) {
                 const uint64_t mine = P.tile_out[tile].sig_in;
                 // a tile whose lead-in reaches step 0 is exact by construction
                 const TileGeom g = stream_geom(C.n, P.tiles[tile].t0);
-                redo = (g.S0 > P.lead) && (prev != mine);
+                redo = (g.S0 > tile_lead(P.lead)) && (prev != mine);
                 entry = prev;
             }
             __syncthreads();

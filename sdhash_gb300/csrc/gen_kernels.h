@@ -8,9 +8,10 @@
 namespace sdbfg {
 
 constexpr int kGenThreads = 128;     // CTA size of the tile / block kernels
-constexpr int kSegs = 64;            // popularity-chain segments per tile
+constexpr int kSegs = 128;           // popularity-chain segments per tile (one per thread)
 constexpr uint32_t kLead = 128;      // maximum speculative lead-in steps per segment
-constexpr uint32_t kDefaultLead = 96; // default lead-in (mis-speculation ~1e-4 per segment)
+constexpr uint32_t kDefaultLead = 48; // default lead-in; mis-speculated segments are re-walked only
+                                     // until their chain meets the speculative one
 // window steps owned by a stream tile: with the 64-step credit halo and the
 // 128-step maximum lead-in a tile simulates 8192 steps = 128 aligned
 // 64-step blocks, one per thread of the full-rescan table

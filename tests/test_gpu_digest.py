@@ -51,7 +51,7 @@ def test_short_lead_in_exercises_relink(ctx, golden, lead):
     try:
         out = ctx.digest_buffers([d.tobytes() for d in datas], [r["name"] for r in recs + big], 0)
     finally:
-        ctx.set_lead(96)
+        ctx.set_lead(48)
     bad = [r["name"] for r, d in zip(recs + big, out) if sha(d.to_string()) != r["sha256"]]
     assert not bad, bad
     if lead <= 17:
@@ -142,6 +142,6 @@ def test_short_lead_in_block_mode(ctx, golden, lead):
     try:
         out = ctx.digest_buffers([d.tobytes() for d in datas], [r["name"] for r in recs], 16384)
     finally:
-        ctx.set_lead(96)
+        ctx.set_lead(48)
     bad = [r["name"] for r, d in zip(recs, out) if sha(d.to_string()) != r["sha256"]]
     assert not bad, bad
