@@ -77,8 +77,17 @@ __host__ __device__ constexpr uint32_t padded_len(uint32_t n) { return pidx(n) +
 
 // Byte address of thread t's counter for byte value v in the histogram area:
 // each lane's 256 counters occupy 64 words of its own bank.
+static_assert(kRankThreads % 32 == 0, "histogram layout assumes full warps");
 __device__ __forceinline__ uint32_t hist_off(uint32_t t, uint32_t v) {
     return ((((t >> 5) * 64 + (v >> 2)) * 32 + (t & 31)) << 2) | (v & 3);
+}
+
+// Layout: bytes | ranks | union { histograms (ranks phase) ;
+//                                 fres | run bits | scores | list | sig | tau } | misc
+__host__ __device__ inline uint32_t phase3_bytes(uint32_t Lmax) {
+    const uint32_t span = Lmax + 64 + kLead + 64;
+    return align_up(padded_len(Lmax + 64 + kLead) * 2, 16) + align_up((span / 32 + 4) * 4, 16) +
+           align_up(Lmax + 16, 16) + align_up(((Lmax + 64) / 15 + 8) * 4, 16) + 2 * kSegs * 8;
 }
 
 __host__ __device__ inline uint32_t tile_smem_bytes(uint32_t Lmax) {
@@ -86,12 +95,8 @@ __host__ __device__ inline uint32_t tile_smem_bytes(uint32_t Lmax) {
     uint32_t b = 0;
     b += align_up(span + 64 + 16, 16);                       // bytes
     b += align_up(padded_len(span) * 2, 16);                 // ranks
-    const uint32_t hist = 256 * kGenThreads;
-    const uint32_t phase3 = align_up(padded_len(Lmax + 64 + kLead) * 2, 16) + align_up((span / 32 + 4) * 4, 16) +
-                            align_up(Lmax + 16, 16);
-    b += hist > phase3 ? hist : phase3;                      // union
-    b += align_up(((Lmax + 64) / 15 + 8) * 4, 16);           // selected / candidate positions
-    b += 2 * kSegs * 8;                                      // sig, tau
+    const uint32_t hist = 256 * kRankThreads, p3 = phase3_bytes(Lmax);
+    b += hist > p3 ? hist : p3;                              // union
     b += 64 * 4;                                             // misc
     return b;
 }
@@ -107,12 +112,11 @@ __device__ inline TileSmem carve(uint8_t* base, uint32_t Lmax) {
     s.fres = reinterpret_cast<uint16_t*>(u); u += align_up(padded_len(Lmax + 64 + kLead) * 2, 16);
     s.eqw = reinterpret_cast<uint32_t*>(u); u += align_up((span / 32 + 4) * 4, 16);
     s.score32 = reinterpret_cast<uint32_t*>(u); u += align_up(Lmax + 16, 16);
-    const uint32_t hist = 256 * kGenThreads;
-    const uint32_t phase3 = (uint32_t)(u - p);
-    p += hist > phase3 ? hist : phase3;
-    s.list = reinterpret_cast<uint32_t*>(p); p += align_up(((Lmax + 64) / 15 + 8) * 4, 16);
-    s.sig = reinterpret_cast<uint64_t*>(p); p += kSegs * 8;
-    s.tau = reinterpret_cast<uint64_t*>(p); p += kSegs * 8;
+    s.list = reinterpret_cast<uint32_t*>(u); u += align_up(((Lmax + 64) / 15 + 8) * 4, 16);
+    s.sig = reinterpret_cast<uint64_t*>(u); u += kSegs * 8;
+    s.tau = reinterpret_cast<uint64_t*>(u); u += kSegs * 8;
+    const uint32_t hist = 256 * kRankThreads, p3 = phase3_bytes(Lmax);
+    p += hist > p3 ? hist : p3;
     s.misc = reinterpret_cast<uint32_t*>(p);
     return s;
 }
@@ -141,8 +145,9 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
                                      const int32_t* dtab) {
     const uint8_t* b8 = reinterpret_cast<const uint8_t*>(s.bytes32);
     const uint32_t np = g.RE - g.Q0;
-    const uint32_t per = (np + kGenThreads - 1) / kGenThreads;
+    const uint32_t per = (np + kRankThreads - 1) / kRankThreads;
     const uint32_t tid = threadIdx.x;
+    if (tid >= (uint32_t)kRankThreads) return;
     uint8_t* h = s.hist;  // counts at hist_off(tid, v) (cleared by the caller)
     const uint32_t lo = tid * per, hi = min(np, lo + per);
     const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
@@ -158,7 +163,7 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
             e += dtab[c];
             h[off] = (uint8_t)(c + 1);
         }
-        s.ranks[pidx(r)] = rank_tab[e >> 10];
+        s.ranks[pidx(r)] = __ldg(rank_tab + (e >> 10));
         r++;
     }
     // two steps per iteration: the second step's counts are loaded together
@@ -176,9 +181,9 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
             ca1 += (int32_t)(a1 == b0) - (int32_t)(a1 == a0);
             cb1 += (int32_t)(b1 == b0) - (int32_t)(b1 == a0);
         }
-        const uint16_t rk0 = rank_tab[e >> 10];
+        const uint16_t rk0 = __ldg(rank_tab + (e >> 10));
         if (d1) e += dtab[cb1] - dtab[ca1 - 1];
-        const uint16_t rk1 = rank_tab[e >> 10];
+        const uint16_t rk1 = __ldg(rank_tab + (e >> 10));
         if (d0) {
             h[ha0] = (uint8_t)(ca0 - 1);
             h[hb0] = (uint8_t)(cb0 + 1);
@@ -205,7 +210,7 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
             h[hb] = (uint8_t)(cb + 1);
             e += dtab[cb] - dtab[ca - 1];
         }
-        s.ranks[pidx(r)] = rank_tab[e >> 10];
+        s.ranks[pidx(r)] = __ldg(rank_tab + (e >> 10));
     }
 }
 
@@ -396,7 +401,7 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
     load_bytes(chunk, g, s.bytes32);
     {
         uint4* h4 = reinterpret_cast<uint4*>(s.hist);
-        for (uint32_t i = threadIdx.x; i < 256 * kGenThreads / 16; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
+        for (uint32_t i = threadIdx.x; i < 256 * kRankThreads / 16; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
     }
     __syncthreads();
     stamp(tm, 1);
@@ -545,11 +550,10 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
     const GenChunk C = P.chunks[T.chunk];
     const TileGeom g = stream_geom(C.n, T.t0);
     TileSmem s = carve(smem, kTileL);
-    __shared__ uint16_t rank_tab[SDBF_RANK_BINS];
     __shared__ int32_t dtab[64];
-    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) rank_tab[i] = P.rank_tab[i];
     for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
     __syncthreads();
+    const uint16_t* rank_tab = P.rank_tab;  // 2 KB, read through the read-only cache
     TileOut* out = P.tile_out + tile;
     long long tm[9];
     tile_pipeline(P.data + C.data_off, g, s, rank_tab, dtab, entry, &out->sig_in, &out->tau_out, P.lead,
@@ -886,16 +890,15 @@ __device__ inline TileGeom block_geom(uint32_t n) {
 
 __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ uint16_t rank_tab[SDBF_RANK_BINS];
     __shared__ int32_t dtab[64];
     __shared__ uint32_t histo[66];
     __shared__ uint32_t counts[kGenThreads / 32];
     __shared__ uint32_t filt[64];
     __shared__ uint32_t hsh[kGenThreads][5];
     __shared__ int state[4];  // k, allowed, hashed, done
-    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) rank_tab[i] = P.rank_tab[i];
     for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
     __syncthreads();
+    const uint16_t* rank_tab = P.rank_tab;  // read through the read-only cache
     TileSmem s = carve(smem, P.block_lmax);
     for (uint32_t b = blockIdx.x; b < P.nchunks; b += gridDim.x) {
         const GenChunk C = P.chunks[b];

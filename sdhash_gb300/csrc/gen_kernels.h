@@ -8,14 +8,16 @@
 namespace sdbfg {
 
 constexpr int kGenThreads = 128;     // CTA size of the tile / block kernels
+constexpr int kRankThreads = 96;     // threads computing ranks: 3 full warps, each lane owning
+                                     // a 256-byte histogram in its own bank
 constexpr int kSegs = 128;           // popularity-chain segments per tile (one per thread)
 constexpr uint32_t kLead = 128;      // maximum speculative lead-in steps per segment
 constexpr uint32_t kDefaultLead = 48; // default lead-in; mis-speculated segments are re-walked only
                                      // until their chain meets the speculative one
 // window steps owned by a stream tile: with the 64-step credit halo and the
-// 128-step maximum lead-in a tile simulates 8192 steps = 128 aligned
-// 64-step blocks, one per thread of the full-rescan table
-constexpr uint32_t kTileL = 8000;
+// 128-step maximum lead-in a tile simulates 8128 steps (127 aligned 64-step
+// blocks, one per thread of the full-rescan table)
+constexpr uint32_t kTileL = 7936;
 // at most one selected feature per 17 credited steps (score > 16), and a
 // tile's positions are credited by kTileL + 64 steps
 constexpr uint32_t kTileCap = ((kTileL + 64) / 17 + 2 + 3) / 4 * 4;  // rows 16-byte aligned

@@ -109,9 +109,9 @@ struct sdbfg_ctx {
         bool used = false;
         DevBuf data, chunks, tiles, files, order, tile_out, features, work;
         HostBuf h_tables;
-    } slot[2];
+    } slot[3];
     DevBuf d_binfo, d_boff, d_total, d_phase;
-    cudaEvent_t ev_scan[2] = {nullptr, nullptr};
+    cudaEvent_t ev_scan[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev_start = nullptr;
 };
 
@@ -475,8 +475,10 @@ __global__ void k_pack_group(const uint32_t* __restrict__ work, const GenFile* _
     }
 }
 
+constexpr int kSlots = 3;  // launch groups in flight (one tiles kernel + up to two commits)
+
 static int ensure_pipeline(sdbfg_ctx* c) {
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < kSlots; k++) {
         if (!c->slot[k].stream) {
             CUDA_TRY(c, cudaStreamCreateWithFlags(&c->slot[k].stream, cudaStreamNonBlocking));
             CUDA_TRY(c, cudaEventCreateWithFlags(&c->slot[k].done, cudaEventDisableTiming));
@@ -495,10 +497,24 @@ static int ensure_pipeline(sdbfg_ctx* c) {
 // commit of one group overlaps the tiles (and the input copy) of the next;
 // the host synchronises once, at the end.
 static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const uint8_t* dev_data,
-                                   const uint64_t* offsets, const uint64_t* lens, uint32_t n, uint32_t* dev_out,
+                                   const uint64_t* offsets_in, const uint64_t* lens_in, uint32_t n, uint32_t* dev_out,
                                    uint64_t out_cap, sdbfg_digest_result* res, uint64_t* total_out) {
     int rc = ensure_pipeline(c);
     if (rc) return rc;
+    // Launch groups are formed over the inputs sorted by size (largest first),
+    // so the long ordered commits of the largest inputs start early and
+    // overlap the rest of the batch; the packed output follows this order and
+    // results[] records where each input's filters are.
+    std::vector<uint32_t> perm(n);
+    std::iota(perm.begin(), perm.end(), 0u);
+    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) { return lens_in[a] > lens_in[b]; });
+    std::vector<uint64_t> lens_v(n), offs_v(n);
+    for (uint32_t i = 0; i < n; i++) {
+        lens_v[i] = lens_in[perm[i]];
+        offs_v[i] = offsets_in[perm[i]];
+    }
+    const uint64_t* lens = lens_v.data();
+    const uint64_t* offsets = offs_v.data();
     CUDA_TRY(c, c->d_binfo.ensure(std::max<size_t>(1, n) * sizeof(FileInfoDev)));
     CUDA_TRY(c, c->d_boff.ensure(std::max<size_t>(1, n) * sizeof(uint64_t)));
     CUDA_TRY(c, c->d_total.ensure(64));
@@ -509,7 +525,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
     cudaEvent_t prev_scan = c->ev_start;
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
-        sdbfg_ctx::Slot& S = c->slot[gi & 1];
+        sdbfg_ctx::Slot& S = c->slot[gi % kSlots];
         cudaStream_t st = S.stream;
         if (S.used) CUDA_TRY(c, cudaEventSynchronize(S.done));  // its pinned tables may be reused now
         S.used = true;
@@ -627,8 +643,8 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
                                                              c->d_boff.as<uint64_t>() + g.first, g.count,
                                                              c->d_total.as<uint64_t>()),
                          cudaGetLastError()));
-        CUDA_TRY(c, cudaEventRecord(c->ev_scan[gi & 1], st));
-        prev_scan = c->ev_scan[gi & 1];
+        CUDA_TRY(c, cudaEventRecord(c->ev_scan[gi % kSlots], st));
+        prev_scan = c->ev_scan[gi % kSlots];
         TIMED_LAUNCH_ON(c, "k_pack_filters", st,
                         (k_pack_group<<<std::min<uint32_t>(g.count, (uint32_t)c->sms * 8), 256, 0, st>>>(
                              S.work.as<uint32_t>(), S.files.as<GenFile>(), c->d_binfo.as<FileInfoDev>() + g.first,
@@ -637,7 +653,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         CUDA_TRY(c, cudaEventRecord(S.done, st));
     }
     // join: the caller's stream waits for both slots, then results come back
-    for (int k = 0; k < 2; k++)
+    for (int k = 0; k < kSlots; k++)
         if (c->slot[k].used) CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->slot[k].done, 0));
     std::vector<FileInfoDev> info(n);
     std::vector<uint64_t> off(n);
@@ -656,9 +672,10 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
                     (unsigned long long)flags_total[0]);
     for (uint32_t i = 0; i < n; i++) {
         if (lens[i] < kMinFile) continue;
-        res[i].bf_count = info[i].bf_count;
-        res[i].last_count = info[i].last_count;
-        res[i].filter_offset = off[i];
+        sdbfg_digest_result& r = res[perm[i]];
+        r.bf_count = info[i].bf_count;
+        r.last_count = info[i].last_count;
+        r.filter_offset = off[i];
     }
     if (total_out) *total_out = flags_total[0];
     return SDBFG_OK;
