@@ -45,6 +45,10 @@ CONFIG_BASE = {"workload": "bulk stream-mode digest generation", "files": 4096, 
                "mode": "stream (-b 0)", "l2": "inputs larger than L2 (no flush needed)"}
 
 
+KERNELS = ("k_stream_tiles", "k_stream_check", "k_stream_fix", "k_stream_commit", "k_pack_filters",
+           "k_scan_offsets")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -274,7 +278,6 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = ctx.launch_count
-    ctx.profile(True)
     barrier(world)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -289,14 +292,22 @@ def main():
     clocks.stop()
     dev_ms = e0.elapsed_time(e1)
     launches = ctx.launch_count - launches0
-    tiles_ms, tiles_n = ctx.kernel_time("k_stream_tiles")
-    kern = {k: ctx.kernel_time(k) for k in ("k_stream_tiles", "k_stream_verify", "k_stream_commit", "k_pack_filters",
-                                            "k_scan_offsets")}
+
+    # One more step, outside the timed region, with launch groups run one
+    # after another and per-kernel CUDA events on the launch stream: the
+    # kernels do not overlap, so each event pair brackets one kernel alone.
+    ctx.set_pipeline_depth(1)
+    ctx.profile(True)
+    step_device()
+    torch.cuda.synchronize()
+    kern = {k: ctx.kernel_time(k) for k in KERNELS}
     ntile_ph = ctx.kernel_time("k_stream_tiles.count")[0] or 1.0
     phases = {k: ctx.kernel_time("k_stream_tiles." + k)[0] / ntile_ph
               for k in ("load", "ranks", "fres", "walk", "link", "compact", "sha1", "fixups")}
     commit_ph = {k: ctx.kernel_time("k_stream_commit." + k)[0] for k in ("wait", "busy", "groups", "loops", "max_file")}
     ctx.profile(False)
+    ctx.set_pipeline_depth(3)
+    tiles_ms, tiles_n = kern["k_stream_tiles"]
     ms_per_step = allmax(world, dev_ms / args.steps)
     bytes_all = allsum(world, total_bytes)
     value = bytes_all / (ms_per_step / 1e3) / 1e9
@@ -319,7 +330,7 @@ def main():
         del ds
 
     peak, peak_kind = peaks()
-    ngroups = max(1, tiles_n // max(1, args.steps))
+    ngroups = max(1, tiles_n)
     per_launch_bytes = total_bytes / ngroups
     tile_ms = tiles_ms / max(1, tiles_n)
     achieved = per_launch_bytes / (tile_ms / 1e3) / 1e9 if tile_ms > 0 else None
@@ -329,7 +340,7 @@ def main():
                 "traffic": (tpb * per_launch_bytes) if tpb else None,
                 "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
                 "algorithmic_bytes_per_launch": per_launch_bytes,
-                "kernel_ms_per_step": {k: v[0] / args.steps for k, v in kern.items()},
+                "kernel_ms_unoverlapped_step": {k: v[0] for k, v in kern.items()},
                 "tile_phase_cycles_per_tile": phases, "commit_phase_totals": commit_ph}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",

@@ -53,7 +53,7 @@ uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx *ctx);
 /* Per-kernel timing with CUDA events recorded on the launch stream around
  * every launch (off by default; enabling clears previous totals).
  * sdbfg_ctx_kernel_time reports the accumulated milliseconds and launch
- * count of one kernel ("k_stream_tiles", "k_stream_verify",
+ * count of one kernel ("k_stream_tiles", "k_stream_check", "k_stream_fix",
  * "k_stream_commit", "k_pack_filters", "k_block_digest", "k_compare_pairs",
  * "k_scan_offsets").  While profiling, the stream kernels also count SM
  * cycles per phase; the names "k_stream_tiles.{load,ranks,fres,walk,link,
@@ -68,6 +68,12 @@ int sdbfg_ctx_kernel_time(sdbfg_ctx *ctx, const char *kernel, double *total_ms, 
  * lead-ins only make the re-walk path run more often; tests use this to
  * exercise it.  No counterpart in the reference (its walk is sequential). */
 int sdbfg_ctx_set_lead(sdbfg_ctx *ctx, uint32_t steps);
+/* Stream-mode launch groups (<= 2 GiB of input each) kept in flight on
+ * separate streams, 1..3 (default 3): the ordered commit of one group
+ * overlaps the next groups' tile kernels.  Depth 1 runs groups one after
+ * another (used to time kernels without overlap).  Tuning knob without a
+ * counterpart in the reference. */
+int sdbfg_ctx_set_pipeline_depth(sdbfg_ctx *ctx, int depth);
 /* Tiles whose speculative popularity chain was re-walked (instrumentation). */
 uint64_t sdbfg_ctx_relinked_tiles(sdbfg_ctx *ctx);
 

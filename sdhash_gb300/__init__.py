@@ -72,6 +72,7 @@ def lib() -> C.CDLL:
         L.sdbfg_ctx_launch_count.argtypes = [vp]
         L.sdbfg_ctx_launch_count.restype = C.c_uint64
         L.sdbfg_ctx_set_lead.argtypes = [vp, C.c_uint32]
+        L.sdbfg_ctx_set_pipeline_depth.argtypes = [vp, C.c_int]
         L.sdbfg_ctx_profile.argtypes = [vp, C.c_int]
         L.sdbfg_ctx_kernel_time.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         L.sdbfg_ctx_relinked_tiles.argtypes = [vp]
@@ -236,6 +237,10 @@ class Context:
     def set_lead(self, steps: int):
         """Speculative lead-in of the parallel score walk (exact for any value)."""
         self._check(lib().sdbfg_ctx_set_lead(self.h, steps))
+
+    def set_pipeline_depth(self, depth: int):
+        """Stream-mode launch groups in flight (1..3); 1 = no overlap."""
+        self._check(lib().sdbfg_ctx_set_pipeline_depth(self.h, depth))
 
     def profile(self, enable: bool = True):
         """Per-kernel CUDA-event timing on the launch stream."""

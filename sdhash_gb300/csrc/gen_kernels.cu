@@ -9,9 +9,11 @@
 //                   (gen_chunk_scores :50-89, parallelised below) ->
 //                   selection score > 16 -> SHA-1 of every selected 64-byte
 //                   feature.  Writes the ordered feature digests of the tile.
-//  k_stream_verify  one CTA per chunk: checks that each tile's speculative
-//                   entry state matches its predecessor's exit state and
-//                   recomputes a tile in place when it does not.
+//  k_stream_check   one warp per chunk: finds the first tile whose
+//                   speculative entry state differs from its predecessor's
+//                   exit state.
+//  k_stream_fix     one CTA per chunk with such a tile (others exit at
+//                   once): recomputes tiles in place from the true state.
 //  k_stream_commit  one warp per file: the ordered filter fill of
 //                   gen_chunk_hash (:93-136) -- 256-byte filter insert with
 //                   zero-new-bit suppression, the 16 KiB "big filter"
@@ -32,7 +34,7 @@
 // with the state its left neighbour reaches at the same step.  Equal states
 // prove the segment exact (induction from step 0, which is always a full
 // rescan); a mismatch is re-walked from the neighbour's state.  The same
-// check links consecutive tiles of a chunk (k_stream_verify).
+// check links consecutive tiles of a chunk (k_stream_check / k_stream_fix).
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -596,23 +598,48 @@ __global__ void __launch_bounds__(kGenThreads, 4) k_stream_tiles(GenParams P) {
     }
 }
 
-// One CTA per chunk: link tiles; recompute a tile whose speculative entry
-// state differs from its predecessor's exit state.
-__global__ void __launch_bounds__(kGenThreads) k_stream_verify(GenParams P) {
+// Link tiles of a chunk: a tile's speculative entry state must equal its
+// predecessor's exit state (tiles whose lead-in reaches step 0 are exact).
+// k_stream_check (one warp per chunk, no shared memory) finds the first
+// tile of each chunk whose link fails; k_stream_fix (one CTA per chunk,
+// normally exiting at once) recomputes that tile from the true entry state
+// and walks on through the chunk, recomputing every later tile whose link
+// still fails.
+__device__ __forceinline__ bool link_fails(const GenParams& P, const GenChunk& C, uint32_t tile) {
+    const TileGeom g = stream_geom(C.n, P.tiles[tile].t0);
+    return g.S0 > tile_lead(P.lead) && P.tile_out[tile - 1].tau_out != P.tile_out[tile].sig_in;
+}
+
+__global__ void __launch_bounds__(128) k_stream_check(GenParams P) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const uint32_t nwarps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t c = warp; c < P.nchunks; c += nwarps) {
+        const GenChunk C = P.chunks[c];
+        uint32_t first = 0xFFFFFFFFu;
+        for (uint32_t j0 = 1; j0 < C.ntiles && first == 0xFFFFFFFFu; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            const bool bad = j < C.ntiles && link_fails(P, C, C.first_tile + j);
+            const uint32_t m = __ballot_sync(0xffffffffu, bad);
+            if (m) first = j0 + __ffs(m) - 1;
+        }
+        if (lane == 0) P.chunk_redo[c] = first;
+    }
+}
+
+__global__ void __launch_bounds__(kGenThreads) k_stream_fix(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t entry;
     __shared__ int redo;
     for (uint32_t c = blockIdx.x; c < P.nchunks; c += gridDim.x) {
+        const uint32_t first = P.chunk_redo[c];
+        if (first == 0xFFFFFFFFu) continue;
         const GenChunk C = P.chunks[c];
-        for (uint32_t j = 1; j < C.ntiles; j++) {
+        for (uint32_t j = first; j < C.ntiles; j++) {
             const uint32_t tile = C.first_tile + j;
             if (threadIdx.x == 0) {
-                const uint64_t prev = P.tile_out[tile - 1].tau_out;
-                const uint64_t mine = P.tile_out[tile].sig_in;
-                // a tile whose lead-in reaches step 0 is exact by construction
-                const TileGeom g = stream_geom(C.n, P.tiles[tile].t0);
-                redo = (g.S0 > tile_lead(P.lead)) && (prev != mine);
-                entry = prev;
+                redo = link_fails(P, C, tile);
+                entry = P.tile_out[tile - 1].tau_out;
             }
             __syncthreads();
             if (redo) {
@@ -987,7 +1014,7 @@ static void set_stream_attrs() {
     if (done) return;
     const int sm = (int)stream_tile_smem();
     cudaFuncSetAttribute(k_stream_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    cudaFuncSetAttribute(k_stream_verify, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(k_stream_fix, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     cudaFuncSetAttribute(k_stream_commit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(CommitSmem) * kCommitWarps));
     done = true;
@@ -999,9 +1026,14 @@ cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_stream_verify(const GenParams& P, uint32_t grid, cudaStream_t st) {
+cudaError_t launch_stream_check(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    k_stream_check<<<grid, 128, 0, st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st) {
     set_stream_attrs();
-    k_stream_verify<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
+    k_stream_fix<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
     return cudaGetLastError();
 }
 

@@ -80,6 +80,7 @@ struct GenParams {
     uint32_t block_lmax;         // block mode: max window steps per block
     uint32_t lead;               // speculative lead-in steps (<= kLead)
     unsigned long long* phase;   // optional phase cycle counters (kPhase*), null = off
+    uint32_t* chunk_redo;        // per chunk: first tile whose link failed (stream)
 };
 
 // Phase counters (cycles summed over CTAs / warps) when GenParams::phase is set.
@@ -91,7 +92,8 @@ enum : int {
 size_t stream_tile_smem();
 size_t block_smem(uint32_t lmax);
 cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t st);
-cudaError_t launch_stream_verify(const GenParams& P, uint32_t grid, cudaStream_t st);
+cudaError_t launch_stream_check(const GenParams& P, uint32_t grid, cudaStream_t st);  // 4 chunks per CTA
+cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st);
 cudaError_t launch_stream_commit(const GenParams& P, uint32_t grid, cudaStream_t st);
 cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st);
 

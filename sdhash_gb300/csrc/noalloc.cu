@@ -51,7 +51,8 @@ constexpr uint64_t kOffInfo = align256(kOffOrder + sizeof(uint32_t) * kMaxInputs
 constexpr uint64_t kOffTileOut = align256(kOffInfo + sizeof(FileInfoDev) * kMaxInputs);
 constexpr uint64_t kOffPack = align256(kOffTileOut + sizeof(TileOut) * kMaxTiles);
 constexpr uint64_t kOffWork = align256(kOffPack + (8 + 8 + 4) * kMaxInputs);
-constexpr uint64_t kOffFeat = align256(kOffWork + 256 * kMaxFilters);
+constexpr uint64_t kOffRedo = align256(kOffWork + 256 * kMaxFilters);
+constexpr uint64_t kOffFeat = align256(kOffRedo + sizeof(uint32_t) * kMaxInputs);
 constexpr uint64_t kScratchBytes = align256(kOffFeat + 4ull * 5 * kTileCap * kMaxTiles);
 
 static_assert(kScratchBytes <= SDBFG_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds the stated size");
@@ -201,10 +202,12 @@ extern "C" int sdbfg_digest_stream_noalloc(const uint8_t* dev_data, const uint64
     P.counters = reinterpret_cast<uint32_t*>(base + kOffCounters);
     P.rank_tab = reinterpret_cast<const uint16_t*>(base + kOffRank);
     P.ent_tab = reinterpret_cast<const uint32_t*>(base + kOffEnt);
+    P.chunk_redo = reinterpret_cast<uint32_t*>(base + kOffRedo);
     P.lead = kDefaultLead;
     const uint32_t cap3 = (uint32_t)sms * 3 * 16;
     if (ntiles) NA_TRY(launch_stream_tiles(P, ntiles < cap3 ? ntiles : cap3, st));
-    if (nchunks) NA_TRY(launch_stream_verify(P, nchunks < cap3 ? nchunks : cap3, st));
+    if (nchunks) NA_TRY(launch_stream_check(P, (nchunks + 3) / 4, st));
+    if (nchunks) NA_TRY(launch_stream_fix(P, nchunks < cap3 ? nchunks : cap3, st));
     if (n) NA_TRY(launch_stream_commit(P, (n + kCommitWarps - 1) / kCommitWarps, st));
     FileInfoDev info[kMaxInputs];
     uint32_t flags[2] = {0, 0};

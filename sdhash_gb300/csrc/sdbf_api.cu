@@ -26,6 +26,7 @@ constexpr uint32_t kMaxTilesPerLaunch = 1u << 18;  // 2 GiB of stream input per 
 constexpr uint64_t kMaxBytesPerLaunch = 2ull << 30;
 constexpr uint32_t kMinFile = 512;                 // MIN_FILE_SIZE (sdbf_defines.h:56)
 constexpr uint64_t kPairsPerLaunch = 1ull << 22;
+constexpr int kSlots = 3;  // stream-mode launch groups in flight
 
 struct DevBuf {
     void* p = nullptr;
@@ -107,9 +108,10 @@ struct sdbfg_ctx {
         cudaStream_t stream = nullptr;
         cudaEvent_t done = nullptr;
         bool used = false;
-        DevBuf data, chunks, tiles, files, order, tile_out, features, work;
+        DevBuf data, chunks, tiles, files, order, tile_out, features, work, redo;
         HostBuf h_tables;
     } slot[3];
+    int depth = 3;  // launch groups in flight
     DevBuf d_binfo, d_boff, d_total, d_phase;
     cudaEvent_t ev_scan[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev_start = nullptr;
@@ -234,7 +236,8 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
                       &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase})
         b->release();
     for (auto& S : c->slot) {
-        for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work})
+        for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work,
+                          &S.redo})
             b->release();
         S.h_tables.release();
         if (S.stream) cudaStreamDestroy(S.stream);
@@ -301,6 +304,12 @@ extern "C" int sdbfg_ctx_kernel_time(sdbfg_ctx* c, const char* name, double* tot
             if (total_ms) *total_ms = k.ms;
             if (launches) *launches = k.launches;
         }
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_ctx_set_pipeline_depth(sdbfg_ctx* c, int depth) {
+    if (!c || depth < 1 || depth > kSlots) return SDBFG_ERR_ARG;
+    c->depth = depth;
     return SDBFG_OK;
 }
 
@@ -475,8 +484,6 @@ __global__ void k_pack_group(const uint32_t* __restrict__ work, const GenFile* _
     }
 }
 
-constexpr int kSlots = 3;  // launch groups in flight (one tiles kernel + up to two commits)
-
 static int ensure_pipeline(sdbfg_ctx* c) {
     for (int k = 0; k < kSlots; k++) {
         if (!c->slot[k].stream) {
@@ -525,7 +532,8 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
     cudaEvent_t prev_scan = c->ev_start;
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
-        sdbfg_ctx::Slot& S = c->slot[gi % kSlots];
+        const int depth = std::max(1, std::min(c->depth, kSlots));
+        sdbfg_ctx::Slot& S = c->slot[gi % depth];
         cudaStream_t st = S.stream;
         if (S.used) CUDA_TRY(c, cudaEventSynchronize(S.done));  // its pinned tables may be reused now
         S.used = true;
@@ -605,6 +613,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         CUDA_TRY(c, S.tile_out.ensure(std::max<uint64_t>(1, ntiles) * sizeof(TileOut)));
         CUDA_TRY(c, S.features.ensure(std::max<uint64_t>(1, ntiles) * 5ull * kTileCap * 4));
         CUDA_TRY(c, S.work.ensure(std::max<uint64_t>(1, work) * 256));
+        CUDA_TRY(c, S.redo.ensure(std::max<uint64_t>(1, nchunks) * 4));
         if (tb_chunks) CUDA_TRY(c, cudaMemcpyAsync(S.chunks.p, hc, tb_chunks, cudaMemcpyHostToDevice, st));
         if (tb_tiles) CUDA_TRY(c, cudaMemcpyAsync(S.tiles.p, ht, tb_tiles, cudaMemcpyHostToDevice, st));
         CUDA_TRY(c, cudaMemcpyAsync(S.files.p, hf, tb_files, cudaMemcpyHostToDevice, st));
@@ -627,12 +636,15 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         P.features = S.features.as<uint32_t>();
         P.out_filters = S.work.as<uint32_t>();
         P.out_info = c->d_binfo.as<FileInfoDev>() + g.first;
+        P.chunk_redo = S.redo.as<uint32_t>();
         const uint32_t cap_grid = (uint32_t)c->sms * 3 * 16;
         if (P.ntiles)
             TIMED_LAUNCH_ON(c, "k_stream_tiles", st, launch_stream_tiles(P, std::min<uint32_t>(P.ntiles, cap_grid), st));
-        if (P.nchunks)
-            TIMED_LAUNCH_ON(c, "k_stream_verify", st,
-                            launch_stream_verify(P, std::min<uint32_t>(P.nchunks, cap_grid), st));
+        if (P.nchunks) {
+            TIMED_LAUNCH_ON(c, "k_stream_check", st, launch_stream_check(P, (P.nchunks + 3) / 4, st));
+            TIMED_LAUNCH_ON(c, "k_stream_fix", st,
+                            launch_stream_fix(P, std::min<uint32_t>(P.nchunks, cap_grid), st));
+        }
         TIMED_LAUNCH_ON(c, "k_stream_commit", st,
                         launch_stream_commit(P, std::min<uint32_t>((g.count + kCommitWarps - 1) / kCommitWarps,
                                                                    cap_grid), st));
@@ -643,8 +655,8 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
                                                              c->d_boff.as<uint64_t>() + g.first, g.count,
                                                              c->d_total.as<uint64_t>()),
                          cudaGetLastError()));
-        CUDA_TRY(c, cudaEventRecord(c->ev_scan[gi % kSlots], st));
-        prev_scan = c->ev_scan[gi % kSlots];
+        CUDA_TRY(c, cudaEventRecord(c->ev_scan[gi % depth], st));
+        prev_scan = c->ev_scan[gi % depth];
         TIMED_LAUNCH_ON(c, "k_pack_filters", st,
                         (k_pack_group<<<std::min<uint32_t>(g.count, (uint32_t)c->sms * 8), 256, 0, st>>>(
                              S.work.as<uint32_t>(), S.files.as<GenFile>(), c->d_binfo.as<FileInfoDev>() + g.first,
