@@ -178,6 +178,29 @@ int sdbfg_compare_all(sdbfg_ctx *ctx, const sdbfg_set *set, int32_t *out_scores)
  * out[i*nt + j] = score(query i, target j). */
 int sdbfg_compare_to(sdbfg_ctx *ctx, const sdbfg_set *queries, const sdbfg_set *targets, int32_t *out_scores);
 
+/* sdbfg_compare_all / sdbfg_compare_to run on the batched engine: one
+ * persistent launch over work units (a reference digest against a run of
+ * target digests, largest units first), replayed as a CUDA graph when the
+ * same sets are compared again.  The _device forms write the scores to a
+ * device array (same layout) and return without waiting: the work is
+ * queued on the context stream.  Batched forms of the reference's
+ * OpenMP loops (sdbf/sdbf_set.cc:249-265, 330-346); no single counterpart. */
+int sdbfg_compare_all_device(sdbfg_ctx *ctx, const sdbfg_set *set, int32_t *dev_scores);
+int sdbfg_compare_to_device(sdbfg_ctx *ctx, const sdbfg_set *queries, const sdbfg_set *targets,
+                            int32_t *dev_scores);
+/* Filter pairs the comparison scores (sum of n_ref * n_target over pairs). */
+uint64_t sdbfg_compare_filter_pairs(sdbfg_ctx *ctx, const sdbfg_set *a, const sdbfg_set *b_or_null);
+/* Engine tuning: kernel variant 0..4 (rows per CTA x target filters per
+ * shared-memory tile: 128x32, 128x16, 128x64, 64x32, 256x32), unit work
+ * budget in filter pairs, CUDA-graph replay on/off.  The autotuner times
+ * every variant and budget 2^20, 2^22, 2^24 on a sample of about
+ * sample_pairs filter pairs of the given job (b NULL: all pairs of a) and
+ * keeps the fastest in the context.  No counterpart in the reference. */
+int sdbfg_ctx_set_compare_tuning(sdbfg_ctx *ctx, int variant, uint64_t unit_work, int use_graphs);
+int sdbfg_ctx_get_compare_tuning(const sdbfg_ctx *ctx, int *variant, uint64_t *unit_work);
+int sdbfg_compare_autotune(sdbfg_ctx *ctx, const sdbfg_set *a, const sdbfg_set *b_or_null, uint64_t sample_pairs,
+                           int *out_variant, uint64_t *out_unit_work, double *out_pairs_per_s);
+
 /* ------------------------------------------------------------ SDBF text */
 /* sdbf::to_string (sdbf/sdbf_class.cc:293-334): one SDBF v3 line with
  * trailing newline.  Writes at most cap bytes (NUL-terminated); returns the

@@ -90,6 +90,14 @@ def lib() -> C.CDLL:
         L.sdbfg_score_pairs.argtypes = [vp, vp, vp, u32p, u32p, C.c_uint64, i32p]
         L.sdbfg_compare_all.argtypes = [vp, vp, i32p]
         L.sdbfg_compare_to.argtypes = [vp, vp, vp, i32p]
+        L.sdbfg_compare_all_device.argtypes = [vp, vp, vp]
+        L.sdbfg_compare_to_device.argtypes = [vp, vp, vp, vp]
+        L.sdbfg_compare_filter_pairs.argtypes = [vp, vp, vp]
+        L.sdbfg_compare_filter_pairs.restype = C.c_uint64
+        L.sdbfg_ctx_set_compare_tuning.argtypes = [vp, C.c_int, C.c_uint64, C.c_int]
+        L.sdbfg_ctx_get_compare_tuning.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]
+        L.sdbfg_compare_autotune.argtypes = [vp, vp, vp, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_uint64),
+                                             C.POINTER(C.c_double)]
         L.sdbfg_to_string.argtypes = [C.POINTER(DigestDesc), C.c_char_p, C.c_uint64]
         L.sdbfg_to_string.restype = C.c_int64
         L.sdbfg_parse.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(DigestDesc), C.c_char_p, C.c_uint64, vp, vp]
@@ -338,6 +346,32 @@ class Context:
         if len(q) and len(t):
             self._check(lib().sdbfg_compare_to(self.h, q.h, t.h, _ptr(out, C.c_int32)))
         return out[: len(q) * len(t)].reshape(len(q), len(t))
+
+    def compare_all_device(self, s: DeviceSet, dev_scores: int):
+        """Queue all-pairs scores of s into a device int32 array (n*(n-1)/2)."""
+        self._check(lib().sdbfg_compare_all_device(self.h, s.h, C.c_void_p(dev_scores)))
+
+    def compare_to_device(self, q: DeviceSet, t: DeviceSet, dev_scores: int):
+        """Queue query x target scores into a device int32 array (nq*nt)."""
+        self._check(lib().sdbfg_compare_to_device(self.h, q.h, t.h, C.c_void_p(dev_scores)))
+
+    def filter_pairs(self, a: DeviceSet, b: DeviceSet | None = None) -> int:
+        return int(lib().sdbfg_compare_filter_pairs(self.h, a.h, b.h if b is not None else None))
+
+    def set_compare_tuning(self, variant: int = 0, unit_work: int = 1 << 22, graphs: bool = True):
+        self._check(lib().sdbfg_ctx_set_compare_tuning(self.h, variant, unit_work, int(graphs)))
+
+    def compare_tuning(self) -> tuple[int, int]:
+        v, w = C.c_int(), C.c_uint64()
+        self._check(lib().sdbfg_ctx_get_compare_tuning(self.h, C.byref(v), C.byref(w)))
+        return v.value, w.value
+
+    def autotune_compare(self, a: DeviceSet, b: DeviceSet | None = None, sample_pairs: int = 1 << 34):
+        """Pick the fastest kernel variant and unit budget; returns (variant, unit_work, pairs/s)."""
+        v, w, r = C.c_int(), C.c_uint64(), C.c_double()
+        self._check(lib().sdbfg_compare_autotune(self.h, a.h, b.h if b is not None else None, sample_pairs,
+                                                 C.byref(v), C.byref(w), C.byref(r)))
+        return v.value, w.value, r.value
 
     def score_pairs(self, a: DeviceSet, b: DeviceSet, ia, ib) -> np.ndarray:
         ia = np.ascontiguousarray(ia, dtype=np.uint32)

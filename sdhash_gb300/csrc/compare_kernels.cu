@@ -23,20 +23,130 @@
 #include "compare_kernels.h"
 #include "sdbf_device.cuh"
 
+// Two kernels: k_compare_pairs (one CTA per listed pair: the per-call path)
+// and k_matrix (the batched engine: persistent CTAs over work units of one
+// reference digest against a run of targets).
+//
+// Per filter pair the reference computes a staged AND-popcount whose
+// early exits only ever turn a count into 0, followed by
+// "match <= cut -> 0".  A pair can therefore contribute a non-zero score
+// only if its full 2048-bit AND-popcount exceeds the cut.  The engine
+// computes the full count of every pair with a carry-save (Harley-Seal)
+// adder tree -- 3-input LOP3 majority / parity over the 64 ANDed words, 8
+// POPC instead of 64 -- and runs the reference's staged tests only for the
+// pairs above the cut, which gives exactly the reference's value for every
+// pair.
+
 namespace sdbfg {
 
 constexpr int kTgtTile = 32;  // target filters staged per shared-memory tile
 
-__device__ __forceinline__ uint32_t popc_and(const uint32_t (&a)[64], const uint4* t, int w0, int w1) {
+namespace {
+
+__device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, 0x96;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+__device__ __forceinline__ uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("lop3.b32 %0, %1, %2, %3, 0xE8;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+// carry-save adder: (h, l) = a + b + c bitwise
+#define MAT_CSA(h, l, a, b, c)            \
+    do {                                  \
+        const uint32_t a_ = (a), b_ = (b), c_ = (c); \
+        (h) = maj3(a_, b_, c_);           \
+        (l) = xor3(a_, b_, c_);           \
+    } while (0)
+
+// popcount(a & t) over 64 words: a in registers, t in shared memory.
+__device__ __forceinline__ uint32_t and_popc_hs(const uint32_t (&a)[64], const uint32_t* t) {
+    const uint4* t4 = reinterpret_cast<const uint4*>(t);
+    uint32_t ones = 0, twos = 0, fours = 0, eights = 0, total16 = 0;
+#pragma unroll
+    for (int blk = 0; blk < 4; blk++) {
+        uint32_t x[16];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint4 v = t4[blk * 4 + q];
+            x[4 * q + 0] = a[blk * 16 + 4 * q + 0] & v.x;
+            x[4 * q + 1] = a[blk * 16 + 4 * q + 1] & v.y;
+            x[4 * q + 2] = a[blk * 16 + 4 * q + 2] & v.z;
+            x[4 * q + 3] = a[blk * 16 + 4 * q + 3] & v.w;
+        }
+        uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
+        MAT_CSA(twosA, ones, ones, x[0], x[1]);
+        MAT_CSA(twosB, ones, ones, x[2], x[3]);
+        MAT_CSA(foursA, twos, twos, twosA, twosB);
+        MAT_CSA(twosA, ones, ones, x[4], x[5]);
+        MAT_CSA(twosB, ones, ones, x[6], x[7]);
+        MAT_CSA(foursB, twos, twos, twosA, twosB);
+        MAT_CSA(eightsA, fours, fours, foursA, foursB);
+        MAT_CSA(twosA, ones, ones, x[8], x[9]);
+        MAT_CSA(twosB, ones, ones, x[10], x[11]);
+        MAT_CSA(foursA, twos, twos, twosA, twosB);
+        MAT_CSA(twosA, ones, ones, x[12], x[13]);
+        MAT_CSA(twosB, ones, ones, x[14], x[15]);
+        MAT_CSA(foursB, twos, twos, twosA, twosB);
+        MAT_CSA(eightsB, fours, fours, foursA, foursB);
+        MAT_CSA(sixteens, eights, eights, eightsA, eightsB);
+        total16 += __popc(sixteens);
+    }
+    return 16 * total16 + 8 * __popc(eights) + 4 * __popc(fours) + 2 * __popc(twos) + __popc(ones);
+}
+
+// The reference's staged exits (bf_utils.cc:114-206) for a pair whose full
+// count is above the cut: true when an early stage would have returned 0.
+__device__ __forceinline__ bool staged_exit(const uint32_t (&a)[64], const uint32_t* t, uint32_t cut) {
     uint32_t c = 0;
 #pragma unroll
-    for (int q = w0 / 4; q < w1 / 4; q++) {
-        const uint4 v = t[q];
-        c += __popc(a[4 * q] & v.x) + __popc(a[4 * q + 1] & v.y);
-        c += __popc(a[4 * q + 2] & v.z) + __popc(a[4 * q + 3] & v.w);
-    }
-    return c;
+    for (int w = 0; w < 8; w++) c += __popc(a[w] & t[w]);
+    if (8 * c + 48 < cut) return true;
+#pragma unroll
+    for (int w = 8; w < 16; w++) c += __popc(a[w] & t[w]);
+    if (4 * c + 48 < cut) return true;
+#pragma unroll
+    for (int w = 16; w < 32; w++) c += __popc(a[w] & t[w]);
+    return 2 * c + 48 < cut;
 }
+
+__device__ __forceinline__ uint32_t cut_for(const uint16_t* cut_sum, const uint16_t* cut256, uint32_t s1,
+                                            uint32_t s2) {
+    const uint32_t sum = s1 + s2;
+    return sum < 1024 ? cut_sum[sum] : cut256[4096u / sum];
+}
+
+// A filter's maximum against one target, packed: 0xFFFFFFFF = -1 (no target
+// filter with >= 16 elements), else (num << 16) | den for num/den (0/1 = 0).
+constexpr uint32_t kMaxNone = 0xFFFFFFFFu;
+
+__device__ __forceinline__ double unpack_max(uint32_t v) {
+    if (v == kMaxNone) return -1.0;
+    const uint32_t num = v >> 16, den = v & 0xFFFFu;
+    return num == 0 ? 0.0 : __ddiv_rn((double)num, (double)den);
+}
+
+__device__ __forceinline__ uint64_t out_index(const MatParams& P, bool ref_side1, uint32_t ref, uint32_t tgt) {
+    if (P.mode == kMatModeAll) {
+        const uint64_t i = min(ref, tgt), j = max(ref, tgt);
+        return i * (2ull * P.n - i - 1) / 2 + (j - i - 1);
+    }
+    const uint64_t q = ref_side1 ? tgt : ref, t = ref_side1 ? ref : tgt;
+    return q * P.n + t;
+}
+
+__device__ __forceinline__ int32_t final_score(double sum, uint32_t n1, uint32_t sparse) {
+    uint64_t denom = n1;
+    if (n1 > 1) denom -= sparse;
+    if (denom == 0 || sum < 0) return -1;
+    return (int32_t)floor(__dadd_rn(__ddiv_rn(__dmul_rn(100.0, sum), (double)denom), 0.5));
+}
+
+}  // namespace
 
 __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
     __shared__ __align__(16) uint32_t tf[kTgtTile][64];
@@ -95,24 +205,9 @@ __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
                         const uint32_t e2 = meta >> 16;
                         const uint32_t max_est = min(e1, e2);
                         const uint32_t cut = cut_tab[4096u / (s1 + s2)];
-                        const uint4* t = reinterpret_cast<const uint4*>(&tf[j][0]);
-                        uint32_t c = popc_and(a, t, 0, 8);
-                        uint32_t match = 0;
-                        if (!(8 * c + 48 < cut)) {
-                            c += popc_and(a, t, 8, 16);
-                            if (!(4 * c + 48 < cut)) {
-                                c += popc_and(a, t, 16, 32);
-                                if (!(2 * c + 48 < cut)) {
-                                    c += popc_and(a, t, 32, 64);
-                                    match = c;
-                                }
-                            }
-                        }
-                        uint32_t num, den;
-                        if (match <= cut) {
-                            num = 0;
-                            den = 1;
-                        } else {
+                        const uint32_t match = and_popc_hs(a, &tf[j][0]);
+                        uint32_t num = 0, den = 1;
+                        if (match > cut && !staged_exit(a, &tf[j][0], cut)) {
                             num = match - cut;
                             den = max_est - cut;
                         }
@@ -156,6 +251,259 @@ __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
 cudaError_t launch_compare_pairs(const CmpParams& P, uint32_t grid, cudaStream_t st) {
     if (P.npairs) k_compare_pairs<<<grid, kCmpThreads, 0, st>>>(P);
     return cudaGetLastError();
+}
+
+}  // namespace sdbfg
+
+// ---------------------------------------------------------- matrix engine
+namespace sdbfg {
+
+const MatVariant kMatVariantTable[kMatVariants] = {{128, 32}, {128, 16}, {128, 64}, {64, 32}, {256, 32}};
+
+template <int R, int TJ>
+struct MatSmem {
+    uint32_t tf[TJ][64];          // target filters of the current tile
+    uint32_t tmeta[TJ];
+    uint32_t tinfo[TJ];           // local target index | completion index << 16 | last << 31
+    uint32_t gidx[TJ];            // global filter index per slot
+    uint32_t comp[TJ];            // local target index of the k-th completed target
+    uint32_t mv[R][TJ + 1];       // per row and completed target: packed maximum
+    double run[kMatMaxTargets];   // running sums per target of the unit
+    uint16_t cut_sum[1024];
+    uint16_t cut256[SDBF_CUTOFF_BINS];
+    MatUnit unit;
+    uint32_t unit_id, ntile, ncomp, cur_t, cur_f, sparse;
+};
+
+template <int R, int TJ>
+__global__ void __launch_bounds__(R) k_matrix(MatParams P) {
+    extern __shared__ __align__(16) uint8_t mat_smem[];
+    MatSmem<R, TJ>& S = *reinterpret_cast<MatSmem<R, TJ>*>(mat_smem);
+    const uint32_t tid = threadIdx.x, lane = tid & 31;
+    for (uint32_t i = tid; i < 1024; i += R)
+        S.cut_sum[i] = P.cutoffs[i >= 32 ? 4096u / i : (uint32_t)SDBF_CUTOFF_BINS - 1];
+    for (uint32_t i = tid; i < SDBF_CUTOFF_BINS; i += R) S.cut256[i] = P.cutoffs[i];
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t u = atomicAdd(P.next_unit, 1u);
+            S.unit_id = u;
+            if (u < P.nunits) S.unit = P.units[u];
+        }
+        __syncthreads();
+        if (S.unit_id >= P.nunits) break;
+        const MatUnit U = S.unit;
+        const uint32_t rs = U.flags & kUnitRefSide1 ? 1 : 0, ts = U.flags & kUnitTgtSide1 ? 1 : 0;
+        const bool split = (U.flags & kUnitSplit) != 0;
+        const CmpDigest A = P.digests[rs][U.ref];
+        const uint32_t nT = U.t1 - U.t0;
+        for (uint32_t k = tid; k < nT && !split; k += R) S.run[k] = -1.0;
+        if (tid == 0) S.sparse = 0;
+        __syncthreads();
+        for (uint32_t rc = U.r0; rc < U.r1; rc += R) {
+            const uint32_t row = rc + tid;
+            const bool have = row < U.r1;
+            uint32_t a[64];
+            uint32_t s1 = 0, e1 = 0;
+            if (have) {
+                const uint32_t m = P.meta[rs][A.first + row];
+                s1 = m & 0xFFFFu;
+                e1 = m >> 16;
+                const uint4* src = reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)(A.first + row) * 64);
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const uint4 v = __ldg(src + q);
+                    a[4 * q] = v.x; a[4 * q + 1] = v.y; a[4 * q + 2] = v.z; a[4 * q + 3] = v.w;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 64; q++) a[q] = 0;
+            }
+            const bool active = have && s1 >= (uint32_t)kMinElem;
+            const uint32_t nsparse = __syncthreads_count(have && !active);
+            if (tid == 0) {
+                S.sparse += nsparse;
+                S.cur_t = 0;
+                S.cur_f = 0;
+            }
+            uint32_t bnum = 0, bden = 0;  // bden == 0: no counted target filter yet
+            const uint32_t nrows = min((uint32_t)R, U.r1 - rc);
+            __syncthreads();
+            for (;;) {
+                const bool more = S.cur_t < nT;
+                __syncthreads();  // every thread has read the cursor before warp 0 moves it
+                if (!more) break;
+                // ---- tile composition (warp 0): targets cur_t.. fill TJ slots in order
+                if (tid < 32) {
+                    const uint32_t te = S.cur_t + lane;
+                    const uint32_t f0 = lane == 0 ? S.cur_f : 0;
+                    uint32_t rem = 0, first = 0;
+                    if (te < nT) {
+                        const CmpDigest B = P.digests[ts][P.targets[U.t0 + te]];
+                        rem = B.nfilters - f0;
+                        first = B.first + f0;
+                    }
+                    uint32_t incl = rem;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+                        if (lane >= (uint32_t)d) incl += v;
+                    }
+                    const uint32_t excl = incl - rem;
+                    const bool done_here = rem > 0 && incl <= (uint32_t)TJ;
+                    for (uint32_t s = excl; s < min(incl, (uint32_t)TJ); s++) {
+                        const uint32_t f = first + (s - excl);
+                        S.gidx[s] = f;
+                        S.tmeta[s] = P.meta[ts][f];
+                        S.tinfo[s] = te | (lane << 16) | ((done_here && s + 1 == incl) ? 0x80000000u : 0u);
+                    }
+                    if (done_here) S.comp[lane] = te;
+                    const uint32_t done_mask = __ballot_sync(0xffffffffu, done_here);
+                    const uint32_t over_mask = __ballot_sync(0xffffffffu, rem > 0 && incl > (uint32_t)TJ);
+                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                    if (lane == 0) {
+                        S.ncomp = __popc(done_mask);
+                        S.ntile = min(total, (uint32_t)TJ);
+                    }
+                    // cursor update: first lane whose target does not fit
+                    const uint32_t l = over_mask ? (uint32_t)(__ffs(over_mask) - 1) : 32u;
+                    const uint32_t ex_l = __shfl_sync(0xffffffffu, excl, l & 31);
+                    const uint32_t f0_l = __shfl_sync(0xffffffffu, f0, l & 31);
+                    if (lane == 0) {
+                        if (l < 32) {
+                            S.cur_t += l;
+                            S.cur_f = f0_l + ((uint32_t)TJ - ex_l);
+                        } else {
+                            S.cur_t = min(S.cur_t + 32u, nT);
+                            S.cur_f = 0;
+                        }
+                    }
+                }
+                __syncthreads();
+                // ---- target filters -> shared memory
+                const uint32_t nt = S.ntile;
+                for (uint32_t q = tid; q < nt * 16; q += R) {
+                    const uint4* src = reinterpret_cast<const uint4*>(P.filters[ts] + (size_t)S.gidx[q >> 4] * 64);
+                    reinterpret_cast<uint4*>(&S.tf[q >> 4][0])[q & 15] = __ldg(src + (q & 15));
+                }
+                __syncthreads();
+                // ---- every row against the tile
+                for (uint32_t j = 0; j < nt; j++) {
+                    const uint32_t tm = S.tmeta[j];
+                    const uint32_t s2 = tm & 0xFFFFu;
+                    if (active && s2 >= (uint32_t)kMinElem) {
+                        const uint32_t match = and_popc_hs(a, &S.tf[j][0]);
+                        const uint32_t cut = cut_for(S.cut_sum, S.cut256, s1, s2);
+                        uint32_t num = 0, den = 1;
+                        if (match > cut && !staged_exit(a, &S.tf[j][0], cut)) {
+                            num = match - cut;
+                            den = min(e1, tm >> 16) - cut;
+                        }
+                        if (bden == 0 || (uint64_t)num * bden > (uint64_t)bnum * den) {
+                            bnum = num;
+                            bden = den;
+                        }
+                    }
+                    const uint32_t info = S.tinfo[j];
+                    if (info & 0x80000000u) {
+                        const uint32_t packed = !active ? 1u : (bden == 0 ? kMaxNone : (bnum << 16) | bden);
+                        if (split) {
+                            if (have) P.slots[P.split[U.split].slot_base + row] = unpack_max(packed);
+                        } else {
+                            S.mv[tid][(info >> 16) & 0x7FFFu] = packed;
+                        }
+                        bnum = 0;
+                        bden = 0;
+                    }
+                }
+                __syncthreads();
+                // ---- fold the completed targets' maxima in filter order
+                if (!split) {
+                    for (uint32_t k = tid; k < S.ncomp; k += R) {
+                        double sum = S.run[S.comp[k]];
+                        for (uint32_t r = 0; r < nrows; r++) {
+                            const uint32_t v = S.mv[r][k];
+                            if (sum < 0) sum = unpack_max(v);
+                            else if (v != 1u) sum = __dadd_rn(sum, unpack_max(v));
+                        }
+                        S.run[S.comp[k]] = sum;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        if (!split) {
+            for (uint32_t k = tid; k < nT; k += R) {
+                const uint32_t tgt = P.targets[U.t0 + k];
+                P.scores[out_index(P, rs != 0, U.ref, tgt)] = final_score(S.run[k], A.nfilters, S.sparse);
+            }
+        }
+    }
+}
+
+// One thread per split pair: the ordered sum over the reference's filters.
+__global__ void k_matrix_finalize(MatParams P) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.nsplit) return;
+    const MatSplit sp = P.split[i];
+    const uint32_t rs = sp.flags & kUnitRefSide1 ? 1 : 0;
+    const CmpDigest A = P.digests[rs][sp.ref];
+    double sum = -1.0;
+    uint32_t sparse = 0;
+    for (uint32_t r = 0; r < A.nfilters; r++) {
+        const double m = P.slots[sp.slot_base + r];
+        sum = sum < 0 ? m : __dadd_rn(sum, m);
+        sparse += (P.meta[rs][A.first + r] & 0xFFFFu) < (uint32_t)kMinElem;
+    }
+    P.scores[out_index(P, rs != 0, sp.ref, sp.tgt)] = final_score(sum, A.nfilters, sparse);
+}
+
+template <int R, int TJ>
+static cudaError_t launch_variant(const MatParams& P, uint32_t grid, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_matrix<R, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(MatSmem<R, TJ>));
+        attr = true;
+    }
+    k_matrix<R, TJ><<<grid, R, sizeof(MatSmem<R, TJ>), st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_matrix(const MatParams& P, int variant, uint32_t grid, cudaStream_t st) {
+    if (P.nunits == 0) return cudaSuccess;
+    switch (variant) {
+        case 0: return launch_variant<128, 32>(P, grid, st);
+        case 1: return launch_variant<128, 16>(P, grid, st);
+        case 2: return launch_variant<128, 64>(P, grid, st);
+        case 3: return launch_variant<64, 32>(P, grid, st);
+        case 4: return launch_variant<256, 32>(P, grid, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_matrix_finalize(const MatParams& P, cudaStream_t st) {
+    if (P.nsplit) k_matrix_finalize<<<(P.nsplit + 127) / 128, 128, 0, st>>>(P);
+    return cudaGetLastError();
+}
+
+template <int R, int TJ>
+static int occupancy() {
+    int n = 0;
+    cudaFuncSetAttribute(k_matrix<R, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MatSmem<R, TJ>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_matrix<R, TJ>, R, sizeof(MatSmem<R, TJ>));
+    return n > 0 ? n : 1;
+}
+
+int matrix_ctas_per_sm(int variant) {
+    switch (variant) {
+        case 0: return occupancy<128, 32>();
+        case 1: return occupancy<128, 16>();
+        case 2: return occupancy<128, 64>();
+        case 3: return occupancy<64, 32>();
+        case 4: return occupancy<256, 32>();
+    }
+    return 1;
 }
 
 }  // namespace sdbfg

@@ -37,3 +37,64 @@ struct CmpParams {
 cudaError_t launch_compare_pairs(const CmpParams& P, uint32_t grid, cudaStream_t st);
 
 }  // namespace sdbfg
+
+// ------------------------------------------------------------------------
+// Batched comparison ("filter matrix" engine): one persistent launch scores
+// many digest pairs.  Work is cut into units: one reference digest (the side
+// whose filters are summed after the swap rule) against a run of target
+// digests from a target list, or -- for a single pair too large for one unit --
+// a row range of the reference digest against one target ("split" unit, its
+// per-filter maxima go to a slot array and k_matrix_finalize sums them).
+namespace sdbfg {
+
+constexpr uint32_t kMatMaxTargets = 512;  // targets per unit (running sums in shared memory)
+
+enum : uint32_t { kMatModeAll = 0, kMatModeCross = 1 };
+enum : uint32_t { kUnitRefSide1 = 1u, kUnitTgtSide1 = 2u, kUnitSplit = 4u };
+
+struct MatUnit {
+    uint32_t ref;     // reference digest (side: flags & kUnitRefSide1)
+    uint32_t r0, r1;  // its filters [r0, r1)
+    uint32_t t0, t1;  // target list entries [t0, t1); one entry for split units
+    uint32_t flags;
+    uint32_t split;   // split units: index into MatParams::split
+    uint32_t pad;
+};
+
+struct MatSplit {
+    uint32_t ref, tgt;
+    uint32_t flags;       // kUnitRefSide1 / kUnitTgtSide1
+    uint32_t pad;
+    uint64_t slot_base;   // maxima of ref filter r at slots[slot_base + r]
+};
+
+struct MatParams {
+    const uint32_t* filters[2];
+    const uint32_t* meta[2];
+    const CmpDigest* digests[2];
+    const MatUnit* units;
+    uint32_t nunits;
+    uint32_t* next_unit;       // work counter (zero before the launch)
+    const uint32_t* targets;   // target list (digest ids)
+    const MatSplit* split;
+    uint32_t nsplit;
+    double* slots;
+    int32_t* scores;
+    uint32_t mode;             // kMatModeAll: n*(n-1)/2 pair order; kMatModeCross: q*nt+t
+    uint32_t n;                // set size (all) / number of targets (cross)
+    const uint16_t* cutoffs;   // CUTOFFS256
+};
+
+// Kernel variants (rows per CTA x target filters per shared-memory tile),
+// chosen by the autotuner.
+struct MatVariant {
+    int rows, tile;
+};
+constexpr int kMatVariants = 5;
+extern const MatVariant kMatVariantTable[kMatVariants];
+
+cudaError_t launch_matrix(const MatParams& P, int variant, uint32_t grid, cudaStream_t st);
+cudaError_t launch_matrix_finalize(const MatParams& P, cudaStream_t st);
+int matrix_ctas_per_sm(int variant);
+
+}  // namespace sdbfg

@@ -1,7 +1,8 @@
 // sdbf_api.cu -- host orchestration behind the C ABI (include/sdbf_gb300.h).
 //
-// Owns device memory, builds the chunk / tile / file work lists for a batch,
-// launches the generation and comparison kernels and moves results back.
+// Owns the context and the generation path: builds the chunk / tile / file
+// work lists for a batch, launches the generation kernels and moves digests
+// back.  Comparison lives in compare_api.cu.
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -14,186 +15,8 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sdbf_gb300.h"
-#include "compare_kernels.h"
-#include "gen_kernels.h"
+#include "ctx_internal.h"
 #include "sdbf_tables.h"
-
-using namespace sdbfg;
-
-namespace {
-
-constexpr uint32_t kMaxTilesPerLaunch = 1u << 18;  // 2 GiB of stream input per launch group
-constexpr uint64_t kMaxBytesPerLaunch = 2ull << 30;
-constexpr uint32_t kMinFile = 512;                 // MIN_FILE_SIZE (sdbf_defines.h:56)
-constexpr uint64_t kPairsPerLaunch = 1ull << 22;
-constexpr int kSlots = 3;  // stream-mode launch groups in flight
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (bytes <= cap) return cudaSuccess;
-        const size_t want = std::max(bytes, cap + cap / 2);
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc(&p, want);
-        if (e == cudaSuccess) cap = want;
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-    template <class T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
-struct HostBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMallocHost(&p, bytes);
-        if (e == cudaSuccess) cap = bytes;
-        return e;
-    }
-    void release() {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-    }
-    template <class T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
-}  // namespace
-
-struct KernelTimer {
-    const char* name;
-    cudaEvent_t a, b;
-};
-
-struct KernelStat {
-    std::string name;
-    double ms = 0;
-    uint64_t launches = 0;
-};
-
-struct sdbfg_ctx {
-    bool profile = false;
-    std::vector<KernelTimer> pending;
-    std::vector<KernelStat> stats;
-    int device = 0;
-    cudaStream_t own = nullptr;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    uint64_t launches = 0;
-    int sms = 152;
-    uint32_t lead = kDefaultLead;
-    // constant tables
-    DevBuf d_rank, d_ent, d_cut;
-    // generation buffers
-    DevBuf d_data, d_chunks, d_tiles, d_files, d_order, d_tile_out, d_features, d_work_filters, d_info, d_counters,
-        d_pack_src, d_pack_dst_off, d_out_filters, d_out_counts;
-    HostBuf h_stage;
-    // comparison buffers
-    DevBuf d_pairs, d_scores;
-    // stream-mode pipeline: two launch-group slots on their own streams
-    struct Slot {
-        cudaStream_t stream = nullptr;
-        cudaEvent_t done = nullptr;
-        bool used = false;
-        DevBuf data, chunks, tiles, files, order, tile_out, features, work, redo;
-        HostBuf h_tables;
-    } slot[3];
-    int depth = 3;  // launch groups in flight
-    DevBuf d_binfo, d_boff, d_total, d_phase;
-    cudaEvent_t ev_scan[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t ev_start = nullptr;
-};
-
-struct sdbfg_set {
-    sdbfg_ctx* ctx = nullptr;
-    uint32_t n = 0;
-    std::vector<std::string> names;
-    std::vector<uint32_t> bf_count;
-    std::vector<uint32_t> last_elem;  // element count of the last filter (swap rule)
-    DevBuf d_filters, d_meta, d_digests;
-};
-
-// Per-kernel CUDA-event timing on the launch stream (only when enabled).
-static void timer_begin(sdbfg_ctx* c, const char* name, cudaEvent_t* a, cudaStream_t st) {
-    *a = nullptr;
-    if (!c->profile) return;
-    cudaEventCreate(a);
-    cudaEventRecord(*a, st);
-    (void)name;
-}
-
-static void timer_end(sdbfg_ctx* c, const char* name, cudaEvent_t a, cudaStream_t st) {
-    if (!c->profile || !a) return;
-    cudaEvent_t b;
-    cudaEventCreate(&b);
-    cudaEventRecord(b, st);
-    c->pending.push_back({name, a, b});
-}
-
-static void timer_collect(sdbfg_ctx* c) {
-    for (KernelTimer& t : c->pending) {
-        cudaEventSynchronize(t.b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, t.a, t.b);
-        KernelStat* st = nullptr;
-        for (KernelStat& k : c->stats)
-            if (k.name == t.name) st = &k;
-        if (!st) {
-            c->stats.push_back(KernelStat{t.name, 0, 0});
-            st = &c->stats.back();
-        }
-        st->ms += ms;
-        st->launches += 1;
-        cudaEventDestroy(t.a);
-        cudaEventDestroy(t.b);
-    }
-    c->pending.clear();
-}
-
-#define TIMED_LAUNCH_ON(c, name, st_, expr)     \
-    do {                                        \
-        cudaEvent_t ev_;                        \
-        timer_begin((c), (name), &ev_, (st_));  \
-        cudaError_t le_ = (expr);               \
-        timer_end((c), (name), ev_, (st_));     \
-        if (le_ != cudaSuccess)                 \
-            return fail((c), SDBFG_ERR_CUDA, "%s launch: %s", (name), cudaGetErrorString(le_)); \
-        (c)->launches += 1;                     \
-    } while (0)
-#define TIMED_LAUNCH(c, name, expr) TIMED_LAUNCH_ON(c, name, (c)->stream, expr)
-
-static int fail(sdbfg_ctx* c, int code, const char* fmt, ...);
-
-static int fail(sdbfg_ctx* c, int code, const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof buf, fmt, ap);
-    va_end(ap);
-    if (c) c->err = buf;
-    return code;
-}
-
-#define CUDA_TRY(ctx, call)                                                                       \
-    do {                                                                                         \
-        cudaError_t e_ = (call);                                                                 \
-        if (e_ != cudaSuccess)                                                                   \
-            return fail((ctx), e_ == cudaErrorMemoryAllocation ? SDBFG_ERR_NOMEM : SDBFG_ERR_CUDA, \
-                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);    \
-    } while (0)
 
 // ------------------------------------------------------------------ context
 extern "C" int sdbfg_ctx_create(int device, sdbfg_ctx** out) {
@@ -230,6 +53,8 @@ extern "C" int sdbfg_ctx_create(int device, sdbfg_ctx** out) {
 extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
+    for (MatPlan* p : c->plans) delete p;
+    c->plans.clear();
     for (DevBuf* b : {&c->d_rank, &c->d_ent, &c->d_cut, &c->d_data, &c->d_chunks, &c->d_tiles, &c->d_files,
                       &c->d_order, &c->d_tile_out, &c->d_features, &c->d_work_filters, &c->d_info,
                       &c->d_counters, &c->d_pack_src, &c->d_pack_dst_off, &c->d_out_filters, &c->d_out_counts,
@@ -836,166 +661,3 @@ extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const 
     return SDBFG_OK;
 }
 
-// -------------------------------------------------------------- comparison
-extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint32_t n, sdbfg_set** out) {
-    if (!c || !out || (n && !ds)) return SDBFG_ERR_ARG;
-    *out = nullptr;
-    CUDA_TRY(c, cudaSetDevice(c->device));
-    auto* s = new sdbfg_set();
-    s->ctx = c;
-    s->n = n;
-    uint64_t total = 0;
-    std::vector<CmpDigest> dig(n);
-    for (uint32_t i = 0; i < n; i++) {
-        if (ds[i].bf_count == 0 || !ds[i].filters) {
-            delete s;
-            return fail(c, SDBFG_ERR_ARG, "digest %u has no filters", i);
-        }
-        dig[i] = {(uint32_t)total, ds[i].bf_count};
-        total += ds[i].bf_count;
-    }
-    if (total >= (1ull << 32)) {
-        delete s;
-        return fail(c, SDBFG_ERR_ARG, "set too large");
-    }
-    std::vector<uint32_t> meta(total);
-    std::vector<uint8_t> filt(total * 256);
-    s->names.resize(n);
-    s->bf_count.resize(n);
-    s->last_elem.resize(n);
-    for (uint32_t i = 0; i < n; i++) {
-        const sdbfg_digest_desc& d = ds[i];
-        s->names[i] = d.name ? d.name : "";
-        s->bf_count[i] = d.bf_count;
-        memcpy(&filt[(uint64_t)dig[i].first * 256], d.filters, (uint64_t)d.bf_count * 256);
-        for (uint32_t f = 0; f < d.bf_count; f++) {
-            // get_elem_count (sdbf_class.cc:406-415)
-            uint32_t e = d.elem_counts ? d.elem_counts[f] : (f + 1 < d.bf_count ? d.max_elem : d.last_count);
-            uint32_t h = 0;
-            const uint8_t* p = d.filters + (uint64_t)f * 256;
-            for (int b = 0; b < 256; b += 8) {
-                uint64_t w;
-                memcpy(&w, p + b, 8);
-                h += (uint32_t)__builtin_popcountll(w);
-            }
-            meta[dig[i].first + f] = (h << 16) | (e & 0xFFFFu);
-            if (f + 1 == d.bf_count) s->last_elem[i] = e;
-        }
-    }
-    if (s->d_filters.ensure(std::max<uint64_t>(1, total) * 256) || s->d_meta.ensure(std::max<uint64_t>(1, total) * 4) ||
-        s->d_digests.ensure(std::max<uint32_t>(1, n) * sizeof(CmpDigest))) {
-        s->d_filters.release();
-        s->d_meta.release();
-        s->d_digests.release();
-        delete s;
-        return fail(c, SDBFG_ERR_NOMEM, "set upload: out of device memory");
-    }
-    cudaMemcpy(s->d_filters.p, filt.data(), total * 256, cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_meta.p, meta.data(), total * 4, cudaMemcpyHostToDevice);
-    cudaMemcpy(s->d_digests.p, dig.data(), n * sizeof(CmpDigest), cudaMemcpyHostToDevice);
-    *out = s;
-    return SDBFG_OK;
-}
-
-extern "C" void sdbfg_set_free(sdbfg_set* s) {
-    if (!s) return;
-    cudaSetDevice(s->ctx->device);
-    s->d_filters.release();
-    s->d_meta.release();
-    s->d_digests.release();
-    delete s;
-}
-
-extern "C" uint32_t sdbfg_set_size(const sdbfg_set* s) { return s ? s->n : 0; }
-
-// Orientation of a pair: sdbf_score's swap rule (sdbf_core.cc:351-359).
-static CmpPair orient(const sdbfg_set* a, uint32_t i, const sdbfg_set* b, uint32_t j) {
-    const uint32_t n1 = a->bf_count[i], n2 = b->bf_count[j];
-    const bool swap = n1 > n2 || (n1 == n2 && (a->last_elem[i] > b->last_elem[j] ||
-                                               strcmp(a->names[i].c_str(), b->names[j].c_str()) > 0));
-    if (swap) return CmpPair{j, i, n2, 1u | 0u};  // ref from b (side 1), tgt from a (side 0)
-    return CmpPair{i, j, n1, 2u};                  // ref from a (side 0), tgt from b (side 1)
-}
-
-static int run_pairs(sdbfg_ctx* c, const sdbfg_set* a, const sdbfg_set* b, const std::vector<CmpPair>& pairs,
-                     int32_t* out) {
-    cudaStream_t st = c->stream;
-    CUDA_TRY(c, c->d_pairs.ensure(std::max<size_t>(1, pairs.size()) * sizeof(CmpPair)));
-    CUDA_TRY(c, c->d_scores.ensure(std::max<size_t>(1, pairs.size()) * 4));
-    CUDA_TRY(c, cudaMemcpyAsync(c->d_pairs.p, pairs.data(), pairs.size() * sizeof(CmpPair), cudaMemcpyHostToDevice,
-                                st));
-    CmpParams P{};
-    P.filters[0] = a->d_filters.as<uint32_t>();
-    P.meta[0] = a->d_meta.as<uint32_t>();
-    P.digests[0] = a->d_digests.as<CmpDigest>();
-    P.filters[1] = b->d_filters.as<uint32_t>();
-    P.meta[1] = b->d_meta.as<uint32_t>();
-    P.digests[1] = b->d_digests.as<CmpDigest>();
-    P.pairs = c->d_pairs.as<CmpPair>();
-    P.npairs = pairs.size();
-    P.scores = c->d_scores.as<int32_t>();
-    P.cutoffs = c->d_cut.as<uint16_t>();
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(pairs.size(), (uint64_t)c->sms * 16);
-    TIMED_LAUNCH(c, "k_compare_pairs", launch_compare_pairs(P, std::max(1u, grid), st));
-    CUDA_TRY(c, cudaMemcpyAsync(out, c->d_scores.p, pairs.size() * 4, cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(c, cudaStreamSynchronize(st));
-    return SDBFG_OK;
-}
-
-extern "C" int sdbfg_score_pairs(sdbfg_ctx* c, const sdbfg_set* a, const sdbfg_set* b, const uint32_t* ia,
-                                 const uint32_t* ib, uint64_t npairs, int32_t* out) {
-    if (!c || !a || !b || (npairs && (!ia || !ib || !out))) return SDBFG_ERR_ARG;
-    CUDA_TRY(c, cudaSetDevice(c->device));
-    for (uint64_t base = 0; base < npairs; base += kPairsPerLaunch) {
-        const uint64_t m = std::min<uint64_t>(kPairsPerLaunch, npairs - base);
-        std::vector<CmpPair> pairs(m);
-        for (uint64_t k = 0; k < m; k++) {
-            const uint32_t i = ia[base + k], j = ib[base + k];
-            if (i >= a->n || j >= b->n) return fail(c, SDBFG_ERR_ARG, "pair %llu out of range", (unsigned long long)k);
-            pairs[k] = orient(a, i, b, j);
-        }
-        int rc = run_pairs(c, a, b, pairs, out + base);
-        if (rc) return rc;
-    }
-    return SDBFG_OK;
-}
-
-extern "C" int sdbfg_compare_all(sdbfg_ctx* c, const sdbfg_set* s, int32_t* out) {
-    if (!c || !s || !out) return SDBFG_ERR_ARG;
-    CUDA_TRY(c, cudaSetDevice(c->device));
-    std::vector<CmpPair> pairs;
-    uint64_t done = 0;
-    for (uint32_t i = 0; i < s->n; i++) {
-        for (uint32_t j = i + 1; j < s->n; j++) {
-            pairs.push_back(orient(s, i, s, j));
-            if (pairs.size() == kPairsPerLaunch) {
-                int rc = run_pairs(c, s, s, pairs, out + done);
-                if (rc) return rc;
-                done += pairs.size();
-                pairs.clear();
-            }
-        }
-    }
-    if (!pairs.empty()) return run_pairs(c, s, s, pairs, out + done);
-    return SDBFG_OK;
-}
-
-extern "C" int sdbfg_compare_to(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_set* t, int32_t* out) {
-    if (!c || !q || !t || !out) return SDBFG_ERR_ARG;
-    CUDA_TRY(c, cudaSetDevice(c->device));
-    std::vector<CmpPair> pairs;
-    uint64_t done = 0;
-    for (uint32_t i = 0; i < q->n; i++) {
-        for (uint32_t j = 0; j < t->n; j++) {
-            pairs.push_back(orient(q, i, t, j));
-            if (pairs.size() == kPairsPerLaunch) {
-                int rc = run_pairs(c, q, t, pairs, out + done);
-                if (rc) return rc;
-                done += pairs.size();
-                pairs.clear();
-            }
-        }
-    }
-    if (!pairs.empty()) return run_pairs(c, q, t, pairs, out + done);
-    return SDBFG_OK;
-}

@@ -1,0 +1,97 @@
+"""Batched comparison engine (persistent work units, kernel variants, unit
+budgets, split pairs, CUDA-graph replay, autotuner) against the oracle.
+Integer-identical scores for every variant and schedule."""
+import numpy as np
+import pytest
+
+from sdhash_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def uneven(ctx, oracle):
+    """Digests with very uneven filter counts (1..~260), stream and block
+    mode, related pairs (partners) so that scores are non-trivial, sparse
+    last filters, equal filter counts and equal names for the swap rule's
+    tie-breaks."""
+    sizes = [int(s) for s in synth.log_uniform_sizes(41, 36, 600, 3 << 20)]
+    files = [synth.mixture_bytes(41, i, s) for i, s in enumerate(sizes)]
+    files += [synth.partner(41, i, files[i]) for i in range(0, 12)]
+    files += [files[3].copy(), files[3].copy()]          # identical digests
+    names = [f"u{i:03d}" for i in range(len(files))]
+    names[-1] = names[-2]                               # identical names
+    ds = ctx.digest_buffers([f.tobytes() for f in files], names, 0)
+    ds += ctx.digest_buffers([f.tobytes() for f in files[:10]], [n + ".dd" for n in names[:10]], 4096)
+    ds = [d for d in ds if d is not None]
+    ods = [oracle.parse(d.to_string()) for d in ds]
+    want_all = oracle.score_all_matrix(ods)
+    iu = np.triu_indices(len(ds), 1)
+    return ds, ods, want_all[iu]
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("unit_work", [1 << 12, 1 << 22])
+def test_all_pairs_every_variant_and_budget(ctx, uneven, variant, unit_work):
+    ds, ods, want = uneven
+    ctx.set_compare_tuning(variant, unit_work, graphs=(variant % 2 == 0))
+    try:
+        dev = ctx.upload(ds)
+        got = ctx.compare_all(dev)
+    finally:
+        ctx.set_compare_tuning(0, 1 << 22, True)
+    assert np.array_equal(got, want)
+    assert (want > 0).sum() > 20  # related pairs present
+
+
+def test_cross_with_split_pairs(ctx, oracle, uneven):
+    """A unit budget below single-pair sizes row-splits pairs; the maxima go
+    through the slot array and the finalize kernel."""
+    ds, ods, _ = uneven
+    q, t = ds[::3], ds[1::2]
+    want = oracle.score_cross_matrix([ods[i] for i in range(0, len(ds), 3)], [ods[i] for i in range(1, len(ds), 2)])
+    ctx.set_compare_tuning(3, 1 << 10, True)
+    try:
+        got = ctx.compare_to(ctx.upload(q), ctx.upload(t))
+    finally:
+        ctx.set_compare_tuning(0, 1 << 22, True)
+    assert np.array_equal(got, want)
+
+
+def test_graph_replay_and_device_output(ctx, uneven):
+    import torch
+    ds, ods, want = uneven
+    dev = ctx.upload(ds)
+    n = len(ds)
+    out = torch.full((n * (n - 1) // 2,), -7, dtype=torch.int32, device="cuda")
+    l0 = ctx.launch_count
+    ctx.compare_all_device(dev, out.data_ptr())
+    ctx.synchronize()
+    first = out.cpu().numpy().copy()
+    out.fill_(-7)
+    ctx.compare_all_device(dev, out.data_ptr())   # replays the captured graph
+    ctx.synchronize()
+    assert np.array_equal(first, want)
+    assert np.array_equal(out.cpu().numpy(), want)
+    assert ctx.launch_count - l0 >= 2
+    assert ctx.filter_pairs(dev) == sum(a.bf_count * b.bf_count for i, a in enumerate(ds) for b in ds[i + 1:])
+
+
+def test_autotuner_keeps_results(ctx, uneven):
+    ds, ods, want = uneven
+    dev = ctx.upload(ds)
+    v, w, rate = ctx.autotune_compare(dev, sample_pairs=1 << 20)
+    try:
+        assert 0 <= v < 5 and w in (1 << 20, 1 << 22, 1 << 24) and rate > 0
+        assert ctx.compare_tuning() == (v, w)
+        assert np.array_equal(ctx.compare_all(dev), want)
+    finally:
+        ctx.set_compare_tuning(0, 1 << 22, True)
+
+
+def test_plain_per_pair_path_agrees(ctx, uneven):
+    ds, ods, want = uneven
+    dev = ctx.upload(ds)
+    iu = np.triu_indices(len(ds), 1)
+    got = ctx.score_pairs(dev, dev, iu[0], iu[1])
+    assert np.array_equal(got, want)
