@@ -386,6 +386,7 @@ static int enqueue_plan(sdbfg_ctx* c, const MatPlan* p, const MatParams& P, cuda
 static int run_plan(sdbfg_ctx* c, MatPlan* p, const sdbfg_set* a, const sdbfg_set* b, int32_t* dev_scores) {
     cudaStream_t st = c->stream;
     const MatParams P = plan_params(c, p, a, b, dev_scores);
+    matrix_ctas_per_sm(p->variant);  // sets the kernel's attributes outside any capture
     if (!c->mat_graphs || c->profile) return enqueue_plan(c, p, P, st);
     if (p->graph && p->graph_out == dev_scores) {
         CUDA_TRY(c, cudaGraphLaunch(p->graph, st));

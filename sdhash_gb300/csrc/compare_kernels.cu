@@ -458,14 +458,10 @@ __global__ void k_matrix_finalize(MatParams P) {
     P.scores[out_index(P, rs != 0, sp.ref, sp.tgt)] = final_score(sum, A.nfilters, sparse);
 }
 
+// The dynamic shared-memory attribute is set by matrix_ctas_per_sm, which
+// callers run before the first launch (and before any stream capture).
 template <int R, int TJ>
 static cudaError_t launch_variant(const MatParams& P, uint32_t grid, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_matrix<R, TJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(MatSmem<R, TJ>));
-        attr = true;
-    }
     k_matrix<R, TJ><<<grid, R, sizeof(MatSmem<R, TJ>), st>>>(P);
     return cudaGetLastError();
 }
@@ -496,14 +492,19 @@ static int occupancy() {
 }
 
 int matrix_ctas_per_sm(int variant) {
+    static int cached[kMatVariants] = {0, 0, 0, 0, 0};
+    if (variant >= 0 && variant < kMatVariants && cached[variant]) return cached[variant];
+    int n = 1;
     switch (variant) {
-        case 0: return occupancy<128, 32>();
-        case 1: return occupancy<128, 16>();
-        case 2: return occupancy<128, 64>();
-        case 3: return occupancy<64, 32>();
-        case 4: return occupancy<256, 32>();
+        case 0: n = occupancy<128, 32>(); break;
+        case 1: n = occupancy<128, 16>(); break;
+        case 2: n = occupancy<128, 64>(); break;
+        case 3: n = occupancy<64, 32>(); break;
+        case 4: n = occupancy<256, 32>(); break;
+        default: return 1;
     }
-    return 1;
+    cached[variant] = n;
+    return n;
 }
 
 }  // namespace sdbfg
