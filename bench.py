@@ -60,6 +60,13 @@ def parse():
     ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
     ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs"],
+                    help="stream: bulk digest generation (headline); allpairs: batched uneven all-pairs compare")
+    ap.add_argument("--digests", type=int, default=20000, help="allpairs: digests in the set")
+    ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
+    ap.add_argument("--pool-gib", type=float, default=4.0, help="allpairs: mixture content digested for the filter pool")
+    ap.add_argument("--plain-pairs", type=int, default=400, help="allpairs: pairs timed one call each")
+    ap.add_argument("--cpu-pairs", type=int, default=256, help="allpairs: pairs timed on the host (oracle)")
     return ap.parse_args()
 
 
@@ -250,8 +257,155 @@ def run_reference(args):
     return 0
 
 
+# ----------------------------------------------------------------- allpairs
+AP_METRIC = "filter-pair compares/s (batched all-pairs)"
+AP_UNIT = "filter pairs/s"
+
+
+def allpairs_digests(args, ctx):
+    """20,000 stream digests with filter counts log-uniform over 1..2000.
+
+    Filters come from a pool of mixture content digested on the GPU (stream
+    mode, element counts from generation).  Digest i takes a random run of
+    n_i consecutive pool filters, each rotated by a per-digest byte offset so
+    that digests whose runs overlap do not share identical filters; the
+    rotation keeps every filter's popcount and element count."""
+    import sdhash_gb300 as g
+    from sdhash_gb300 import synth
+    rng = np.random.default_rng(args.seed + 1000)
+    counts = np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(args.max_filters + 1), args.digests))), 1,
+                     args.max_filters).astype(np.int64)
+    nfile = max(1, int(args.pool_gib * 64))
+    sizes = np.full(nfile, 16 << 20, dtype=np.uint64)
+    data, offs, lens = synth.fill_many(args.seed + 1001, "mixture", sizes)
+    pool = ctx.digest_packed(data, offs, lens, 0)
+    del data
+    pf = np.concatenate([d.filters.reshape(-1, 256) for d in pool])
+    pe = np.concatenate([np.r_[np.full(d.bf_count - 1, 160, np.uint16), np.uint16(d.last_count)] for d in pool])
+    P = len(pf)
+    assert P >= args.max_filters
+    F = np.empty((int(counts.sum()), 256), dtype=np.uint8)
+    E = np.empty(int(counts.sum()), dtype=np.uint16)
+    starts = rng.integers(0, P - counts + 1)
+    rots = rng.integers(0, 256, args.digests)
+    digs, o = [], 0
+    for i, (n, st, r) in enumerate(zip(counts, starts, rots)):
+        n, st = int(n), int(st)
+        F[o:o + n] = np.roll(pf[st:st + n], int(r), axis=1)
+        E[o:o + n] = pe[st:st + n]
+        digs.append(g.Digest(f"d{i:05d}", 0, n, int(E[o + n - 1]), 160, 0, F[o:o + n], E[o:o + n]))
+        o += n
+    return digs, counts, P
+
+
+def main_allpairs(args):
+    import torch
+    import sdhash_gb300 as g
+    torch.cuda.set_device(0)
+    ctx = g.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    digs, counts, pool_filters = allpairs_digests(args, ctx)
+    t_build = time.perf_counter() - t0
+    n = len(digs)
+    npairs = n * (n - 1) // 2
+    dev = ctx.upload(digs)
+    fpairs = ctx.filter_pairs(dev)
+    out = torch.empty(npairs, dtype=torch.int32, device="cuda")
+    # autotuner on a sample of the job's units (also the warm-up)
+    t0 = time.perf_counter()
+    variant, unit_work, tuned_rate = ctx.autotune_compare(dev, sample_pairs=1 << 35)
+    t_tune = time.perf_counter() - t0
+    for _ in range(args.warmup):  # a capture-and-replay run of the full job
+        ctx.compare_all_device(dev, out.data_ptr())
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = ctx.launch_count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.compare_all_device(dev, out.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks.stop()
+    launches = ctx.launch_count - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    value = fpairs / (ms / 1e3)
+    scores = out.cpu().numpy()
+
+    # plain per-call GPU path: one sdbf::compare-style call (one launch, one
+    # pair, result read back) per pair, on random pairs of the same set
+    rng = np.random.default_rng(5)
+    pi = rng.integers(0, n, 4 * args.plain_pairs)
+    pj = rng.integers(0, n, 4 * args.plain_pairs)
+    keep = pi != pj
+    pi, pj = np.minimum(pi, pj)[keep][: args.plain_pairs], np.maximum(pi, pj)[keep][: args.plain_pairs]
+    ctx.score_pairs(dev, dev, pi[:4], pj[:4])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_scores = [int(ctx.score_pairs(dev, dev, [int(a)], [int(b)])[0]) for a, b in zip(pi, pj)]
+    t_plain = time.perf_counter() - t0
+    plain_work = int(sum(int(counts[a]) * int(counts[b]) for a, b in zip(pi, pj)))
+    idx = pi * (2 * n - pi - 1) // 2 + (pj - pi - 1)
+    assert plain_scores == [int(x) for x in scores[idx]], "per-call and batched scores differ"
+    plain_rate = plain_work / t_plain
+
+    # CPU reference path (oracle port, all host threads) on random pairs
+    from oracle import Oracle
+    O = Oracle()
+    ci, cj = pi[: args.cpu_pairs], pj[: args.cpu_pairs]
+    used = sorted(set(ci.tolist()) | set(cj.tolist()))
+    loc = {d: k for k, d in enumerate(used)}
+    ods = [O.parse(digs[d].to_string()) for d in used]
+    nt = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cpu_scores = O.score_pairs(ods, [loc[int(a)] for a in ci], [loc[int(b)] for b in cj], nt)
+    t_cpu = time.perf_counter() - t0
+    assert [int(x) for x in cpu_scores] == [int(x) for x in scores[idx[: len(ci)]]], "oracle and GPU scores differ"
+    cpu_work = int(sum(int(counts[a]) * int(counts[b]) for a, b in zip(ci, cj)))
+
+    e2e = None
+    if not args.no_e2e:
+        # public host API: upload the set (H2D), all pairs, scores back (D2H)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = ctx.upload(digs)
+        host_scores = ctx.compare_all(s2)
+        s2.close()
+        t_e2e = time.perf_counter() - t0
+        assert np.array_equal(host_scores, scores)
+        e2e = {"value": fpairs / t_e2e, "unit": AP_UNIT, "h2d_bytes_per_step": int(counts.sum()) * 256,
+               "d2h_bytes_per_step": int(npairs) * 4, "ms_per_step": t_e2e * 1e3}
+    line = {"metric": AP_METRIC, "value": value, "unit": AP_UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32 (2048-bit Bloom filters, integer scores)", "data": "synthetic",
+            "config": {"workload": "batched uneven all-pairs compare", "digests": n, "pairs": npairs,
+                       "filters_per_digest": f"log-uniform 1..{args.max_filters}", "filters": int(counts.sum()),
+                       "filter_pairs_per_step": fpairs, "threshold": 1,
+                       "filter_source": f"{pool_filters} stream filters of {args.pool_gib:g} GiB mixture content",
+                       "variant": variant, "unit_work": unit_work, "autotune_s": round(t_tune, 2),
+                       "autotune_sample_rate": tuned_rate, "build_s": round(t_build, 1),
+                       "l2": "filters 5x larger than L2"},
+            "gpu_launches": launches, "clocks": clocks.summary(),
+            "plain_per_call": {"value": plain_rate, "unit": AP_UNIT, "pairs": len(pi), "filter_pairs": plain_work,
+                               "seconds": round(t_plain, 3),
+                               "path": "sdbfg_score_pairs with one pair per call (one launch + sync each)"},
+            "batched_over_plain": value / plain_rate,
+            "e2e": e2e,
+            "cpu_baseline": {"value": cpu_work / t_cpu, "unit": AP_UNIT, "cores": nt, "kind": "port",
+                             "sample": f"{len(ci)} random pairs ({cpu_work} filter pairs)",
+                             "seconds": round(t_cpu, 3)},
+            "scores_ge_1": int((scores >= 1).sum())}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "allpairs":
+        return main_allpairs(args)
     if args.impl == "reference":
         return run_reference(args)
     rank, world, local = dist_setup(args.gpus)

@@ -211,6 +211,17 @@ class Oracle:
                                       out.ctypes.data_as(C.POINTER(C.c_int32)), nthreads)
         return out
 
+    def score_pairs(self, ds, pi, pj, nthreads: int = 0):
+        """Scores of pairs (ds[pi[k]], ds[pj[k]]) as sdbf_score(ds[pi], ds[pj]), multithreaded."""
+        import numpy as np
+        pi = np.ascontiguousarray(pi, dtype=np.uint32)
+        pj = np.ascontiguousarray(pj, dtype=np.uint32)
+        out = np.zeros(max(1, len(pi)), dtype=np.int32)
+        self.L.orc_score_pairs(self._array(ds), pi.ctypes.data_as(C.POINTER(C.c_uint32)),
+                               pj.ctypes.data_as(C.POINTER(C.c_uint32)), len(pi),
+                               out.ctypes.data_as(C.POINTER(C.c_int32)), nthreads)
+        return out[: len(pi)]
+
     def digest_many(self, bufs, dd_block_size: int = 0, nthreads: int = 0, names=None):
         """Digest a list of bytes-like buffers on nthreads threads (file-parallel)."""
         n = len(bufs)
