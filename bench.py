@@ -60,8 +60,11 @@ def parse():
     ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
     ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs"],
-                    help="stream: bulk digest generation (headline); allpairs: batched uneven all-pairs compare")
+    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image"],
+                    help="stream: bulk digest generation (headline); allpairs: batched uneven all-pairs compare; "
+                         "image: block-mode disk image + query fragments compared against it")
+    ap.add_argument("--image-gib", type=int, default=16, help="image: disk image size (GiB, multiple of 128 MiB)")
+    ap.add_argument("--queries", type=int, default=100000, help="image: query fragments")
     ap.add_argument("--digests", type=int, default=20000, help="allpairs: digests in the set")
     ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
     ap.add_argument("--pool-gib", type=float, default=4.0, help="allpairs: mixture content digested for the filter pool")
@@ -402,8 +405,190 @@ def main_allpairs(args):
     return 0
 
 
+# -------------------------------------------------------------------- image
+IM_METRIC = "query-vs-image filter-pair compares/s"
+SEG = 128 << 20  # sdhash -b segments files above 128 MiB into 128 MiB digests
+
+
+def digests_from_device(g, res, names, lens, dd, out_dev, counts_dev):
+    filt = out_dev.cpu().numpy()
+    cnt = counts_dev.cpu().numpy() if counts_dev is not None else None
+    ds = []
+    for i in range(len(names)):
+        r = res[i]
+        if r.status != 0:
+            ds.append(None)
+            continue
+        o, k = int(r.filter_offset), int(r.bf_count)
+        f = filt[o * 256:(o + k) * 256].copy()
+        if dd:
+            ds.append(g.Digest(names[i], int(lens[i]), k, 0, 192, dd, f, cnt[o:o + k].copy()))
+        else:
+            ds.append(g.Digest(names[i], int(lens[i]), k, int(r.last_count), 160, 0, f, None))
+    return ds
+
+
+def timed(stream, fn, reps=1):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        r = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return r, e0.elapsed_time(e1) / reps
+
+
+def main_image(args):
+    """Block-mode image digest (-b 16, 128 MiB segments) and query-fragment
+    digests (stream mode), then every query against every image segment."""
+    import torch
+    import sdhash_gb300 as g
+    from sdhash_gb300 import synth
+    torch.cuda.set_device(0)
+    ctx = g.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    dd = 16384
+    nseg = args.image_gib * (1 << 30) // SEG
+    t0 = time.perf_counter()
+    image, ioffs, ilens = synth.fill_many(args.seed + 2000, "mixture", np.full(nseg, SEG, dtype=np.uint64))
+    t_synth = time.perf_counter() - t0
+    inames = [f"image.{k * SEG // (1 << 20):04d}M" for k in range(nseg)]
+    # ---- block-mode image digest, device resident
+    dimg = torch.from_numpy(image).cuda()
+    cap = ctx.capacity(ilens, dd)
+    iout = torch.empty(cap * 256, dtype=torch.uint8, device="cuda")
+    icnt = torch.empty(cap, dtype=torch.uint16, device="cuda")
+    run = lambda: ctx.digest_device(dimg.data_ptr(), ioffs, ilens, dd, iout.data_ptr(), cap, icnt.data_ptr())
+    for _ in range(args.warmup):
+        run()
+    ires, img_ms = timed(stream, run)
+    idigs = digests_from_device(g, ires, inames, ilens, dd, iout, icnt)
+    del dimg
+    # ---- query fragments: 60% cut from the image, 40% fresh random data
+    rng = np.random.default_rng(args.seed + 2001)
+    qsz = synth.log_uniform_sizes(args.seed + 2002, args.queries, 4096, 1 << 20)
+    cut = rng.random(args.queries) < 0.6
+    qoffs, qtot = synth.packed_layout(qsz)
+    qdata = np.empty(max(16, qtot), dtype=np.uint8)
+    src = rng.integers(0, len(image) - qsz.astype(np.int64))
+    fresh = np.nonzero(~cut)[0]
+    fr_data, fr_offs, _ = synth.fill_many(args.seed + 2003, "random", qsz[fresh])
+    for k, i in enumerate(fresh):
+        qdata[int(qoffs[i]):int(qoffs[i]) + int(qsz[i])] = fr_data[int(fr_offs[k]):int(fr_offs[k]) + int(qsz[i])]
+    del fr_data
+    for i in np.nonzero(cut)[0]:
+        qdata[int(qoffs[i]):int(qoffs[i]) + int(qsz[i])] = image[int(src[i]):int(src[i]) + int(qsz[i])]
+    qnames = [f"q{i:06d}" for i in range(args.queries)]
+    dq = torch.from_numpy(qdata).cuda()
+    qcap = ctx.capacity(qsz, 0)
+    qout = torch.empty(qcap * 256, dtype=torch.uint8, device="cuda")
+    runq = lambda: ctx.digest_device(dq.data_ptr(), qoffs, qsz, 0, qout.data_ptr(), qcap)
+    for _ in range(args.warmup):
+        runq()
+    qres, q_ms = timed(stream, runq)
+    qdigs = digests_from_device(g, qres, qnames, qsz, 0, qout, None)
+    del dq
+    # ---- parity spot checks against the oracle (sampled)
+    from oracle import Oracle
+    O = Oracle()
+    chk = [0, nseg - 1]
+    refs = O.digest_many([image[int(ioffs[k]):int(ioffs[k]) + SEG] for k in chk], dd, len(chk),
+                         names=[inames[k] for k in chk])
+    for k, ref in zip(chk, refs):
+        assert ref.to_string() == idigs[k].to_string(), inames[k]
+    for i in rng.choice(args.queries, 24, replace=False):
+        ref = O.digest(qnames[i], qdata[int(qoffs[i]):int(qoffs[i]) + int(qsz[i])].tobytes(), 0)
+        assert ref.to_string() == qdigs[i].to_string(), qnames[i]
+    # ---- comparison: every query x every segment
+    qset, iset = ctx.upload(qdigs), ctx.upload(idigs)
+    fpairs = ctx.filter_pairs(qset, iset)
+    scores_dev = torch.empty(args.queries * nseg, dtype=torch.int32, device="cuda")
+    t0 = time.perf_counter()
+    variant, unit_work, tuned = ctx.autotune_compare(qset, iset, sample_pairs=1 << 34)
+    t_tune = time.perf_counter() - t0
+    runc = lambda: ctx.compare_to_device(qset, iset, scores_dev.data_ptr())
+    for _ in range(max(1, args.warmup)):
+        runc()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = ctx.launch_count
+    _, cmp_ms = timed(stream, runc, args.steps)
+    launches = ctx.launch_count - l0
+    clocks.stop()
+    scores = scores_dev.cpu().numpy().reshape(args.queries, nseg)
+    best = scores.argmax(1)
+    seg_of = (src // SEG).astype(np.int64)
+    seg_end = ((src + qsz.astype(np.int64) - 1) // SEG).astype(np.int64)
+    found = cut & ((best == seg_of) | (best == seg_end)) & (scores.max(1) >= 1)
+    # e2e: host query buffer -> digests -> compare against the resident image set -> scores on the host
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    q2 = ctx.digest_packed(qdata, qoffs, qsz, 0, names=qnames)
+    qs2 = ctx.upload(q2)
+    host_scores = ctx.compare_to(qs2, iset)
+    t_e2e = time.perf_counter() - t0
+    assert np.array_equal(host_scores, scores)
+    qs2.close()
+    # plain per-call GPU path: one query per call against the resident image set
+    pick = rng.choice(args.queries, min(200, args.queries), replace=False)
+    ctx.compare_to(ctx.upload([qdigs[pick[0]]]), iset)
+    t0 = time.perf_counter()
+    for i in pick:
+        one = ctx.upload([qdigs[i]])
+        r = ctx.compare_to(one, iset)
+        one.close()
+        assert np.array_equal(r[0], scores[i])
+    t_plain = time.perf_counter() - t0
+    plain_work = int(sum(qdigs[i].bf_count for i in pick)) * sum(d.bf_count for d in idigs)
+    # CPU reference path on a sample (oracle, all host threads)
+    segs = list(range(0, nseg, max(1, nseg // 8)))
+    cq = pick[:16]
+    oq = [O.parse(qdigs[i].to_string()) for i in cq]
+    oi = [O.parse(idigs[k].to_string()) for k in segs]
+    nt = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cpu = O.score_cross_matrix(oq, oi, nt)
+    t_cpu = time.perf_counter() - t0
+    assert np.array_equal(cpu, scores[np.ix_(cq, segs)])
+    cpu_work = int(sum(qdigs[i].bf_count for i in cq)) * sum(idigs[k].bf_count for k in segs)
+    value = fpairs / (cmp_ms / 1e3)
+    line = {"metric": IM_METRIC, "value": value, "unit": AP_UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": cmp_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32 (2048-bit Bloom filters, integer scores)", "data": "synthetic",
+            "config": {"workload": "block-mode image vs query fragments", "image_bytes": int(ilens.sum()),
+                       "image_segments": nseg, "dd_block_size": dd, "image_filters": sum(d.bf_count for d in idigs),
+                       "queries": args.queries, "query_bytes": int(qsz.sum()),
+                       "query_filters": sum(d.bf_count for d in qdigs), "query_sizes": "log-uniform 4 KiB..1 MiB",
+                       "cut_from_image": int(cut.sum()), "filter_pairs_per_step": fpairs, "threshold": 1,
+                       "variant": variant, "unit_work": unit_work, "autotune_s": round(t_tune, 2),
+                       "synth_s": round(t_synth, 1)},
+            "image_digest": {"value": int(ilens.sum()) / (img_ms / 1e3) / 1e9, "unit": "GB/s", "ms": img_ms,
+                             "mode": "block (-b 16), device resident"},
+            "query_digest": {"value": int(qsz.sum()) / (q_ms / 1e3) / 1e9, "unit": "GB/s", "ms": q_ms,
+                             "mode": "stream, device resident"},
+            "top_match": {"cut_queries_best_segment_found": int(found.sum()), "cut_queries": int(cut.sum()),
+                          "queries_with_score_ge_1": int((scores.max(1) >= 1).sum())},
+            "gpu_launches": launches, "clocks": clocks.summary(),
+            "plain_per_call": {"value": plain_work / t_plain, "unit": AP_UNIT, "queries": len(pick),
+                               "seconds": round(t_plain, 3),
+                               "path": "one query per call: upload + compare_to + scores back"},
+            "batched_over_plain": value / (plain_work / t_plain),
+            "e2e": {"value": fpairs / t_e2e, "unit": AP_UNIT, "h2d_bytes_per_step": int(qsz.sum()),
+                    "d2h_bytes_per_step": int(args.queries) * nseg * 4, "ms_per_step": t_e2e * 1e3,
+                    "path": "host query bytes -> digests -> compare_to -> host scores"},
+            "cpu_baseline": {"value": cpu_work / t_cpu, "unit": AP_UNIT, "cores": nt, "kind": "port",
+                             "sample": f"{len(cq)} queries x {len(segs)} segments", "seconds": round(t_cpu, 3)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "image":
+        return main_image(args)
     if args.workload == "allpairs":
         return main_allpairs(args)
     if args.impl == "reference":

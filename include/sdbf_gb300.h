@@ -201,6 +201,49 @@ int sdbfg_ctx_get_compare_tuning(const sdbfg_ctx *ctx, int *variant, uint64_t *u
 int sdbfg_compare_autotune(sdbfg_ctx *ctx, const sdbfg_set *a, const sdbfg_set *b_or_null, uint64_t sample_pairs,
                            int *out_variant, uint64_t *out_unit_work, double *out_pairs_per_s);
 
+/* ------------------------------------------------------------- serving
+ * A serving loop over a device-resident target set (the resident form of
+ * sdhash's compare_to of query digests against a reference set,
+ * sdbf/sdbf_set.cc:318-346; no counterpart as a service in the reference).
+ * A worker thread admits queued query digests into batch slots (one CUDA
+ * stream each) as slots free up, in arrival order, while their filters fit
+ * the slot's share of memory_budget; every query is scored against every
+ * target exactly as sdbfg_compare_to would score it.  The context must not
+ * be used from other threads while its server runs; the target set must
+ * outlive the server. */
+typedef struct sdbfg_server sdbfg_server;
+typedef struct {
+    uint32_t slots;              /* batches in flight, 1..8 (default 3) */
+    uint32_t max_batch_queries;  /* queries per batch (default 256) */
+    uint64_t memory_budget;      /* device bytes for batches in flight (default 256 MiB) */
+    int32_t threshold;           /* a target matches at score >= threshold (default 1) */
+} sdbfg_server_config;
+typedef struct {
+    uint64_t tag;                /* as submitted */
+    int32_t status;              /* SDBFG_OK */
+    int32_t best_score;          /* highest score over the targets (-1: none) */
+    uint32_t best_target;        /* its index in the target set */
+    uint32_t matches;            /* targets with score >= threshold */
+    uint32_t batch_queries;      /* queries in the batch it was scored in */
+    uint32_t pad;
+    uint64_t submit_ns, start_ns, done_ns;  /* steady clock: queued, admitted, scores on the host */
+} sdbfg_server_result;
+/* cfg NULL: defaults. */
+int sdbfg_server_create(sdbfg_ctx *ctx, const sdbfg_set *targets, const sdbfg_server_config *cfg,
+                        sdbfg_server **out);
+/* Copies the query digest; thread-safe.  SDBFG_ERR_CAPACITY if the digest
+ * alone exceeds a slot's memory share. */
+int sdbfg_server_submit(sdbfg_server *srv, const sdbfg_digest_desc *query, uint64_t tag);
+/* Up to max finished queries, oldest first; scores (max * n_targets, may
+ * be NULL) receives each query's score row.  timeout_ms: 0 = do not wait,
+ * < 0 = wait for at least one. */
+int sdbfg_server_poll(sdbfg_server *srv, sdbfg_server_result *out, int32_t *scores, uint32_t max, uint32_t *n,
+                      int timeout_ms);
+int sdbfg_server_stats(const sdbfg_server *srv, uint64_t *pending, uint64_t *served, uint64_t *batches,
+                       uint64_t *launches);
+/* Finishes queued and running queries, then frees the server. */
+void sdbfg_server_destroy(sdbfg_server *srv);
+
 /* ------------------------------------------------------------ SDBF text */
 /* sdbf::to_string (sdbf/sdbf_class.cc:293-334): one SDBF v3 line with
  * trailing newline.  Writes at most cap bytes (NUL-terminated); returns the

@@ -43,6 +43,17 @@ class DigestResult(C.Structure):
                 ("reserved", C.c_uint32), ("filter_offset", C.c_uint64)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_uint32), ("max_batch_queries", C.c_uint32), ("memory_budget", C.c_uint64),
+                ("threshold", C.c_int32)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("status", C.c_int32), ("best_score", C.c_int32), ("best_target", C.c_uint32),
+                ("matches", C.c_uint32), ("batch_queries", C.c_uint32), ("pad", C.c_uint32),
+                ("submit_ns", C.c_uint64), ("start_ns", C.c_uint64), ("done_ns", C.c_uint64)]
+
+
 class DigestDesc(C.Structure):
     _fields_ = [("name", C.c_char_p), ("filters", C.c_void_p), ("elem_counts", C.c_void_p),
                 ("bf_count", C.c_uint32), ("last_count", C.c_uint32), ("max_elem", C.c_uint32),
@@ -98,6 +109,13 @@ def lib() -> C.CDLL:
         L.sdbfg_ctx_get_compare_tuning.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]
         L.sdbfg_compare_autotune.argtypes = [vp, vp, vp, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_uint64),
                                              C.POINTER(C.c_double)]
+        L.sdbfg_server_create.argtypes = [vp, vp, C.POINTER(ServerConfig), C.POINTER(vp)]
+        L.sdbfg_server_submit.argtypes = [vp, C.POINTER(DigestDesc), C.c_uint64]
+        L.sdbfg_server_poll.argtypes = [vp, C.POINTER(ServerResult), i32p, C.c_uint32, C.POINTER(C.c_uint32),
+                                        C.c_int]
+        L.sdbfg_server_stats.argtypes = [vp, u64p, u64p, u64p, u64p]
+        L.sdbfg_server_destroy.argtypes = [vp]
+        L.sdbfg_server_destroy.restype = None
         L.sdbfg_to_string.argtypes = [C.POINTER(DigestDesc), C.c_char_p, C.c_uint64]
         L.sdbfg_to_string.restype = C.c_int64
         L.sdbfg_parse.argtypes = [C.c_char_p, C.c_uint64, C.POINTER(DigestDesc), C.c_char_p, C.c_uint64, vp, vp]
@@ -381,6 +399,50 @@ class Context:
             self._check(lib().sdbfg_score_pairs(self.h, a.h, b.h, _ptr(ia, C.c_uint32), _ptr(ib, C.c_uint32),
                                                 len(ia), _ptr(out, C.c_int32)))
         return out[: len(ia)]
+
+
+class Server:
+    """Serving loop over a device-resident target set (sdbfg_server): submit
+    query digests from any thread, poll finished ones with their score rows."""
+
+    def __init__(self, ctx: "Context", targets: DeviceSet, slots: int = 3, max_batch_queries: int = 256,
+                 memory_budget: int = 256 << 20, threshold: int = 1):
+        self.ctx, self.targets = ctx, targets
+        cfg = ServerConfig(slots, max_batch_queries, memory_budget, threshold)
+        h = C.c_void_p()
+        ctx._check(lib().sdbfg_server_create(ctx.h, targets.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.nt = len(targets)
+
+    def submit(self, d: "Digest", tag: int):
+        keep: list = []
+        desc = d._desc(keep)
+        self.ctx._check(lib().sdbfg_server_submit(self.h, C.byref(desc), tag))
+
+    def poll(self, max_results: int = 1024, timeout_ms: int = 0, scores: bool = True):
+        """List of (result, score row or None)."""
+        res = (ServerResult * max_results)()
+        sc = np.zeros(max_results * self.nt if scores else 1, dtype=np.int32)
+        n = C.c_uint32()
+        self.ctx._check(lib().sdbfg_server_poll(self.h, res, _ptr(sc, C.c_int32) if scores else None, max_results,
+                                                C.byref(n), timeout_ms))
+        return [(res[k], sc[k * self.nt:(k + 1) * self.nt].copy() if scores else None) for k in range(n.value)]
+
+    def stats(self) -> dict:
+        v = [C.c_uint64() for _ in range(4)]
+        self.ctx._check(lib().sdbfg_server_stats(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("pending", "served", "batches", "launches"), (x.value for x in v)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sdbfg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ----------------------------------------------------- reference object API

@@ -11,6 +11,7 @@
 #include <atomic>
 
 #include "ctx_internal.h"
+#include "matrix_plan.h"
 
 static std::atomic<uint64_t> g_set_serial{1};
 
@@ -158,59 +159,6 @@ static bool swaps(const sdbfg_set* a, uint32_t x, const sdbfg_set* b, uint32_t y
            (n1 == n2 && (a->last_elem[x] > b->last_elem[y] || strcmp(a->names[x].c_str(), b->names[y].c_str()) > 0));
 }
 
-namespace {
-
-// Accumulates the work units of one reference digest over a run of target
-// list entries, cutting a new unit when the work budget or the per-unit
-// target limit is reached, and row-splitting single pairs above the budget.
-struct UnitBuilder {
-    std::vector<MatUnit> units;
-    std::vector<uint64_t> work;  // per unit, for the largest-first order
-    std::vector<MatSplit> split;
-    uint64_t slots = 0;
-    uint64_t budget;
-    uint64_t filter_pairs = 0;
-    explicit UnitBuilder(uint64_t w) : budget(std::max<uint64_t>(w, 1)) {}
-
-    // targets [t0, t1) of list `tl`, nf(e) = filters of list entry e
-    template <class NF, class ID>
-    void add(uint32_t ref, uint32_t nref, uint32_t flags, uint32_t t0, uint32_t t1, NF nf, ID id) {
-        uint32_t start = t0;
-        uint64_t acc = 0;
-        auto flush = [&](uint32_t end) {
-            if (end > start) {
-                units.push_back(MatUnit{ref, 0, nref, start, end, flags, 0, 0});
-                work.push_back(acc + (uint64_t)(end - start) * nref * 4);
-            }
-            start = end;
-            acc = 0;
-        };
-        for (uint32_t e = t0; e < t1; e++) {
-            const uint64_t w = (uint64_t)nref * nf(e);
-            filter_pairs += w;
-            if (w > budget) {  // one pair larger than a unit: split the reference's rows
-                flush(e);
-                const uint32_t rows = (uint32_t)std::max<uint64_t>(128, budget / nf(e) / 128 * 128);
-                const uint32_t si = (uint32_t)split.size();
-                split.push_back(MatSplit{ref, id(e), flags & (kUnitRefSide1 | kUnitTgtSide1), 0, slots});
-                slots += nref;
-                for (uint32_t r = 0; r < nref; r += rows) {
-                    const uint32_t r1 = std::min(nref, r + rows);
-                    units.push_back(MatUnit{ref, r, r1, e, e + 1, flags | kUnitSplit, si, 0});
-                    work.push_back((uint64_t)(r1 - r) * nf(e));
-                }
-                start = e + 1;
-                continue;
-            }
-            if (e > start && (acc + w > budget || e - start >= kMatMaxTargets)) flush(e);
-            acc += w;
-        }
-        flush(t1);
-    }
-};
-
-}  // namespace
-
 static MatPlan* find_plan(sdbfg_ctx* c, uint64_t sa, uint64_t sb, uint32_t mode) {
     static uint64_t tick = 0;
     for (MatPlan* p : c->plans)
@@ -223,12 +171,7 @@ static MatPlan* find_plan(sdbfg_ctx* c, uint64_t sa, uint64_t sb, uint32_t mode)
 }
 
 static int upload_plan(sdbfg_ctx* c, MatPlan* p, UnitBuilder& ub, const std::vector<uint32_t>& targets) {
-    // largest units first (LPT order for the persistent CTAs)
-    std::vector<uint32_t> order(ub.units.size());
-    std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return ub.work[x] > ub.work[y]; });
-    std::vector<MatUnit> units(ub.units.size());
-    for (size_t k = 0; k < order.size(); k++) units[k] = ub.units[order[k]];
+    const std::vector<MatUnit> units = ub.sorted_units();
     p->nunits = (uint32_t)units.size();
     p->nsplit = (uint32_t)ub.split.size();
     p->filter_pairs = ub.filter_pairs;
@@ -261,7 +204,13 @@ static int build_plan_all(sdbfg_ctx* c, const sdbfg_set* s, MatPlan* p) {
     std::stable_sort(sorted.begin(), sorted.end(),
                      [&](uint32_t x, uint32_t y) { return s->bf_count[x] < s->bf_count[y]; });
     std::vector<uint32_t> targets(sorted);
-    UnitBuilder ub(c->mat_unit_work);
+    uint64_t sum = 0, sum2 = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        sum += s->bf_count[i];
+        sum2 += (uint64_t)s->bf_count[i] * s->bf_count[i];
+    }
+    const uint64_t ctas = (uint64_t)c->sms * matrix_ctas_per_sm(c->mat_variant);
+    UnitBuilder ub(effective_unit_budget(c->mat_unit_work, (sum * sum - sum2) / 2, ctas));
     const auto nf = [&](uint32_t e) { return s->bf_count[targets[e]]; };
     const auto id = [&](uint32_t e) { return targets[e]; };
     uint32_t g0 = 0;
@@ -308,7 +257,8 @@ static int build_plan_cross(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_set* t
             if (swaps(q, i, t, j)) targets[off_q[q->n] + fill_t[j]++] = i;
             else targets[fill_q[i]++] = j;
         }
-    UnitBuilder ub(c->mat_unit_work);
+    const uint64_t ctas = (uint64_t)c->sms * matrix_ctas_per_sm(c->mat_variant);
+    UnitBuilder ub(effective_unit_budget(c->mat_unit_work, (uint64_t)q->total_filters * t->total_filters, ctas));
     const auto id = [&](uint32_t e) { return targets[e]; };
     const auto nf_t = [&](uint32_t e) { return t->bf_count[targets[e]]; };
     const auto nf_q = [&](uint32_t e) { return q->bf_count[targets[e]]; };
