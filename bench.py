@@ -60,11 +60,14 @@ def parse():
     ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
     ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image"],
+    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve"],
                     help="stream: bulk digest generation (headline); allpairs: batched uneven all-pairs compare; "
                          "image: block-mode disk image + query fragments compared against it")
     ap.add_argument("--image-gib", type=int, default=16, help="image: disk image size (GiB, multiple of 128 MiB)")
     ap.add_argument("--queries", type=int, default=100000, help="image: query fragments")
+    ap.add_argument("--ref-filters", type=int, default=2_000_000, help="serve: block filters in the reference set")
+    ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered Poisson load (queries/s)")
+    ap.add_argument("--serve-queries", type=int, default=1500, help="serve: queries per load run")
     ap.add_argument("--digests", type=int, default=20000, help="allpairs: digests in the set")
     ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
     ap.add_argument("--pool-gib", type=float, default=4.0, help="allpairs: mixture content digested for the filter pool")
@@ -585,8 +588,197 @@ def main_image(args):
     return 0
 
 
+# -------------------------------------------------------------------- serve
+SV_METRIC = "served queries/s (p50/p99 latency)"
+
+
+def serve_reference_set(args, ctx, stream, pool_queries):
+    """Reference set: a disk image of `ref_filters` 16 KiB blocks digested in
+    block mode (-b 16) in 128 MiB segments, generated and digested a few GiB
+    at a time.  Query digests: 60% cut from the image, 40% fresh random data,
+    sizes log-uniform 4 KiB..48 MiB (1..~4096 filters)."""
+    import torch
+    import sdhash_gb300 as g
+    from sdhash_gb300 import synth
+    dd = 16384
+    total = args.ref_filters * dd
+    seg_sizes = [SEG] * (total // SEG) + ([total % SEG] if total % SEG else [])
+    names = [f"image.{k * SEG // (1 << 20):04d}M" for k in range(len(seg_sizes))]
+    rng = np.random.default_rng(args.seed + 3000)
+    qsz = synth.log_uniform_sizes(args.seed + 3001, pool_queries, 4096, 48 << 20)
+    cut = rng.random(pool_queries) < 0.6
+    qbufs = [None] * pool_queries
+    digs = []
+    per = 16  # segments per group (2 GiB)
+    for g0 in range(0, len(seg_sizes), per):
+        sz = np.array(seg_sizes[g0:g0 + per], dtype=np.uint64)
+        data, offs, lens = synth.fill_many(args.seed + 3100 + g0, "mixture", sz)
+        dimg = torch.from_numpy(data).cuda()
+        cap = ctx.capacity(lens, dd)
+        out = torch.empty(cap * 256, dtype=torch.uint8, device="cuda")
+        cnt = torch.empty(cap, dtype=torch.uint16, device="cuda")
+        res = ctx.digest_device(dimg.data_ptr(), offs, lens, dd, out.data_ptr(), cap, cnt.data_ptr())
+        digs += digests_from_device(g, res, names[g0:g0 + per], lens, dd, out, cnt)
+        for i in np.nonzero(cut)[0]:   # queries cut from this part of the image
+            if qbufs[i] is None and rng.random() < per / len(seg_sizes) * 1.5 and int(qsz[i]) < len(data):
+                o = int(rng.integers(0, len(data) - int(qsz[i])))
+                qbufs[i] = data[o:o + int(qsz[i])].copy()
+        del dimg, data
+    for i in range(pool_queries):
+        if qbufs[i] is None:
+            qbufs[i] = synth.random_bytes(args.seed + 3002, i, int(qsz[i]))
+    qnames = [f"q{i:05d}" for i in range(pool_queries)]
+    queries = []
+    for k in range(0, pool_queries, 64):
+        queries += ctx.digest_buffers([b.tobytes() for b in qbufs[k:k + 64]], qnames[k:k + 64], 0)
+    return digs, [q for q in queries if q is not None], cut
+
+
+def poisson_run(srv, pool, rate, n, seed):
+    """Submit n queries (cycling over the pool) at Poisson arrival times from
+    a feeder thread; collect every result.  Returns (results, wall seconds)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n)
+    order = rng.integers(0, len(pool), n)
+    got = {}
+    done = threading.Event()
+
+    def feed():
+        t0 = time.perf_counter()
+        at = 0.0
+        for k in range(n):
+            at += gaps[k]
+            while True:
+                d = at - (time.perf_counter() - t0)
+                if d <= 0:
+                    break
+                time.sleep(min(d, 0.0005) if d > 0.0002 else 0)
+            srv.submit(pool[int(order[k])], k)
+        done.set()
+
+    th = threading.Thread(target=feed)
+    t0 = time.perf_counter()
+    th.start()
+    while len(got) < n:
+        for r, row in srv.poll(256, timeout_ms=20, scores=False):
+            got[int(r.tag)] = (int(r.submit_ns), int(r.start_ns), int(r.done_ns), int(r.batch_queries),
+                               int(r.best_score), int(r.matches))
+    th.join()
+    return got, order, time.perf_counter() - t0
+
+
+def lat_summary(got):
+    lat = np.array([(v[2] - v[0]) / 1e6 for v in got.values()])
+    first = min(v[0] for v in got.values())
+    last = max(v[2] for v in got.values())
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "throughput_qps": len(got) / ((last - first) / 1e9),
+            "mean_batch": float(np.mean([v[3] for v in got.values()]))}
+
+
+def main_serve(args):
+    import torch
+    import sdhash_gb300 as g
+    torch.cuda.set_device(0)
+    ctx = g.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    refs, pool, cut = serve_reference_set(args, ctx, stream, 600)
+    t_build = time.perf_counter() - t0
+    tset = ctx.upload(refs)
+    nt = len(refs)
+    ref_filters = sum(d.bf_count for d in refs)
+    qf = np.array([q.bf_count for q in pool])
+    # solo scores of every pool query (one batched compare_to): the served rows must equal them
+    solo = ctx.compare_to(ctx.upload(pool), tset)
+    srv = g.Server(ctx, tset, slots=3, max_batch_queries=64, memory_budget=1 << 30, threshold=1)
+    try:
+        warm, _, _ = poisson_run(srv, pool, args.rate, 64, seed=1)
+        clocks = ClockSampler(0)
+        clocks.start()
+        got_a, order_a, wall_a = poisson_run(srv, pool, args.rate, args.serve_queries, seed=2)
+        clocks.stop()
+        sa = lat_summary(got_a)
+        rate_b = 0.7 * sa["throughput_qps"]
+        got_b, order_b, wall_b = poisson_run(srv, pool, rate_b, max(200, args.serve_queries // 2), seed=3)
+        sb = lat_summary(got_b)
+        for k, v in list(got_a.items())[:200]:
+            q = int(order_a[k])
+            assert v[4] == solo[q].max() and v[5] == int((solo[q] >= 1).sum()), "served result differs"
+        stats = srv.stats()
+    finally:
+        srv.close()
+    # plain per-call GPU path: one query per call (upload, compare_to, scores back), one at a time;
+    # its latency under the same Poisson load follows from the FIFO recurrence on measured service times
+    rng = np.random.default_rng(4)
+    pick = rng.integers(0, len(pool), 200)
+    ctx.compare_to(ctx.upload([pool[0]]), tset)
+    svc = []
+    for q in pick:
+        t1 = time.perf_counter()
+        one = ctx.upload([pool[int(q)]])
+        row = ctx.compare_to(one, tset)
+        one.close()
+        svc.append(time.perf_counter() - t1)
+        assert np.array_equal(row[0], solo[int(q)])
+    svc = np.array(svc)
+    plain_qps = len(svc) / svc.sum()
+
+    def fifo(rate, seed):
+        r = np.random.default_rng(seed)
+        arr = np.cumsum(r.exponential(1.0 / rate, len(svc)))
+        fin, lat = 0.0, []
+        for a, s_ in zip(arr, svc):
+            fin = max(fin, a) + s_
+            lat.append((fin - a) * 1e3)
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+
+    # CPU reference path (oracle, all host threads): a few queries against the whole reference set
+    from oracle import Oracle
+    O = Oracle()
+    oref = [O.parse(d.to_string()) for d in refs]
+    cq = [int(q) for q in pick[:3]]
+    oq = [O.parse(pool[q].to_string()) for q in cq]
+    ncpu = os.cpu_count() or 1
+    t1 = time.perf_counter()
+    cpu = O.score_cross_matrix(oq, oref, ncpu)
+    t_cpu = time.perf_counter() - t1
+    assert np.array_equal(cpu, solo[cq])
+    line = {"metric": SV_METRIC, "value": sa["throughput_qps"], "unit": "queries/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": wall_a * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32 (2048-bit Bloom filters, integer scores)", "data": "synthetic",
+            "config": {"workload": "serving: Poisson query digests vs resident block-mode reference set",
+                       "ref_filters": ref_filters, "ref_segments": nt, "ref_bytes": ref_filters * 256,
+                       "query_pool": len(pool), "query_filters": f"{int(qf.min())}..{int(qf.max())} "
+                       f"(mean {qf.mean():.0f}, median {np.median(qf):.0f})", "offered_rate_qps": args.rate,
+                       "queries": args.serve_queries, "slots": 3, "max_batch_queries": 64, "memory_budget": 1 << 30,
+                       "threshold": 1, "build_s": round(t_build, 1)},
+            "latency_at_offered_rate": sa,
+            "latency_at_70pct_of_capacity": dict(sb, offered_rate_qps=rate_b),
+            "filter_pairs_per_s": float(qf[order_a].sum()) * ref_filters / (
+                (max(v[2] for v in got_a.values()) - min(v[0] for v in got_a.values())) / 1e9),
+            "server_stats": stats, "clocks": clocks.summary(), "gpu_launches": int(stats["launches"]),
+            "plain_per_call": {"value": plain_qps, "unit": "queries/s", "queries": len(svc),
+                               "mean_service_ms": float(svc.mean() * 1e3),
+                               "latency_at_70pct_of_served_capacity": fifo(rate_b, 5),
+                               "path": "one query per call: upload + compare_to + scores back"},
+            "served_over_plain": sa["throughput_qps"] / plain_qps,
+            "e2e": {"value": sa["throughput_qps"], "unit": "queries/s",
+                    "h2d_bytes_per_step": int(qf[order_a].sum()) * 256,
+                    "d2h_bytes_per_step": args.serve_queries * nt * 4,
+                    "path": "host query digests submitted -> score rows polled on the host"},
+            "cpu_baseline": {"value": len(cq) / t_cpu, "unit": "queries/s", "cores": ncpu, "kind": "port",
+                             "sample": f"{len(cq)} pool queries against all {nt} segments",
+                             "seconds": round(t_cpu, 3)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "serve":
+        return main_serve(args)
     if args.workload == "image":
         return main_image(args)
     if args.workload == "allpairs":
