@@ -309,7 +309,8 @@ def main_allpairs(args):
     import sdhash_gb300 as g
     torch.cuda.set_device(0)
     ctx = g.Context(0)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     t0 = time.perf_counter()
     digs, counts, pool_filters = allpairs_digests(args, ctx)
@@ -451,7 +452,8 @@ def main_image(args):
     from sdhash_gb300 import synth
     torch.cuda.set_device(0)
     ctx = g.Context(0)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     dd = 16384
     nseg = args.image_gib * (1 << 30) // SEG
@@ -510,7 +512,7 @@ def main_image(args):
     fpairs = ctx.filter_pairs(qset, iset)
     scores_dev = torch.empty(args.queries * nseg, dtype=torch.int32, device="cuda")
     t0 = time.perf_counter()
-    variant, unit_work, tuned = ctx.autotune_compare(qset, iset, sample_pairs=1 << 34)
+    variant, unit_work, tuned = ctx.autotune_compare(qset, iset, sample_pairs=1 << 33)
     t_tune = time.perf_counter() - t0
     runc = lambda: ctx.compare_to_device(qset, iset, scores_dev.data_ptr())
     for _ in range(max(1, args.warmup)):
@@ -681,7 +683,8 @@ def main_serve(args):
     import sdhash_gb300 as g
     torch.cuda.set_device(0)
     ctx = g.Context(0)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     t0 = time.perf_counter()
     refs, pool, cut = serve_reference_set(args, ctx, stream, 600)
@@ -792,7 +795,8 @@ def main():
     buf, data, offs, sizes, sizes_all = make_workload(args, rank, world, pinned=True)
     total_bytes = int(sizes.sum())
     ctx = g.Context(local)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     dev = torch.empty(max(16, len(data)), dtype=torch.uint8, device="cuda")
     dev.copy_(buf, non_blocking=True)

@@ -255,7 +255,14 @@ class Context:
             raise RuntimeError(f"sdbf_gb300 error {rc}: {lib().sdbfg_last_error(self.h).decode()}")
 
     def set_stream(self, stream_handle: int | None):
-        self._check(lib().sdbfg_ctx_set_stream(self.h, stream_handle or None))
+        """Launch on this CUDA stream (a torch.cuda.Stream's cuda_stream).  None:
+        the context's own stream; 0 (the legacy default stream) is passed as
+        cudaStreamLegacy so that it is not mistaken for None."""
+        if stream_handle is None:
+            h = None
+        else:
+            h = stream_handle if stream_handle != 0 else 1  # cudaStreamLegacy
+        self._check(lib().sdbfg_ctx_set_stream(self.h, h))
 
     def synchronize(self):
         self._check(lib().sdbfg_ctx_synchronize(self.h))

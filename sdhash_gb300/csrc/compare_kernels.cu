@@ -99,6 +99,53 @@ __device__ __forceinline__ uint32_t and_popc_hs(const uint32_t (&a)[64], const u
     return 16 * total16 + 8 * __popc(eights) + 4 * __popc(fours) + 2 * __popc(twos) + __popc(ones);
 }
 
+// Two independent carry-save trees: popcount(a & t0) and popcount(a & t1).
+// The two dependency chains interleave, which doubles the instruction-level
+// parallelism of the inner loop; a[] is read once for both.
+struct HsAcc {
+    uint32_t ones = 0, twos = 0, fours = 0, eights = 0, total16 = 0;
+    uint32_t foursA = 0, eightsA = 0;
+};
+
+__device__ __forceinline__ void hs_quad(HsAcc& h, uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3, int q) {
+    uint32_t twosA, twosB, fours_new;
+    MAT_CSA(twosA, h.ones, h.ones, x0, x1);
+    MAT_CSA(twosB, h.ones, h.ones, x2, x3);
+    MAT_CSA(fours_new, h.twos, h.twos, twosA, twosB);
+    if ((q & 1) == 0) {
+        h.foursA = fours_new;
+    } else {
+        uint32_t eights_new;
+        MAT_CSA(eights_new, h.fours, h.fours, h.foursA, fours_new);
+        if ((q & 3) == 1) {
+            h.eightsA = eights_new;
+        } else {
+            uint32_t sixteens;
+            MAT_CSA(sixteens, h.eights, h.eights, h.eightsA, eights_new);
+            h.total16 += __popc(sixteens);
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t hs_total(const HsAcc& h) {
+    return 16 * h.total16 + 8 * __popc(h.eights) + 4 * __popc(h.fours) + 2 * __popc(h.twos) + __popc(h.ones);
+}
+
+__device__ __forceinline__ void and_popc_hs2(const uint32_t (&a)[64], const uint32_t* t0, const uint32_t* t1,
+                                             uint32_t& c0, uint32_t& c1) {
+    const uint4* u0 = reinterpret_cast<const uint4*>(t0);
+    const uint4* u1 = reinterpret_cast<const uint4*>(t1);
+    HsAcc h0, h1;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const uint4 v0 = u0[q], v1 = u1[q];
+        hs_quad(h0, a[4 * q] & v0.x, a[4 * q + 1] & v0.y, a[4 * q + 2] & v0.z, a[4 * q + 3] & v0.w, q);
+        hs_quad(h1, a[4 * q] & v1.x, a[4 * q + 1] & v1.y, a[4 * q + 2] & v1.z, a[4 * q + 3] & v1.w, q);
+    }
+    c0 = hs_total(h0);
+    c1 = hs_total(h1);
+}
+
 // The reference's staged exits (bf_utils.cc:114-206) for a pair whose full
 // count is above the cut: true when an early stage would have returned 0.
 __device__ __forceinline__ bool staged_exit(const uint32_t (&a)[64], const uint32_t* t, uint32_t cut) {
@@ -276,7 +323,7 @@ struct MatSmem {
 };
 
 template <int R, int TJ>
-__global__ void __launch_bounds__(R) k_matrix(MatParams P) {
+__global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
     extern __shared__ __align__(16) uint8_t mat_smem[];
     MatSmem<R, TJ>& S = *reinterpret_cast<MatSmem<R, TJ>*>(mat_smem);
     const uint32_t tid = threadIdx.x, lane = tid & 31;
@@ -387,12 +434,11 @@ __global__ void __launch_bounds__(R) k_matrix(MatParams P) {
                     reinterpret_cast<uint4*>(&S.tf[q >> 4][0])[q & 15] = __ldg(src + (q & 15));
                 }
                 __syncthreads();
-                // ---- every row against the tile
-                for (uint32_t j = 0; j < nt; j++) {
+                // ---- every row against the tile, two target filters at a time
+                auto consume = [&](uint32_t j, uint32_t match) {
                     const uint32_t tm = S.tmeta[j];
                     const uint32_t s2 = tm & 0xFFFFu;
                     if (active && s2 >= (uint32_t)kMinElem) {
-                        const uint32_t match = and_popc_hs(a, &S.tf[j][0]);
                         const uint32_t cut = cut_for(S.cut_sum, S.cut256, s1, s2);
                         uint32_t num = 0, den = 1;
                         if (match > cut && !staged_exit(a, &S.tf[j][0], cut)) {
@@ -415,7 +461,15 @@ __global__ void __launch_bounds__(R) k_matrix(MatParams P) {
                         bnum = 0;
                         bden = 0;
                     }
+                };
+                uint32_t j = 0;
+                for (; j + 1 < nt; j += 2) {
+                    uint32_t m0 = 0, m1 = 0;
+                    if (active) and_popc_hs2(a, &S.tf[j][0], &S.tf[j + 1][0], m0, m1);
+                    consume(j, m0);
+                    consume(j + 1, m1);
                 }
+                if (j < nt) consume(j, active ? and_popc_hs(a, &S.tf[j][0]) : 0u);
                 __syncthreads();
                 // ---- fold the completed targets' maxima in filter order
                 if (!split) {
