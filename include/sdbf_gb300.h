@@ -188,6 +188,19 @@ int sdbfg_compare_to(sdbfg_ctx *ctx, const sdbfg_set *queries, const sdbfg_set *
 int sdbfg_compare_all_device(sdbfg_ctx *ctx, const sdbfg_set *set, int32_t *dev_scores);
 int sdbfg_compare_to_device(sdbfg_ctx *ctx, const sdbfg_set *queries, const sdbfg_set *targets,
                             int32_t *dev_scores);
+/* The pairs whose score is >= threshold, in pair order, as the rows
+ * sdbf_set::compare_all / compare_to print them (sdbf/sdbf_set.cc:249-265,
+ * 330-346; i < j for all pairs, (query, target) for compare_to).  Returns
+ * SDBFG_ERR_CAPACITY with *count = the number of matches when cap is too
+ * small (call again with room for *count). */
+typedef struct {
+    uint32_t i, j;
+    int32_t score;
+} sdbfg_match;
+int sdbfg_compare_all_matches(sdbfg_ctx *ctx, const sdbfg_set *set, int32_t threshold, sdbfg_match *out,
+                              uint64_t cap, uint64_t *count);
+int sdbfg_compare_to_matches(sdbfg_ctx *ctx, const sdbfg_set *queries, const sdbfg_set *targets, int32_t threshold,
+                             sdbfg_match *out, uint64_t cap, uint64_t *count);
 /* Filter pairs the comparison scores (sum of n_ref * n_target over pairs). */
 uint64_t sdbfg_compare_filter_pairs(sdbfg_ctx *ctx, const sdbfg_set *a, const sdbfg_set *b_or_null);
 /* Engine tuning: kernel variant 0..4 (rows per CTA x target filters per

@@ -102,6 +102,8 @@ def lib() -> C.CDLL:
         L.sdbfg_compare_all.argtypes = [vp, vp, i32p]
         L.sdbfg_compare_to.argtypes = [vp, vp, vp, i32p]
         L.sdbfg_compare_all_device.argtypes = [vp, vp, vp]
+        L.sdbfg_compare_all_matches.argtypes = [vp, vp, C.c_int32, vp, C.c_uint64, u64p]
+        L.sdbfg_compare_to_matches.argtypes = [vp, vp, vp, C.c_int32, vp, C.c_uint64, u64p]
         L.sdbfg_compare_to_device.argtypes = [vp, vp, vp, vp]
         L.sdbfg_compare_filter_pairs.argtypes = [vp, vp, vp]
         L.sdbfg_compare_filter_pairs.restype = C.c_uint64
@@ -371,6 +373,26 @@ class Context:
         if len(q) and len(t):
             self._check(lib().sdbfg_compare_to(self.h, q.h, t.h, _ptr(out, C.c_int32)))
         return out[: len(q) * len(t)].reshape(len(q), len(t))
+
+    def _matches(self, fn, args, threshold):
+        cnt = C.c_uint64()
+        cap = 1 << 16
+        while True:
+            out = np.zeros((cap, 3), dtype=np.int32)
+            rc = fn(self.h, *args, threshold, out.ctypes.data, cap, C.byref(cnt))
+            if rc == -5 and cnt.value > cap:  # SDBFG_ERR_CAPACITY: room for the reported count
+                cap = int(cnt.value)
+                continue
+            self._check(rc)
+            return out[: cnt.value].copy()
+
+    def compare_all_matches(self, s: DeviceSet, threshold: int = 1) -> np.ndarray:
+        """(i, j, score) rows with score >= threshold, i < j, in pair order."""
+        return self._matches(lib().sdbfg_compare_all_matches, (s.h,), threshold)
+
+    def compare_to_matches(self, q: DeviceSet, t: DeviceSet, threshold: int = 1) -> np.ndarray:
+        """(query, target, score) rows with score >= threshold, in pair order."""
+        return self._matches(lib().sdbfg_compare_to_matches, (q.h, t.h), threshold)
 
     def compare_all_device(self, s: DeviceSet, dev_scores: int):
         """Queue all-pairs scores of s into a device int32 array (n*(n-1)/2)."""

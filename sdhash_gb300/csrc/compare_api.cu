@@ -419,6 +419,62 @@ extern "C" int sdbfg_compare_to(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_se
     return SDBFG_OK;
 }
 
+// scores (already queued into c->d_scores) -> matches on the host
+static int collect_matches(sdbfg_ctx* c, uint64_t nscores, uint32_t mode, uint64_t dim, int32_t threshold,
+                           sdbfg_match* out, uint64_t cap, uint64_t* count) {
+    cudaStream_t st = c->stream;
+    const uint64_t nb = (nscores + kMatchBlockScores - 1) / kMatchBlockScores;
+    CUDA_TRY(c, c->d_match_counts.ensure(std::max<uint64_t>(1, nb) * 4));
+    CUDA_TRY(c, c->d_match_offs.ensure((nb + 1) * 8));
+    const int32_t* sc = c->d_scores.as<int32_t>();
+    TIMED_LAUNCH_ON(c, "k_match_count", st, launch_match_count(sc, nscores, threshold, c->d_match_counts.as<uint32_t>(), st));
+    TIMED_LAUNCH_ON(c, "k_match_scan", st, launch_match_scan(c->d_match_counts.as<uint32_t>(), nb,
+                                                             c->d_match_offs.as<uint64_t>(), st));
+    uint64_t total = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&total, c->d_match_offs.as<uint64_t>() + nb, 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    *count = total;
+    if (total > cap) return fail(c, SDBFG_ERR_CAPACITY, "%llu matches, room for %llu", (unsigned long long)total,
+                                 (unsigned long long)cap);
+    if (!total) return SDBFG_OK;
+    CUDA_TRY(c, c->d_matches.ensure(total * sizeof(sdbfg_match)));
+    TIMED_LAUNCH_ON(c, "k_match_write", st, launch_match_write(sc, nscores, threshold, c->d_match_offs.as<uint64_t>(),
+                                                               mode, dim, c->d_matches.as<uint32_t>(), total, st));
+    CUDA_TRY(c, cudaMemcpyAsync(out, c->d_matches.p, total * sizeof(sdbfg_match), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    return SDBFG_OK;
+}
+
+extern "C" int sdbfg_compare_all_matches(sdbfg_ctx* c, const sdbfg_set* s, int32_t threshold, sdbfg_match* out,
+                                         uint64_t cap, uint64_t* count) {
+    if (!c || !s || !count || (cap && !out)) return SDBFG_ERR_ARG;
+    *count = 0;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (s->n < 2) return SDBFG_OK;
+    MatPlan* p;
+    int rc = get_plan(c, s, nullptr, kMatModeAll, &p);
+    if (rc) return rc;
+    CUDA_TRY(c, c->d_scores.ensure(p->nscores * 4));
+    rc = run_plan(c, p, s, nullptr, c->d_scores.as<int32_t>());
+    if (rc) return rc;
+    return collect_matches(c, p->nscores, kMatModeAll, s->n, threshold, out, cap, count);
+}
+
+extern "C" int sdbfg_compare_to_matches(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_set* t, int32_t threshold,
+                                        sdbfg_match* out, uint64_t cap, uint64_t* count) {
+    if (!c || !q || !t || !count || (cap && !out)) return SDBFG_ERR_ARG;
+    *count = 0;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!q->n || !t->n) return SDBFG_OK;
+    MatPlan* p;
+    int rc = get_plan(c, q, t, kMatModeCross, &p);
+    if (rc) return rc;
+    CUDA_TRY(c, c->d_scores.ensure(p->nscores * 4));
+    rc = run_plan(c, p, q, t, c->d_scores.as<int32_t>());
+    if (rc) return rc;
+    return collect_matches(c, p->nscores, kMatModeCross, t->n, threshold, out, cap, count);
+}
+
 extern "C" int sdbfg_ctx_set_compare_tuning(sdbfg_ctx* c, int variant, uint64_t unit_work, int use_graphs) {
     if (!c || variant < 0 || variant >= kMatVariants || unit_work == 0) return SDBFG_ERR_ARG;
     c->mat_variant = variant;

@@ -562,3 +562,139 @@ int matrix_ctas_per_sm(int variant) {
 }
 
 }  // namespace sdbfg
+
+// ------------------------------------------------------ threshold matches
+// Scores >= threshold compacted in pair order into (i, j, score) triples:
+// per 1024-score block a count, one exclusive scan over the block counts,
+// then each block writes its matches at its offset (order preserving).
+namespace sdbfg {
+
+constexpr uint32_t kMatchBlock = 1024;  // scores per block, 256 threads x 4
+
+__global__ void __launch_bounds__(256) k_match_count(const int32_t* __restrict__ scores, uint64_t n, int32_t thr,
+                                                     uint32_t* __restrict__ counts) {
+    const uint64_t b = blockIdx.x;
+    const uint64_t base = b * kMatchBlock + threadIdx.x * 4;
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) c += (base + k < n) && scores[base + k] >= thr;
+    __shared__ uint32_t part[8];
+    uint32_t w = c;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) w += __shfl_xor_sync(0xffffffffu, w, d);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int k = 0; k < 8; k++) s += part[k];
+        counts[b] = s;
+    }
+}
+
+// single CTA: counts[] -> exclusive offsets (u64), total in offs[nb]
+__global__ void __launch_bounds__(1024) k_match_scan(const uint32_t* __restrict__ counts, uint64_t nb,
+                                                     uint64_t* __restrict__ offs) {
+    __shared__ uint64_t part[1024];
+    const uint64_t per = (nb + 1023) / 1024;
+    const uint64_t b0 = threadIdx.x * per, b1 = min(nb, b0 + per);
+    uint64_t s = 0;
+    for (uint64_t b = b0; b < b1; b++) s += counts[b];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int d = 1; d < 1024; d <<= 1) {
+        const uint64_t v = threadIdx.x >= (uint32_t)d ? part[threadIdx.x - d] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint64_t run = part[threadIdx.x] - s;
+    for (uint64_t b = b0; b < b1; b++) {
+        offs[b] = run;
+        run += counts[b];
+    }
+    if (threadIdx.x == 1023) offs[nb] = part[1023];
+}
+
+__device__ __forceinline__ void pair_of(uint64_t k, uint32_t mode, uint64_t n, uint32_t& i, uint32_t& j) {
+    if (mode == kMatModeCross) {
+        i = (uint32_t)(k / n);
+        j = (uint32_t)(k % n);
+        return;
+    }
+    // row i of the upper triangle: start(i) = i*(2n-i-1)/2 <= k < start(i+1)
+    const double nn = (double)n;
+    double r = floor(((2.0 * nn - 1.0) - sqrt((2.0 * nn - 1.0) * (2.0 * nn - 1.0) - 8.0 * (double)k)) / 2.0);
+    uint64_t ii = r < 0 ? 0 : (uint64_t)r;
+    auto start = [&](uint64_t x) { return x * (2 * n - x - 1) / 2; };
+    while (ii > 0 && start(ii) > k) ii--;
+    while (ii + 1 < n && start(ii + 1) <= k) ii++;
+    i = (uint32_t)ii;
+    j = (uint32_t)(k - start(ii) + ii + 1);
+}
+
+__global__ void __launch_bounds__(256) k_match_write(const int32_t* __restrict__ scores, uint64_t n, int32_t thr,
+                                                     const uint64_t* __restrict__ offs, uint32_t mode,
+                                                     uint64_t dim, uint32_t* __restrict__ out, uint64_t cap) {
+    __shared__ uint32_t warp_base[8];
+    const uint64_t b = blockIdx.x;
+    const uint64_t base = b * kMatchBlock + threadIdx.x * 4;
+    bool hit[4];
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        hit[k] = (base + k < n) && scores[base + k] >= thr;
+        c += hit[k];
+    }
+    // exclusive prefix of c over the block (thread order == score order)
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= (uint32_t)d) incl += v;
+    }
+    if (lane == 31) warp_base[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int k = 0; k < 8; k++) {
+            const uint32_t v = warp_base[k];
+            warp_base[k] = s;
+            s += v;
+        }
+    }
+    __syncthreads();
+    uint64_t pos = offs[b] + warp_base[warp] + incl - c;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (!hit[k]) continue;
+        if (pos < cap) {
+            uint32_t i, j;
+            pair_of(base + k, mode, dim, i, j);
+            out[3 * pos] = i;
+            out[3 * pos + 1] = j;
+            out[3 * pos + 2] = (uint32_t)scores[base + k];
+        }
+        pos++;
+    }
+}
+
+cudaError_t launch_match_count(const int32_t* scores, uint64_t n, int32_t thr, uint32_t* counts, cudaStream_t st) {
+    const uint64_t nb = (n + kMatchBlock - 1) / kMatchBlock;
+    if (nb) k_match_count<<<(uint32_t)nb, 256, 0, st>>>(scores, n, thr, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_match_scan(const uint32_t* counts, uint64_t nb, uint64_t* offs, cudaStream_t st) {
+    k_match_scan<<<1, 1024, 0, st>>>(counts, nb, offs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_match_write(const int32_t* scores, uint64_t n, int32_t thr, const uint64_t* offs, uint32_t mode,
+                               uint64_t dim, uint32_t* out, uint64_t cap, cudaStream_t st) {
+    const uint64_t nb = (n + kMatchBlock - 1) / kMatchBlock;
+    if (nb) k_match_write<<<(uint32_t)nb, 256, 0, st>>>(scores, n, thr, offs, mode, dim, out, cap);
+    return cudaGetLastError();
+}
+
+}  // namespace sdbfg

@@ -97,4 +97,11 @@ cudaError_t launch_matrix(const MatParams& P, int variant, uint32_t grid, cudaSt
 cudaError_t launch_matrix_finalize(const MatParams& P, cudaStream_t st);
 int matrix_ctas_per_sm(int variant);
 
+// scores >= threshold -> (i, j, score) u32 triples in pair order
+constexpr uint32_t kMatchBlockScores = 1024;
+cudaError_t launch_match_count(const int32_t* scores, uint64_t n, int32_t thr, uint32_t* counts, cudaStream_t st);
+cudaError_t launch_match_scan(const uint32_t* counts, uint64_t nblocks, uint64_t* offs, cudaStream_t st);
+cudaError_t launch_match_write(const int32_t* scores, uint64_t n, int32_t thr, const uint64_t* offs, uint32_t mode,
+                               uint64_t dim, uint32_t* out, uint64_t cap, cudaStream_t st);
+
 }  // namespace sdbfg

@@ -58,7 +58,8 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
     for (DevBuf* b : {&c->d_rank, &c->d_ent, &c->d_cut, &c->d_data, &c->d_chunks, &c->d_tiles, &c->d_files,
                       &c->d_order, &c->d_tile_out, &c->d_features, &c->d_work_filters, &c->d_info,
                       &c->d_counters, &c->d_pack_src, &c->d_pack_dst_off, &c->d_out_filters, &c->d_out_counts,
-                      &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase})
+                      &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase,
+                      &c->d_match_counts, &c->d_match_offs, &c->d_matches})
         b->release();
     for (auto& S : c->slot) {
         for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work,

@@ -95,3 +95,19 @@ def test_plain_per_pair_path_agrees(ctx, uneven):
     iu = np.triu_indices(len(ds), 1)
     got = ctx.score_pairs(dev, dev, iu[0], iu[1])
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("threshold", [1, 5, -1])
+def test_threshold_matches_in_pair_order(ctx, uneven, threshold):
+    ds, ods, want = uneven
+    dev = ctx.upload(ds)
+    got = ctx.compare_all_matches(dev, threshold)
+    iu = np.triu_indices(len(ds), 1)
+    keep = want >= threshold
+    exp = np.stack([iu[0][keep], iu[1][keep], want[keep]], axis=1).astype(np.int32)
+    assert np.array_equal(got, exp)
+    q, t = ctx.upload(ds[::2]), ctx.upload(ds[1::3])
+    full = ctx.compare_to(q, t)
+    qi, ti = np.nonzero(full >= threshold)
+    expx = np.stack([qi, ti, full[qi, ti]], axis=1).astype(np.int32)
+    assert np.array_equal(ctx.compare_to_matches(q, t, threshold), expx)
