@@ -65,12 +65,11 @@ def parse():
                          "image: block-mode disk image + query fragments compared against it")
     ap.add_argument("--image-gib", type=int, default=16, help="image: disk image size (GiB, multiple of 128 MiB)")
     ap.add_argument("--queries", type=int, default=100000, help="image: query fragments")
-    ap.add_argument("--ref-filters", type=int, default=2_000_000, help="serve: block filters in the reference set")
+    ap.add_argument("--ref-filters", type=int, default=244 * 8192, help="serve: block filters in the reference set")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered Poisson load (queries/s)")
     ap.add_argument("--serve-queries", type=int, default=1500, help="serve: queries per load run")
     ap.add_argument("--digests", type=int, default=20000, help="allpairs: digests in the set")
     ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
-    ap.add_argument("--pool-gib", type=float, default=4.0, help="allpairs: mixture content digested for the filter pool")
     ap.add_argument("--plain-pairs", type=int, default=400, help="allpairs: pairs timed one call each")
     ap.add_argument("--cpu-pairs", type=int, default=256, help="allpairs: pairs timed on the host (oracle)")
     return ap.parse_args()
@@ -269,39 +268,27 @@ AP_UNIT = "filter pairs/s"
 
 
 def allpairs_digests(args, ctx):
-    """20,000 stream digests with filter counts log-uniform over 1..2000.
+    """20,000 stream digests with filter counts about round(exp(U(0, ln 2000))).
 
-    Filters come from a pool of mixture content digested on the GPU (stream
-    mode, element counts from generation).  Digest i takes a random run of
-    n_i consecutive pool filters, each rotated by a per-digest byte offset so
-    that digests whose runs overlap do not share identical filters; the
-    rotation keeps every filter's popcount and element count."""
-    import sdhash_gb300 as g
+    Each digest is generated on the GPU from its own mixture content sized
+    n x 12 KiB (mixture content yields one stream filter per ~12.3 KiB), so
+    filters and element counts come from generation.  Content is produced and
+    digested in groups to bound host memory."""
     from sdhash_gb300 import synth
     rng = np.random.default_rng(args.seed + 1000)
-    counts = np.clip(np.floor(np.exp(rng.uniform(0.0, np.log(args.max_filters + 1), args.digests))), 1,
+    target = np.clip(np.rint(np.exp(rng.uniform(0.0, np.log(args.max_filters), args.digests))), 1,
                      args.max_filters).astype(np.int64)
-    nfile = max(1, int(args.pool_gib * 64))
-    sizes = np.full(nfile, 16 << 20, dtype=np.uint64)
-    data, offs, lens = synth.fill_many(args.seed + 1001, "mixture", sizes)
-    pool = ctx.digest_packed(data, offs, lens, 0)
-    del data
-    pf = np.concatenate([d.filters.reshape(-1, 256) for d in pool])
-    pe = np.concatenate([np.r_[np.full(d.bf_count - 1, 160, np.uint16), np.uint16(d.last_count)] for d in pool])
-    P = len(pf)
-    assert P >= args.max_filters
-    F = np.empty((int(counts.sum()), 256), dtype=np.uint8)
-    E = np.empty(int(counts.sum()), dtype=np.uint16)
-    starts = rng.integers(0, P - counts + 1)
-    rots = rng.integers(0, 256, args.digests)
-    digs, o = [], 0
-    for i, (n, st, r) in enumerate(zip(counts, starts, rots)):
-        n, st = int(n), int(st)
-        F[o:o + n] = np.roll(pf[st:st + n], int(r), axis=1)
-        E[o:o + n] = pe[st:st + n]
-        digs.append(g.Digest(f"d{i:05d}", 0, n, int(E[o + n - 1]), 160, 0, F[o:o + n], E[o:o + n]))
-        o += n
-    return digs, counts, P
+    sizes = (target * (12 << 10)).astype(np.uint64)
+    names = [f"d{i:05d}" for i in range(args.digests)]
+    digs = []
+    step = 1000
+    for g0 in range(0, args.digests, step):
+        sz = sizes[g0:g0 + step]
+        data, offs, lens = synth.fill_many(args.seed + 1001 + g0, "mixture", sz)
+        digs += ctx.digest_packed(data, offs, lens, 0, names=names[g0:g0 + step])
+        del data
+    counts = np.array([d.bf_count for d in digs], dtype=np.int64)
+    return digs, counts, int(sizes.sum())
 
 
 def main_allpairs(args):
@@ -313,7 +300,7 @@ def main_allpairs(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     t0 = time.perf_counter()
-    digs, counts, pool_filters = allpairs_digests(args, ctx)
+    digs, counts, content_bytes = allpairs_digests(args, ctx)
     t_build = time.perf_counter() - t0
     n = len(digs)
     npairs = n * (n - 1) // 2
@@ -391,7 +378,8 @@ def main_allpairs(args):
             "config": {"workload": "batched uneven all-pairs compare", "digests": n, "pairs": npairs,
                        "filters_per_digest": f"log-uniform 1..{args.max_filters}", "filters": int(counts.sum()),
                        "filter_pairs_per_step": fpairs, "threshold": 1,
-                       "filter_source": f"{pool_filters} stream filters of {args.pool_gib:g} GiB mixture content",
+                       "filter_source": f"stream digests of {content_bytes / 1e9:.1f} GB mixture content "
+                                        "(n x 12 KiB per digest) generated on the GPU",
                        "variant": variant, "unit_work": unit_work, "autotune_s": round(t_tune, 2),
                        "autotune_sample_rate": tuned_rate, "build_s": round(t_build, 1),
                        "l2": "filters 5x larger than L2"},
@@ -446,7 +434,8 @@ def timed(stream, fn, reps=1):
 
 def main_image(args):
     """Block-mode image digest (-b 16, 128 MiB segments) and query-fragment
-    digests (stream mode), then every query against every image segment."""
+    digests (-b 16, 1..64 filters each), then every query against every
+    image segment."""
     import torch
     import sdhash_gb300 as g
     from sdhash_gb300 import synth
@@ -488,13 +477,14 @@ def main_image(args):
         qdata[int(qoffs[i]):int(qoffs[i]) + int(qsz[i])] = image[int(src[i]):int(src[i]) + int(qsz[i])]
     qnames = [f"q{i:06d}" for i in range(args.queries)]
     dq = torch.from_numpy(qdata).cuda()
-    qcap = ctx.capacity(qsz, 0)
+    qcap = ctx.capacity(qsz, dd)
     qout = torch.empty(qcap * 256, dtype=torch.uint8, device="cuda")
-    runq = lambda: ctx.digest_device(dq.data_ptr(), qoffs, qsz, 0, qout.data_ptr(), qcap)
+    qcnt = torch.empty(qcap, dtype=torch.uint16, device="cuda")
+    runq = lambda: ctx.digest_device(dq.data_ptr(), qoffs, qsz, dd, qout.data_ptr(), qcap, qcnt.data_ptr())
     for _ in range(args.warmup):
         runq()
     qres, q_ms = timed(stream, runq)
-    qdigs = digests_from_device(g, qres, qnames, qsz, 0, qout, None)
+    qdigs = digests_from_device(g, qres, qnames, qsz, dd, qout, qcnt)
     del dq
     # ---- parity spot checks against the oracle (sampled)
     from oracle import Oracle
@@ -505,7 +495,7 @@ def main_image(args):
     for k, ref in zip(chk, refs):
         assert ref.to_string() == idigs[k].to_string(), inames[k]
     for i in rng.choice(args.queries, 24, replace=False):
-        ref = O.digest(qnames[i], qdata[int(qoffs[i]):int(qoffs[i]) + int(qsz[i])].tobytes(), 0)
+        ref = O.digest(qnames[i], qdata[int(qoffs[i]):int(qoffs[i]) + int(qsz[i])].tobytes(), dd)
         assert ref.to_string() == qdigs[i].to_string(), qnames[i]
     # ---- comparison: every query x every segment
     qset, iset = ctx.upload(qdigs), ctx.upload(idigs)
@@ -531,7 +521,7 @@ def main_image(args):
     # e2e: host query buffer -> digests -> compare against the resident image set -> scores on the host
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    q2 = ctx.digest_packed(qdata, qoffs, qsz, 0, names=qnames)
+    q2 = ctx.digest_packed(qdata, qoffs, qsz, dd, names=qnames)
     qs2 = ctx.upload(q2)
     host_scores = ctx.compare_to(qs2, iset)
     t_e2e = time.perf_counter() - t0
@@ -573,7 +563,7 @@ def main_image(args):
             "image_digest": {"value": int(ilens.sum()) / (img_ms / 1e3) / 1e9, "unit": "GB/s", "ms": img_ms,
                              "mode": "block (-b 16), device resident"},
             "query_digest": {"value": int(qsz.sum()) / (q_ms / 1e3) / 1e9, "unit": "GB/s", "ms": q_ms,
-                             "mode": "stream, device resident"},
+                             "mode": "block (-b 16), device resident"},
             "top_match": {"cut_queries_best_segment_found": int(found.sum()), "cut_queries": int(cut.sum()),
                           "queries_with_score_ge_1": int((scores.max(1) >= 1).sum())},
             "gpu_launches": launches, "clocks": clocks.summary(),
@@ -597,8 +587,8 @@ SV_METRIC = "served queries/s (p50/p99 latency)"
 def serve_reference_set(args, ctx, stream, pool_queries):
     """Reference set: a disk image of `ref_filters` 16 KiB blocks digested in
     block mode (-b 16) in 128 MiB segments, generated and digested a few GiB
-    at a time.  Query digests: 60% cut from the image, 40% fresh random data,
-    sizes log-uniform 4 KiB..48 MiB (1..~4096 filters)."""
+    at a time.  Query digests: block mode, round(exp(U(0, ln 4096))) filters
+    (n x 16 KiB of content), 60% cut from the image, 40% fresh random data."""
     import torch
     import sdhash_gb300 as g
     from sdhash_gb300 import synth
@@ -607,7 +597,8 @@ def serve_reference_set(args, ctx, stream, pool_queries):
     seg_sizes = [SEG] * (total // SEG) + ([total % SEG] if total % SEG else [])
     names = [f"image.{k * SEG // (1 << 20):04d}M" for k in range(len(seg_sizes))]
     rng = np.random.default_rng(args.seed + 3000)
-    qsz = synth.log_uniform_sizes(args.seed + 3001, pool_queries, 4096, 48 << 20)
+    qn = np.clip(np.rint(np.exp(rng.uniform(0.0, np.log(4096), pool_queries))), 1, 4096).astype(np.int64)
+    qsz = (qn * dd).astype(np.uint64)  # one block-mode filter per 16 KiB block
     cut = rng.random(pool_queries) < 0.6
     qbufs = [None] * pool_queries
     digs = []
@@ -632,7 +623,7 @@ def serve_reference_set(args, ctx, stream, pool_queries):
     qnames = [f"q{i:05d}" for i in range(pool_queries)]
     queries = []
     for k in range(0, pool_queries, 64):
-        queries += ctx.digest_buffers([b.tobytes() for b in qbufs[k:k + 64]], qnames[k:k + 64], 0)
+        queries += ctx.digest_buffers([b.tobytes() for b in qbufs[k:k + 64]], qnames[k:k + 64], dd)
     return digs, [q for q in queries if q is not None], cut
 
 
