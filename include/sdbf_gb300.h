@@ -160,6 +160,14 @@ typedef struct {
  * (sdbf::compute_hamming, sdbf_class.cc:388-401). */
 int sdbfg_set_upload(sdbfg_ctx *ctx, const sdbfg_digest_desc *digests, uint32_t n, sdbfg_set **out);
 void sdbfg_set_free(sdbfg_set *set);
+/* sdbf::fast (sdbf/sdbf_class.cc:425-439) on digests [first, first+count)
+ * of a resident set: every filter's 256 bytes are folded into its first 64
+ * (bloom_filter::fold(2), bloom_filter.cc:262-288; the other bytes are left
+ * as they were), its hamming weight becomes that of the folded 64 bytes, and
+ * the digest is scored in fast mode (CUTOFFS64, 64-byte one-stage count)
+ * whenever it is the reference side of a pair -- the reference's fastmode
+ * rule (sdbf_core.cc:422-440).  Folding twice changes nothing. */
+int sdbfg_set_fast(sdbfg_ctx *ctx, sdbfg_set *set, uint32_t first, uint32_t count);
 uint32_t sdbfg_set_size(const sdbfg_set *set);
 
 /* Scores of explicit pairs (a[ia[k]], b[ib[k]]) as sdbf::compare(other, 0)

@@ -47,7 +47,7 @@ class _Digest(C.Structure):
     _fields_ = [("name", C.c_char_p), ("orig_size", C.c_uint64), ("bf_count", C.c_uint32),
                 ("last_count", C.c_uint32), ("max_elem", C.c_uint32), ("dd_block_size", C.c_uint32),
                 ("filters", C.POINTER(C.c_uint8)), ("elem_counts", C.POINTER(C.c_uint16)),
-                ("hamming", C.POINTER(C.c_uint16))]
+                ("hamming", C.POINTER(C.c_uint16)), ("fastmode", C.c_int32)]
 
 
 class OracleDigest:
@@ -121,6 +121,8 @@ class Oracle:
         L.orc_score_all_matrix.argtypes = [C.POINTER(_Digest), C.c_uint32, i32p, C.c_int]
         L.orc_score_cross_matrix.argtypes = [C.POINTER(_Digest), C.c_uint32, C.POINTER(_Digest), C.c_uint32,
                                              i32p, C.c_int]
+        L.orc_fast.argtypes = [C.POINTER(_Digest)]
+        L.orc_fast.restype = None
         L.orc_score_pairs.argtypes = [C.POINTER(_Digest), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                       C.c_uint64, i32p, C.c_int]
         L.orc_digest_many.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.POINTER(C.c_char_p),
@@ -172,6 +174,11 @@ class Oracle:
         if rc != 0:
             raise ValueError(f"oracle parse failed ({rc})")
         return OracleDigest(self.L, st)
+
+    def fast(self, d: OracleDigest) -> OracleDigest:
+        """sdbf::fast: fold the digest's filters to 64 bytes in place."""
+        self.L.orc_fast(C.byref(d.st))
+        return d
 
     def score(self, a: OracleDigest, b: OracleDigest) -> int:
         return self.L.orc_score(C.byref(a.st), C.byref(b.st))
@@ -264,6 +271,10 @@ class Reference:
         L.ref_compare_all_file.restype = C.c_void_p
         L.ref_compare_to_files.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_uint]
         L.ref_compare_to_files.restype = C.c_void_p
+        L.ref_compare_all_file_fast.argtypes = [C.c_char_p, C.c_int]
+        L.ref_compare_all_file_fast.restype = C.c_void_p
+        L.ref_compare_to_files_fast.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
+        L.ref_compare_to_files_fast.restype = C.c_void_p
         L.ref_free.argtypes = [C.c_void_p]
 
     def _take(self, p) -> str:
@@ -281,8 +292,12 @@ class Reference:
     def compare_text(self, a: str, b: str) -> int:
         return self.L.ref_compare_text(a.encode(), b.encode(), 0)
 
-    def compare_all_file(self, path: str, threshold: int = 1) -> str:
+    def compare_all_file(self, path: str, threshold: int = 1, fast: bool = False) -> str:
+        if fast:
+            return self._take(self.L.ref_compare_all_file_fast(path.encode(), threshold))
         return self._take(self.L.ref_compare_all_file(path.encode(), threshold))
 
-    def compare_to_files(self, q: str, t: str, threshold: int = 1) -> str:
+    def compare_to_files(self, q: str, t: str, threshold: int = 1, fast: bool = False) -> str:
+        if fast:
+            return self._take(self.L.ref_compare_to_files_fast(q.encode(), t.encode(), threshold))
         return self._take(self.L.ref_compare_to_files(q.encode(), t.encode(), threshold, 0))

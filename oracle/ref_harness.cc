@@ -78,6 +78,28 @@ char *ref_compare_to_files(const char *qname, const char *tname,
     return out;
 }
 
+// The same two calls with the reference's --fast flag (sdbf::fast folds the
+// filters before comparing; compare_to folds only the query set's items,
+// sdbf/sdbf_set.cc:321-331).
+char *ref_compare_all_file_fast(const char *fname, int threshold) {
+    sdbf_set set(fname);
+    std::string r = set.compare_all_quiet(threshold, 1, true);
+    for (uint32_t i = 0; i < set.size(); i++) delete set.at(i);
+    char *out = (char *)malloc(r.size() + 1);
+    memcpy(out, r.c_str(), r.size() + 1);
+    return out;
+}
+
+char *ref_compare_to_files_fast(const char *qname, const char *tname, int threshold) {
+    sdbf_set q(qname), t(tname);
+    std::string r = q.compare_to_quiet(&t, threshold, 0, 1, true);
+    for (uint32_t i = 0; i < q.size(); i++) delete q.at(i);
+    for (uint32_t i = 0; i < t.size(); i++) delete t.at(i);
+    char *out = (char *)malloc(r.size() + 1);
+    memcpy(out, r.c_str(), r.size() + 1);
+    return out;
+}
+
 void ref_free(void *p) { free(p); }
 
 }  // extern "C"

@@ -379,8 +379,33 @@ uint32_t orc_match_cut(const uint8_t *f1, const uint8_t *f2, uint32_t cut) {
     return c;
 }
 
+static uint32_t orc_match_cut_64(const uint8_t *f1, const uint8_t *f2, uint32_t cut) {
+    /* bf_bitcount_cut_64_asm, bf_utils.cc:78-110 (first 64 bytes, one stage:
+     * 2c + slack < cut after 32 bytes), then the full recount */
+    const uint32_t slack = 48;
+    uint32_t c = pc64(f1, f2, 0, 4);
+    if (cut > 0 && 2 * c + slack < cut) return 0;
+    c += pc64(f1, f2, 4, 8);
+    return c;
+}
+
+void orc_fast(orc_digest *d) {
+    for (uint32_t i = 0; i < d->bf_count; i++) {
+        uint8_t *f = d->filters + 256ull * i;
+        uint64_t w[32], h = 0;
+        memcpy(w, f, 256);
+        for (int j = 0; j < 16; j++) w[j] |= w[j + 16];  /* fold 1: 256 -> 128 bytes */
+        for (int j = 0; j < 8; j++) w[j] |= w[j + 8];    /* fold 2: 128 -> 64 bytes */
+        memcpy(f, w, 64);                                /* only the folded 64 bytes are copied back */
+        for (int j = 0; j < 8; j++) h += (uint64_t)__builtin_popcountll(w[j]);
+        d->hamming[i] = (uint16_t)h;
+    }
+    d->fastmode = 1;
+}
+
 double orc_max_score(const orc_digest *ref, uint32_t ri, const orc_digest *tgt) {
-    /* sdbf_max_score, sdbf_core.cc:395-455 (non-fast mode) */
+    /* sdbf_max_score, sdbf_core.cc:395-455; the reference digest's fastmode
+     * selects CUTOFFS64 and the 64-byte count (:422-440) */
     uint32_t s1 = (uint32_t)orc_elem_count(ref, ri);
     if (s1 < ORC_MIN_ELEM) return 0;
     const uint8_t *f1 = ref->filters + 256ull * ri;
@@ -391,8 +416,14 @@ double orc_max_score(const orc_digest *ref, uint32_t ri, const orc_digest *tgt) 
         if (s2 < ORC_MIN_ELEM) continue;
         uint32_t e2 = tgt->hamming[j];
         uint32_t max_est = e1 < e2 ? e1 : e2;
-        uint32_t cut = SDBF_CUTOFFS256[4096 / (s1 + s2)];
-        uint32_t match = orc_match_cut(f1, tgt->filters + 256ull * j, cut);
+        uint32_t cut, match;
+        if (!ref->fastmode) {
+            cut = SDBF_CUTOFFS256[4096 / (s1 + s2)];
+            match = orc_match_cut(f1, tgt->filters + 256ull * j, cut);
+        } else {
+            cut = SDBF_CUTOFFS64[1024 / (s1 + s2)];
+            match = orc_match_cut_64(f1, tgt->filters + 256ull * j, cut);
+        }
         double s = (match <= cut) ? 0 : (double)(match - cut) / (double)(max_est - cut);
         if (s > best) best = s;
     }

@@ -32,7 +32,13 @@ typedef struct {
     uint8_t  *filters;        /* bf_count * 256 bytes */
     uint16_t *elem_counts;    /* block mode only (NULL for stream) */
     uint16_t *hamming;        /* popcount per filter */
+    int32_t   fastmode;       /* filters folded to 64 bytes (sdbf::fast) */
 } orc_digest;
+
+/* sdbf::fast (sdbf_class.cc:425-439): fold every filter 256 -> 64 bytes
+ * (bloom_filter::fold(2), bloom_filter.cc:262-288) into its first 64 bytes,
+ * hamming of the folded bytes, fastmode on. */
+void orc_fast(orc_digest *d);
 
 /* FIPS 180-4 SHA-1 of an arbitrary message. */
 void orc_sha1(const uint8_t *msg, uint64_t len, uint8_t out[20]);

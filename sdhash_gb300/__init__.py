@@ -96,6 +96,7 @@ def lib() -> C.CDLL:
                                                 C.POINTER(DigestResult)]
         L.sdbfg_set_upload.argtypes = [vp, C.POINTER(DigestDesc), C.c_uint32, C.POINTER(vp)]
         L.sdbfg_set_free.argtypes = [vp]
+        L.sdbfg_set_fast.argtypes = [vp, vp, C.c_uint32, C.c_uint32]
         L.sdbfg_set_size.argtypes = [vp]
         L.sdbfg_set_size.restype = C.c_uint32
         L.sdbfg_score_pairs.argtypes = [vp, vp, vp, u32p, u32p, C.c_uint64, i32p]
@@ -137,7 +138,7 @@ class Digest:
     """A similarity digest: the data fields of the reference's sdbf object."""
 
     __slots__ = ("name", "orig_size", "bf_count", "last_count", "max_elem", "dd_block_size", "filters",
-                 "elem_counts")
+                 "elem_counts", "fastmode")
 
     def __init__(self, name: str, orig_size: int, bf_count: int, last_count: int, max_elem: int,
                  dd_block_size: int, filters: np.ndarray, elem_counts: np.ndarray | None):
@@ -149,6 +150,16 @@ class Digest:
         self.dd_block_size = dd_block_size
         self.filters = np.ascontiguousarray(filters, dtype=np.uint8).reshape(-1)
         self.elem_counts = None if elem_counts is None else np.ascontiguousarray(elem_counts, dtype=np.uint16)
+        self.fastmode = False
+
+    def fast(self) -> "Digest":
+        """sdbf::fast (sdbf/sdbf_class.cc:425-439): fold each filter into its
+        first 64 bytes (bloom_filter::fold(2)); the other bytes are kept."""
+        f = self.filters.reshape(-1, 256).view(np.uint64)
+        folded = f[:, 0:8] | f[:, 8:16] | f[:, 16:24] | f[:, 24:32]
+        f[:, 0:8] = folded
+        self.fastmode = True
+        return self
 
     def _desc(self, keep: list) -> DigestDesc:
         name = self.name.encode()
@@ -218,6 +229,12 @@ class DeviceSet:
 
     def __len__(self):
         return len(self.digests)
+
+    def fast(self, first: int = 0, count: int | None = None) -> "DeviceSet":
+        """sdbf::fast on digests [first, first+count): fold to 64 bytes on the device."""
+        n = len(self.digests) - first if count is None else count
+        self.ctx._check(lib().sdbfg_set_fast(self.ctx.h, self.h, first, n))
+        return self
 
     def close(self):
         if getattr(self, "h", None):
@@ -359,7 +376,19 @@ class Context:
 
     # ---------------------------------------------------------- compare
     def upload(self, digests: list[Digest]) -> DeviceSet:
-        return DeviceSet(self, digests)
+        """Resident set; digests folded with Digest.fast() keep their fast mode."""
+        ds = DeviceSet(self, digests)
+        i, n = 0, len(digests)
+        while i < n:
+            if digests[i].fastmode:
+                j = i
+                while j < n and digests[j].fastmode:
+                    j += 1
+                ds.fast(i, j - i)
+                i = j
+            else:
+                i += 1
+        return ds
 
     def compare_all(self, s: DeviceSet) -> np.ndarray:
         n = len(s)
@@ -544,6 +573,10 @@ class sdbf:  # noqa: N801 -- the reference's class name
     def get_elem_count(s: "sdbf", index: int) -> int:
         return s._d.elem_count(index)
 
+    def fast(self) -> None:
+        """sdbf::fast (sdbf/sdbf_class.cc:425-439): destructive fold to 64-byte filters."""
+        self._d.fast()
+
     def compare(self, other: "sdbf", sample: int = 0) -> int:
         """sdbf::compare (sdbf/sdbf_class.cc:266); sample must be 0."""
         if sample:
@@ -619,8 +652,9 @@ class sdbf_set:  # noqa: N801
 
     def compare_all_quiet(self, threshold: int = 1, thread_count: int = 0, fast: bool = False) -> str:
         """sdbf_set::compare_all_quiet (sdbf/sdbf_set.cc:278-308), in set order."""
-        if fast:
-            raise NotImplementedError("--fast folding is not supported")
+        if fast:  # sdbf_set.cc:284-289: every item folded first (destructive)
+            for s in self.items:
+                s.fast()
         n = len(self.items)
         if n < 2:
             return ""
@@ -637,8 +671,16 @@ class sdbf_set:  # noqa: N801
     def compare_to_quiet(self, other: "sdbf_set", threshold: int = 1, sample_size: int = 0, thread_count: int = 0,
                          fast: bool = False) -> str:
         """sdbf_set::compare_to_quiet (sdbf/sdbf_set.cc:360-394), in set order."""
-        if sample_size or fast:
-            raise NotImplementedError("sampling / --fast are not supported")
+        if sample_size:
+            raise NotImplementedError("sampling (random, unpinned in the reference) is not supported")
+        if fast:
+            # sdbf_set.cc:369-378 folds this set's items twice (the first loop
+            # runs over other->size() indices of this set: at() throws when the
+            # other set is larger) and leaves the other set unfolded
+            if len(other.items) > len(self.items):
+                raise IndexError("sdbf_set::compare_to with fast: other set larger than this set")
+            for s in self.items:
+                s.fast()
         if not self.items or not other.items:
             return ""
         ctx = default_context()

@@ -78,6 +78,16 @@ extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint3
     return SDBFG_OK;
 }
 
+extern "C" int sdbfg_set_fast(sdbfg_ctx* c, sdbfg_set* s, uint32_t first, uint32_t count) {
+    if (!c || !s || first > s->n || count > s->n - first) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    if (!count) return SDBFG_OK;
+    TIMED_LAUNCH(c, "k_fold", launch_fold(s->d_filters.as<uint32_t>(), s->d_meta.as<uint32_t>(),
+                                          s->d_digests.as<CmpDigest>(), first, count, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return SDBFG_OK;
+}
+
 extern "C" void sdbfg_set_free(sdbfg_set* s) {
     if (!s) return;
     cudaSetDevice(s->ctx->device);
@@ -125,6 +135,7 @@ static int run_pairs(sdbfg_ctx* c, const sdbfg_set* a, const sdbfg_set* b, const
     P.npairs = pairs.size();
     P.scores = c->d_scores.as<int32_t>();
     P.cutoffs = c->d_cut.as<uint16_t>();
+    P.cutoffs64 = c->d_cut64.as<uint16_t>();
     const uint32_t grid = (uint32_t)std::min<uint64_t>(pairs.size(), (uint64_t)c->sms * 16);
     TIMED_LAUNCH(c, "k_compare_pairs", launch_compare_pairs(P, std::max(1u, grid), st));
     CUDA_TRY(c, cudaMemcpyAsync(out, c->d_scores.p, pairs.size() * 4, cudaMemcpyDeviceToHost, st));
@@ -320,6 +331,7 @@ static MatParams plan_params(sdbfg_ctx* c, const MatPlan* p, const sdbfg_set* a,
     P.mode = p->mode;
     P.n = p->mode == kMatModeAll ? a->n : b->n;
     P.cutoffs = c->d_cut.as<uint16_t>();
+    P.cutoffs64 = c->d_cut64.as<uint16_t>();
     return P;
 }
 

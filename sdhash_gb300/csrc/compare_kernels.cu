@@ -167,14 +167,37 @@ __device__ __forceinline__ uint32_t cut_for(const uint16_t* cut_sum, const uint1
     return sum < 1024 ? cut_sum[sum] : cut256[4096u / sum];
 }
 
-// A filter's maximum against one target, packed: 0xFFFFFFFF = -1 (no target
-// filter with >= 16 elements), else (num << 16) | den for num/den (0/1 = 0).
-constexpr uint32_t kMaxNone = 0xFFFFFFFFu;
+// A filter's maximum against one target as the reference's double:
+// -1 when no target filter has >= 16 elements, else num / den (den is the
+// reference's uint32 max_est - cut, which wraps when the hamming weights do
+// not describe the compared bits -- mixed --fast comparisons).
+__device__ __forceinline__ double max_value(bool active, uint32_t bnum, uint32_t bden, bool counted) {
+    if (!active) return 0.0;
+    if (!counted) return -1.0;
+    return bnum == 0 ? 0.0 : __ddiv_rn((double)bnum, (double)bden);
+}
 
-__device__ __forceinline__ double unpack_max(uint32_t v) {
-    if (v == kMaxNone) return -1.0;
-    const uint32_t num = v >> 16, den = v & 0xFFFFu;
-    return num == 0 ? 0.0 : __ddiv_rn((double)num, (double)den);
+// popcount(a & t) over the first 16 words (64 bytes) for two targets, and
+// the 8-word partial counts for the fast-mode stage test.
+__device__ __forceinline__ void and_popc_16x2(const uint32_t (&a)[64], const uint32_t* t0, const uint32_t* t1,
+                                              uint32_t& h0, uint32_t& f0, uint32_t& h1, uint32_t& f1) {
+    const uint4* u0 = reinterpret_cast<const uint4*>(t0);
+    const uint4* u1 = reinterpret_cast<const uint4*>(t1);
+    uint32_t c0 = 0, c1 = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const uint4 v0 = u0[q], v1 = u1[q];
+        c0 += __popc(a[4 * q] & v0.x) + __popc(a[4 * q + 1] & v0.y) + __popc(a[4 * q + 2] & v0.z) +
+              __popc(a[4 * q + 3] & v0.w);
+        c1 += __popc(a[4 * q] & v1.x) + __popc(a[4 * q + 1] & v1.y) + __popc(a[4 * q + 2] & v1.z) +
+              __popc(a[4 * q + 3] & v1.w);
+        if (q == 1) {
+            h0 = c0;
+            h1 = c1;
+        }
+    }
+    f0 = c0;
+    f1 = c1;
 }
 
 __device__ __forceinline__ uint64_t out_index(const MatParams& P, bool ref_side1, uint32_t ref, uint32_t tgt) {
@@ -198,10 +221,13 @@ __device__ __forceinline__ int32_t final_score(double sum, uint32_t n1, uint32_t
 __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
     __shared__ __align__(16) uint32_t tf[kTgtTile][64];
     __shared__ uint32_t tmeta[kTgtTile];
-    __shared__ uint16_t cut_tab[SDBF_CUTOFF_BINS];
+    __shared__ uint16_t cut_tab[SDBF_CUTOFF_BINS], cut64_tab[SDBF_CUTOFF_BINS];
     __shared__ double msc[kCmpThreads];
     __shared__ uint32_t sparse_flag[kCmpThreads];
-    for (uint32_t i = threadIdx.x; i < SDBF_CUTOFF_BINS; i += blockDim.x) cut_tab[i] = P.cutoffs[i];
+    for (uint32_t i = threadIdx.x; i < SDBF_CUTOFF_BINS; i += blockDim.x) {
+        cut_tab[i] = P.cutoffs[i];
+        cut64_tab[i] = P.cutoffs64[i];
+    }
     __syncthreads();
     for (uint64_t pr = blockIdx.x; pr < P.npairs; pr += gridDim.x) {
         const CmpPair pair = P.pairs[pr];
@@ -213,6 +239,7 @@ __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
         const uint32_t* __restrict__ ma = P.meta[sa];
         const uint32_t* __restrict__ mb = P.meta[sb];
         const uint32_t n1 = pair.n1;  // filters of A used (== A.nfilters, sampling not applied here)
+        const bool fastA = (A.flags & kDigestFast) != 0;  // the reference digest's fastmode decides
         double sum = -1.0;
         uint32_t sparse = 0;
         for (uint32_t c0 = 0; c0 < n1; c0 += blockDim.x) {
@@ -232,8 +259,9 @@ __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
                 }
             }
             const bool active = have && s1 >= (uint32_t)kMinElem;
-            // best = num/den; den == 0 means "no target counted yet" (-1)
-            uint32_t bnum = 0, bden = 0;
+            // best = num/den; counted: a target filter with >= 16 elements was seen
+            uint32_t bnum = 0, bden = 1;
+            bool counted = false;
             for (uint32_t j0 = 0; j0 < B.nfilters; j0 += kTgtTile) {
                 const uint32_t nt = min((uint32_t)kTgtTile, B.nfilters - j0);
                 __syncthreads();
@@ -251,26 +279,32 @@ __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
                         if (s2 < (uint32_t)kMinElem) continue;
                         const uint32_t e2 = meta >> 16;
                         const uint32_t max_est = min(e1, e2);
-                        const uint32_t cut = cut_tab[4096u / (s1 + s2)];
-                        const uint32_t match = and_popc_hs(a, &tf[j][0]);
-                        uint32_t num = 0, den = 1;
-                        if (match > cut && !staged_exit(a, &tf[j][0], cut)) {
-                            num = match - cut;
-                            den = max_est - cut;
+                        uint32_t cut, match;
+                        if (!fastA) {
+                            cut = cut_tab[4096u / (s1 + s2)];
+                            match = and_popc_hs(a, &tf[j][0]);
+                            if (match > cut && staged_exit(a, &tf[j][0], cut)) match = 0;
+                        } else {  // bf_bitcount_cut_64 (bf_utils.cc:78-110) on the folded 64 bytes
+                            cut = cut64_tab[1024u / (s1 + s2)];
+                            uint32_t h8, h16, u8, u16;
+                            and_popc_16x2(a, &tf[j][0], &tf[j][0], h8, h16, u8, u16);
+                            match = (2 * h8 + 48 < cut) ? 0u : h16;
                         }
-                        if (bden == 0 || (uint64_t)num * bden > (uint64_t)bnum * den) {
+                        uint32_t num = 0, den = 1;
+                        if (match > cut) {
+                            num = match - cut;
+                            den = max_est - cut;  // uint32 as in the reference
+                        }
+                        if (!counted || (uint64_t)num * bden > (uint64_t)bnum * den) {
                             bnum = num;
                             bden = den;
+                            counted = true;
                         }
                     }
                 }
             }
             if (have) {
-                double m;
-                if (!active) m = 0.0;
-                else if (bden == 0) m = -1.0;
-                else m = __ddiv_rn((double)bnum, (double)bden);
-                msc[threadIdx.x] = m;
+                msc[threadIdx.x] = max_value(active, bnum, bden, counted);
                 sparse_flag[threadIdx.x] = s1 < (uint32_t)kMinElem;
             }
             __syncthreads();
@@ -295,6 +329,38 @@ __global__ void __launch_bounds__(kCmpThreads) k_compare_pairs(CmpParams P) {
     }
 }
 
+// One warp per filter: 16 lanes fold words k, k+16, k+32, k+48 into word k
+// (bloom_filter::fold(2), bloom_filter.cc:262-288: two halvings by OR),
+// write the folded 64 bytes over the first 64, and the hamming weight of
+// the folded filter goes into the meta word (sdbf::fast, sdbf_class.cc:425-439).
+__global__ void k_fold(uint32_t* __restrict__ filters, uint32_t* __restrict__ meta, CmpDigest* digests,
+                       uint32_t first, uint32_t count) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t f0 = digests[first].first;
+    const uint32_t f1 = digests[first + count - 1].first + digests[first + count - 1].nfilters;
+    for (uint32_t f = f0 + warp; f < f1; f += nwarps) {
+        uint32_t* w = filters + (size_t)f * 64;
+        uint32_t v = 0;
+        if (lane < 16) v = w[lane] | w[lane + 16] | w[lane + 32] | w[lane + 48];
+        __syncwarp();
+        if (lane < 16) w[lane] = v;
+        uint32_t h = __popc(v);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) h += __shfl_xor_sync(0xffffffffu, h, d);
+        if (lane == 0) meta[f] = (h << 16) | (meta[f] & 0xFFFFu);
+    }
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    for (uint32_t d = gt; d < count; d += gridDim.x * blockDim.x) digests[first + d].flags |= kDigestFast;
+}
+
+cudaError_t launch_fold(uint32_t* filters, uint32_t* meta, CmpDigest* digests, uint32_t first, uint32_t count,
+                        cudaStream_t st) {
+    if (count) k_fold<<<512, 256, 0, st>>>(filters, meta, digests, first, count);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_compare_pairs(const CmpParams& P, uint32_t grid, cudaStream_t st) {
     if (P.npairs) k_compare_pairs<<<grid, kCmpThreads, 0, st>>>(P);
     return cudaGetLastError();
@@ -314,10 +380,12 @@ struct MatSmem {
     uint32_t tinfo[TJ];           // local target index | completion index << 16 | last << 31
     uint32_t gidx[TJ];            // global filter index per slot
     uint32_t comp[TJ];            // local target index of the k-th completed target
-    uint32_t mv[R][TJ + 1];       // per row and completed target: packed maximum
+    double mv[R][TJ + 1];         // per row and completed target: the filter's maximum
     double run[kMatMaxTargets];   // running sums per target of the unit
-    uint16_t cut_sum[1024];
+    uint16_t cut_sum[1024];       // CUTOFFS256[4096 / (s1 + s2)] by s1 + s2
+    uint16_t cut64_sum[1024];     // CUTOFFS64[1024 / (s1 + s2)] by s1 + s2
     uint16_t cut256[SDBF_CUTOFF_BINS];
+    uint16_t cut64[SDBF_CUTOFF_BINS];
     MatUnit unit;
     uint32_t unit_id, ntile, ncomp, cur_t, cur_f, sparse;
 };
@@ -327,9 +395,14 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
     extern __shared__ __align__(16) uint8_t mat_smem[];
     MatSmem<R, TJ>& S = *reinterpret_cast<MatSmem<R, TJ>*>(mat_smem);
     const uint32_t tid = threadIdx.x, lane = tid & 31;
-    for (uint32_t i = tid; i < 1024; i += R)
+    for (uint32_t i = tid; i < 1024; i += R) {
         S.cut_sum[i] = P.cutoffs[i >= 32 ? 4096u / i : (uint32_t)SDBF_CUTOFF_BINS - 1];
-    for (uint32_t i = tid; i < SDBF_CUTOFF_BINS; i += R) S.cut256[i] = P.cutoffs[i];
+        S.cut64_sum[i] = P.cutoffs64[i >= 8 ? 1024u / i : (uint32_t)SDBF_CUTOFF_BINS - 1];
+    }
+    for (uint32_t i = tid; i < SDBF_CUTOFF_BINS; i += R) {
+        S.cut256[i] = P.cutoffs[i];
+        S.cut64[i] = P.cutoffs64[i];
+    }
     for (;;) {
         __syncthreads();
         if (tid == 0) {
@@ -343,6 +416,7 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
         const uint32_t rs = U.flags & kUnitRefSide1 ? 1 : 0, ts = U.flags & kUnitTgtSide1 ? 1 : 0;
         const bool split = (U.flags & kUnitSplit) != 0;
         const CmpDigest A = P.digests[rs][U.ref];
+        const bool fastA = (A.flags & kDigestFast) != 0;  // the reference digest's fastmode decides
         const uint32_t nT = U.t1 - U.t0;
         for (uint32_t k = tid; k < nT && !split; k += R) S.run[k] = -1.0;
         if (tid == 0) S.sparse = 0;
@@ -373,7 +447,8 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
                 S.cur_t = 0;
                 S.cur_f = 0;
             }
-            uint32_t bnum = 0, bden = 0;  // bden == 0: no counted target filter yet
+            uint32_t bnum = 0, bden = 1;  // best fraction so far
+            bool counted = false;          // a target filter with >= 16 elements was seen
             const uint32_t nrows = min((uint32_t)R, U.r1 - rc);
             __syncthreads();
             for (;;) {
@@ -435,50 +510,72 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
                 }
                 __syncthreads();
                 // ---- every row against the tile, two target filters at a time
-                auto consume = [&](uint32_t j, uint32_t match) {
+                // consume(j, count, h8): count = full 2048-bit count (normal mode) or
+                // the 64-byte count (fast mode, h8 = its first 32 bytes)
+                auto consume = [&](uint32_t j, uint32_t cnt, uint32_t h8) {
                     const uint32_t tm = S.tmeta[j];
                     const uint32_t s2 = tm & 0xFFFFu;
                     if (active && s2 >= (uint32_t)kMinElem) {
-                        const uint32_t cut = cut_for(S.cut_sum, S.cut256, s1, s2);
-                        uint32_t num = 0, den = 1;
-                        if (match > cut && !staged_exit(a, &S.tf[j][0], cut)) {
-                            num = match - cut;
-                            den = min(e1, tm >> 16) - cut;
+                        uint32_t cut, match = cnt;
+                        if (!fastA) {
+                            cut = cut_for(S.cut_sum, S.cut256, s1, s2);
+                            if (match > cut && staged_exit(a, &S.tf[j][0], cut)) match = 0;
+                        } else {
+                            const uint32_t sum = s1 + s2;
+                            cut = sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum];
+                            if (2 * h8 + 48 < cut) match = 0;
                         }
-                        if (bden == 0 || (uint64_t)num * bden > (uint64_t)bnum * den) {
+                        uint32_t num = 0, den = 1;
+                        if (match > cut) {
+                            num = match - cut;
+                            den = min(e1, tm >> 16) - cut;  // uint32 as in the reference
+                        }
+                        if (!counted || (uint64_t)num * bden > (uint64_t)bnum * den) {
                             bnum = num;
                             bden = den;
+                            counted = true;
                         }
                     }
                     const uint32_t info = S.tinfo[j];
                     if (info & 0x80000000u) {
-                        const uint32_t packed = !active ? 1u : (bden == 0 ? kMaxNone : (bnum << 16) | bden);
+                        const double m = max_value(active, bnum, bden, counted);
                         if (split) {
-                            if (have) P.slots[P.split[U.split].slot_base + row] = unpack_max(packed);
+                            if (have) P.slots[P.split[U.split].slot_base + row] = m;
                         } else {
-                            S.mv[tid][(info >> 16) & 0x7FFFu] = packed;
+                            S.mv[tid][(info >> 16) & 0x7FFFu] = m;
                         }
                         bnum = 0;
-                        bden = 0;
+                        bden = 1;
+                        counted = false;
                     }
                 };
                 uint32_t j = 0;
-                for (; j + 1 < nt; j += 2) {
-                    uint32_t m0 = 0, m1 = 0;
-                    if (active) and_popc_hs2(a, &S.tf[j][0], &S.tf[j + 1][0], m0, m1);
-                    consume(j, m0);
-                    consume(j + 1, m1);
+                if (!fastA) {
+                    for (; j + 1 < nt; j += 2) {
+                        uint32_t m0 = 0, m1 = 0;
+                        if (active) and_popc_hs2(a, &S.tf[j][0], &S.tf[j + 1][0], m0, m1);
+                        consume(j, m0, 0);
+                        consume(j + 1, m1, 0);
+                    }
+                    if (j < nt) consume(j, active ? and_popc_hs(a, &S.tf[j][0]) : 0u, 0);
+                } else {
+                    for (; j < nt; j += 2) {
+                        const uint32_t j1 = j + 1 < nt ? j + 1 : j;
+                        uint32_t h0 = 0, f0 = 0, h1 = 0, f1 = 0;
+                        if (active) and_popc_16x2(a, &S.tf[j][0], &S.tf[j1][0], h0, f0, h1, f1);
+                        consume(j, f0, h0);
+                        if (j + 1 < nt) consume(j + 1, f1, h1);
+                    }
                 }
-                if (j < nt) consume(j, active ? and_popc_hs(a, &S.tf[j][0]) : 0u);
                 __syncthreads();
                 // ---- fold the completed targets' maxima in filter order
                 if (!split) {
                     for (uint32_t k = tid; k < S.ncomp; k += R) {
                         double sum = S.run[S.comp[k]];
                         for (uint32_t r = 0; r < nrows; r++) {
-                            const uint32_t v = S.mv[r][k];
-                            if (sum < 0) sum = unpack_max(v);
-                            else if (v != 1u) sum = __dadd_rn(sum, unpack_max(v));
+                            const double m = S.mv[r][k];
+                            if (sum < 0) sum = m;
+                            else if (m != 0.0) sum = __dadd_rn(sum, m);
                         }
                         S.run[S.comp[k]] = sum;
                     }

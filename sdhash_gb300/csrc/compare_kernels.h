@@ -12,7 +12,9 @@ constexpr int kCmpThreads = 128;
 struct CmpDigest {
     uint32_t first;
     uint32_t nfilters;
+    uint32_t flags;  // kDigestFast: filters folded to 64 bytes (sdbf::fast)
 };
+constexpr uint32_t kDigestFast = 1u;
 
 // One scored pair after the swap rule: `ref` is the side whose filters are
 // summed (sdbf_1 after the swap in sdbf_core.cc:351-359).
@@ -32,9 +34,15 @@ struct CmpParams {
     uint64_t npairs;
     int32_t* scores;           // per pair
     const uint16_t* cutoffs;   // CUTOFFS256
+    const uint16_t* cutoffs64; // CUTOFFS64 (fast mode)
 };
 
 cudaError_t launch_compare_pairs(const CmpParams& P, uint32_t grid, cudaStream_t st);
+// sdbf::fast on digests [first, first+count) of a set: fold every filter's
+// 256 bytes into its first 64 (the other bytes unchanged), hamming of the
+// folded bytes, fast flag on.
+cudaError_t launch_fold(uint32_t* filters, uint32_t* meta, CmpDigest* digests, uint32_t first, uint32_t count,
+                        cudaStream_t st);
 
 }  // namespace sdbfg
 
@@ -83,6 +91,7 @@ struct MatParams {
     uint32_t mode;             // kMatModeAll: n*(n-1)/2 pair order; kMatModeCross: q*nt+t
     uint32_t n;                // set size (all) / number of targets (cross)
     const uint16_t* cutoffs;   // CUTOFFS256
+    const uint16_t* cutoffs64; // CUTOFFS64 (fast mode)
 };
 
 // Kernel variants (rows per CTA x target filters per shared-memory tile),

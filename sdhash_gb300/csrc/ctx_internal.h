@@ -96,7 +96,7 @@ struct sdbfg_ctx {
     int sms = 152;
     uint32_t lead = kDefaultLead;
     // constant tables
-    DevBuf d_rank, d_ent, d_cut;
+    DevBuf d_rank, d_ent, d_cut, d_cut64;
     // generation buffers
     DevBuf d_data, d_chunks, d_tiles, d_files, d_order, d_tile_out, d_features, d_work_filters, d_info, d_counters,
         d_pack_src, d_pack_dst_off, d_out_filters, d_out_counts;

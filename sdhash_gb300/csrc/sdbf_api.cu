@@ -38,13 +38,15 @@ extern "C" int sdbfg_ctx_create(int device, sdbfg_ctx** out) {
     uint32_t ent[65];
     for (int i = 0; i < 65; i++) ent[i] = SDBF_ENTROPY64[i];
     if (c->d_rank.ensure(sizeof(SDBF_ENTR64_RANKS)) || c->d_ent.ensure(sizeof(ent)) ||
-        c->d_cut.ensure(sizeof(SDBF_CUTOFFS256)) || c->d_counters.ensure(64)) {
+        c->d_cut.ensure(sizeof(SDBF_CUTOFFS256)) || c->d_cut64.ensure(sizeof(SDBF_CUTOFFS64)) ||
+        c->d_counters.ensure(64)) {
         sdbfg_ctx_destroy(c);
         return SDBFG_ERR_NOMEM;
     }
     cudaMemcpy(c->d_rank.p, SDBF_ENTR64_RANKS, sizeof(SDBF_ENTR64_RANKS), cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_ent.p, ent, sizeof(ent), cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_cut.p, SDBF_CUTOFFS256, sizeof(SDBF_CUTOFFS256), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_cut64.p, SDBF_CUTOFFS64, sizeof(SDBF_CUTOFFS64), cudaMemcpyHostToDevice);
     cudaMemset(c->d_counters.p, 0, 64);
     *out = c;
     return SDBFG_OK;
@@ -55,7 +57,7 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
     cudaSetDevice(c->device);
     for (MatPlan* p : c->plans) delete p;
     c->plans.clear();
-    for (DevBuf* b : {&c->d_rank, &c->d_ent, &c->d_cut, &c->d_data, &c->d_chunks, &c->d_tiles, &c->d_files,
+    for (DevBuf* b : {&c->d_rank, &c->d_ent, &c->d_cut, &c->d_cut64, &c->d_data, &c->d_chunks, &c->d_tiles, &c->d_files,
                       &c->d_order, &c->d_tile_out, &c->d_features, &c->d_work_filters, &c->d_info,
                       &c->d_counters, &c->d_pack_src, &c->d_pack_dst_off, &c->d_out_filters, &c->d_out_counts,
                       &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase,

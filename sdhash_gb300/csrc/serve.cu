@@ -179,6 +179,7 @@ static cudaError_t launch_batch(sdbfg_server* sv, sdbfg_server::Slot& S) {
     P.mode = kMatModeCross;
     P.n = nt;
     P.cutoffs = sv->ctx->d_cut.as<uint16_t>();
+    P.cutoffs64 = sv->ctx->d_cut64.as<uint16_t>();
     const uint32_t grid = (uint32_t)std::min<uint64_t>(ctas, std::max(1u, S.nunits));
     if ((e = launch_matrix(P, sv->ctx->mat_variant, grid, st))) return e;
     if ((e = launch_matrix_finalize(P, st))) return e;

@@ -75,10 +75,40 @@ def main():
     out["plain_small"] = {"seed": 1, "names": names, "sha256": [sha(t) for t in texts],
                           "compare_all_t1": cmp_all, "dd_sha256": [sha(t) for t in dd_texts],
                           "compare_to_dd_vs_stream_t1": cmp_to, "compare_all_dd_tneg1": cmp_all_neg}
+    add_fast(R, out)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=0, sort_keys=True)
     print("wrote golden.json:", len(out["digests"]), "digests,", len(cmp_all.splitlines()), "compare lines")
 
 
+def add_fast(R, out):
+    """--fast results of the reference on the plain small set: all pairs of
+    the stream digests, the stream digests (queries, folded by the reference)
+    against the block digests (targets, left unfolded: compare_to folds only
+    the query set, sdbf/sdbf_set.cc:321-331), all pairs of the block digests."""
+    names, files = synth.plain_small_set(seed=1)
+    texts = [R.digest(n, f.tobytes(), 0) for n, f in zip(names, files)]
+    dd_texts = [R.digest(n + ".dd", f.tobytes(), 16384) for n, f in zip(names[:8], files[:8])]
+    with tempfile.TemporaryDirectory() as td:
+        p = os.path.join(td, "set.sdbf")
+        with open(p, "w") as f:
+            f.write("".join(texts))
+        q = os.path.join(td, "q.sdbf")
+        with open(q, "w") as f:
+            f.write("".join(dd_texts))
+        out["plain_small"]["compare_all_fast_t1"] = R.compare_all_file(p, 1, fast=True)
+        out["plain_small"]["compare_to_fast_stream_vs_dd_t1"] = R.compare_to_files(p, q, 1, fast=True)
+        out["plain_small"]["compare_all_dd_fast_tneg1"] = R.compare_all_file(q, -1, fast=True)
+
+
 if __name__ == "__main__":
-    main()
+    if "--fast-only" in sys.argv:   # add the --fast results to an existing golden.json
+        path = os.path.join(HERE, "golden.json")
+        with open(path) as f:
+            g = json.load(f)
+        add_fast(Reference(), g)
+        with open(path, "w") as f:
+            json.dump(g, f, indent=0, sort_keys=True)
+        print("added --fast results to golden.json")
+    else:
+        main()

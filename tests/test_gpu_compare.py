@@ -72,3 +72,36 @@ def test_score_pairs_and_single_compare(ctx, oracle, plain_set):
     od = [oracle.parse(d.to_string()) for d in dd]
     for k in range(300):
         assert got[k] == oracle.score(os_[ia[k]], od[ib[k]])
+
+
+def test_fast_mode_matches_reference(plain_set, golden):
+    """--fast on the GPU (fold kernel, CUTOFFS64, 64-byte counts; the
+    reference digest's fastmode decides each pair) against the reference."""
+    g, names, files, stream, dd = plain_set
+    import copy
+    s, q = g.sdbf_set(), g.sdbf_set()
+    for d in stream:
+        s.add(g.sdbf(_digest=copy.deepcopy(d)))
+    for d in dd:
+        q.add(g.sdbf(_digest=copy.deepcopy(d)))
+    gp = golden["plain_small"]
+    assert s.compare_all_quiet(1, 0, True) == gp["compare_all_fast_t1"]
+    assert s.compare_to_quiet(q, 1, 0, 0, True) == gp["compare_to_fast_stream_vs_dd_t1"]
+    assert q.compare_all_quiet(-1, 0, True) == gp["compare_all_dd_fast_tneg1"]
+
+
+def test_fast_mode_device_fold_both_paths(ctx, oracle, plain_set):
+    """Device-side fold of a resident set; batched engine and per-pair path
+    agree with the oracle, mixed folded / unfolded pairs included."""
+    g, names, files, stream, dd = plain_set
+    ds = stream[:20] + dd
+    dev = ctx.upload(ds)
+    dev.fast(0, 10)           # fold the first ten stream digests only
+    dev.fast(20, 4)           # and half the block digests
+    ods = [oracle.parse(d.to_string()) for d in ds]
+    for k in list(range(10)) + list(range(20, 24)):
+        oracle.fast(ods[k])
+    want = oracle.score_all_matrix(ods)
+    iu = np.triu_indices(len(ds), 1)
+    assert np.array_equal(ctx.compare_all(dev), want[iu])
+    assert np.array_equal(ctx.score_pairs(dev, dev, iu[0], iu[1]), want[iu])

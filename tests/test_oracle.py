@@ -111,3 +111,20 @@ def test_staged_popcount_cut_semantics(oracle):
         a[i] = b[i] = 0xFF
     assert oracle.L.orc_match_cut(bytes(a), bytes(b), 200) == 0
     assert oracle.L.orc_match_cut(bytes(a), bytes(b), 100) == 8 + 13 * 8
+
+
+def test_oracle_fast_mode_matches_reference(oracle, golden):
+    """--fast (sdbf::fast folding, CUTOFFS64, 64-byte count) against the
+    reference's own --fast results, including its compare_to rule that folds
+    only the query set."""
+    g = golden["plain_small"]
+    names, files = synth.plain_small_set(seed=g["seed"])
+    stream = [oracle.parse(oracle.digest(n, f.tobytes(), 0).to_string()) for n, f in zip(names, files)]
+    dd = [oracle.parse(oracle.digest(n + ".dd", f.tobytes(), 16384).to_string()) for n, f in zip(names[:8], files[:8])]
+    for d in stream:
+        oracle.fast(d)
+    assert oracle.compare_all(stream, 1) == g["compare_all_fast_t1"]
+    assert oracle.compare_to(stream, dd, 1) == g["compare_to_fast_stream_vs_dd_t1"]
+    for d in dd:
+        oracle.fast(oracle.fast(d))  # folding twice changes nothing
+    assert oracle.compare_all(dd, -1) == g["compare_all_dd_fast_tneg1"]
