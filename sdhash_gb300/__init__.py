@@ -38,6 +38,14 @@ class SdbfError(Exception):
         self.code = code
 
 
+class EngineError(RuntimeError):
+    """A C-ABI call returned a status code (``code``: SDBFG_ERR_*)."""
+
+    def __init__(self, code: int, msg: str = ""):
+        super().__init__(f"sdbf_gb300 error {code}: {msg}")
+        self.code = code
+
+
 class DigestResult(C.Structure):
     _fields_ = [("bf_count", C.c_uint32), ("last_count", C.c_uint32), ("status", C.c_int32),
                 ("reserved", C.c_uint32), ("filter_offset", C.c_uint64)]
@@ -271,7 +279,7 @@ class Context:
 
     def _check(self, rc: int):
         if rc != 0:
-            raise RuntimeError(f"sdbf_gb300 error {rc}: {lib().sdbfg_last_error(self.h).decode()}")
+            raise EngineError(rc, lib().sdbfg_last_error(self.h).decode())
 
     def set_stream(self, stream_handle: int | None):
         """Launch on this CUDA stream (a torch.cuda.Stream's cuda_stream).  None:

@@ -92,7 +92,8 @@ def test_server_rejects_oversized_query(ctx, serve_data):
     srv = g.Server(ctx, tset, slots=1, max_batch_queries=4, memory_budget=1 << 20)
     try:
         big = g.Digest("big", 0, 5000, 160, 160, 0, np.zeros(5000 * 256, np.uint8), None)
-        with pytest.raises(g.SdbfError):
+        with pytest.raises(g.EngineError) as e:
             srv.submit(big, 1)
+        assert e.value.code == -5  # SDBFG_ERR_CAPACITY
     finally:
         srv.close()
