@@ -13,12 +13,16 @@
 //  * sdbf_set does not own its items (sdbf_set.cc:76-85);
 //  * result lines "a<sep>b<sep>%03d" (-1 unpadded) for scores >= threshold,
 //    pairs in set order (sdbf_set.cc:239-394).
+//  * fast() folds the filters in place (first 64 bytes of each, hamming of
+//    the folded bytes) and switches the digest to fast-mode scoring
+//    (sdbf_class.cc:425-439); compare_all(fast) folds every item,
+//    compare_to(fast) only this set's items (sdbf_set.cc:284-289, 321-331).
 // Differences: comparisons run on the device in one batched launch per
 // call (so compare_all output is in set order rather than OpenMP order), the
 // thread_count argument only matters for the reference's CPU loop, and
 // filter sampling (sample > 0, seeded from time() in the reference and hence
-// not reproducible) and --fast folding are not offered: those calls fall
-// back to the full comparison and report it on stderr.
+// not reproducible) is not offered: such calls fall back to the full
+// comparison and report it on stderr.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -214,7 +218,37 @@ int32_t sdbf::get_elem_count(sdbf* mine, uint64_t index) {
     return mine->elem_counts[index];
 }
 
-void sdbf::fast() { fprintf(stderr, "sdbf: --fast folding is not offered by this engine; full filters kept\n"); }
+void sdbf::fast() {
+    // bloom_filter::fold(2) (bloom_filter.cc:262-288): OR the halves twice;
+    // only the folded 64 bytes are copied back over the filter
+    for (uint32_t i = 0; i < bf_count; i++) {
+        uint64_t w[32];
+        memcpy(w, buffer + (uint64_t)i * 256, 256);
+        uint32_t h = 0;
+        for (int j = 0; j < 8; j++) {
+            w[j] |= w[j + 8] | w[j + 16] | w[j + 24];
+            h += (uint32_t)__builtin_popcountll(w[j]);
+        }
+        memcpy(buffer + (uint64_t)i * 256, w, 64);
+        hamming[i] = (uint16_t)h;
+    }
+    fastmode = true;
+}
+
+// digests of a freshly uploaded set that were folded on the host keep their
+// fast mode on the device (folding again changes nothing)
+void sdbf_set::mark_fast(sdbfg_ctx* c, sdbfg_set* set, const std::vector<sdbf*>& items) {
+    for (uint32_t i = 0; i < items.size();) {
+        if (!items[i]->fastmode) {
+            i++;
+            continue;
+        }
+        uint32_t j = i;
+        while (j < items.size() && items[j]->fastmode) j++;
+        if (sdbfg_set_fast(c, set, i, j - i) != SDBFG_OK) throw -1;
+        i = j;
+    }
+}
 
 int32_t sdbf::compare(sdbf* other, uint32_t sample) {
     if (sample) fprintf(stderr, "sdbf: filter sampling is not offered; comparing all filters\n");
@@ -226,6 +260,8 @@ int32_t sdbf::compare(sdbf* other, uint32_t sample) {
                  other->orig_file_size, other->hashname, other->buffer)};
     sdbfg_set* s = nullptr;
     if (sdbfg_set_upload(c, d, 2, &s) != SDBFG_OK) throw -1;
+    for (uint32_t k = 0; k < 2; k++)
+        if ((k == 0 ? this : other)->fastmode && sdbfg_set_fast(c, s, k, 1) != SDBFG_OK) throw -1;
     const uint32_t ia = 0, ib = 1;
     int32_t score = -1;
     int rc = sdbfg_score_pairs(c, s, s, &ia, &ib, 1, &score);
@@ -332,6 +368,7 @@ sdbfg_set* sdbf_set::upload_items(sdbfg_ctx* c, std::vector<sdbf*>& items) {
         fprintf(stderr, "sdbf_set: upload failed: %s\n", sdbfg_last_error(c));
         throw -1;
     }
+    mark_fast(c, out, items);
     return out;
 }
 
@@ -342,7 +379,8 @@ static void put(std::ostream& out, const char* a, const char* b, char sep, int32
 }
 
 std::string sdbf_set::compare_all_quiet(int32_t threshold, int32_t, bool fast) {
-    if (fast) fprintf(stderr, "sdbf_set: --fast folding is not offered; comparing full filters\n");
+    if (fast)
+        for (sdbf* s : items) s->fast();
     std::stringstream out;
     out.fill('0');
     const uint64_t n = items.size();
@@ -365,7 +403,13 @@ void sdbf_set::compare_all(int32_t threshold, bool fast) { std::cout << compare_
 std::string sdbf_set::compare_to_quiet(sdbf_set* other, int32_t threshold, uint32_t sample_size, int32_t,
                                        bool fast) {
     if (sample_size) fprintf(stderr, "sdbf_set: filter sampling is not offered; comparing all filters\n");
-    if (fast) fprintf(stderr, "sdbf_set: --fast folding is not offered; comparing full filters\n");
+    if (fast) {
+        // sdbf_set.cc:321-331: the first loop runs over other->size() indices
+        // of this set (items.at() throws past its end), the second over this
+        // set; the other set is not folded
+        for (size_t i = 0; i < other->items.size(); i++) items.at(i)->fast();
+        for (sdbf* s : items) s->fast();
+    }
     std::stringstream out;
     out.fill('0');
     if (items.empty() || other->items.empty()) return out.str();

@@ -65,6 +65,7 @@ public:
 
 private:
     static struct sdbfg_set* upload_items(struct sdbfg_ctx* c, std::vector<class sdbf*>& items);
+    static void mark_fast(struct sdbfg_ctx* c, struct sdbfg_set* set, const std::vector<class sdbf*>& items);
     std::vector<class sdbf*> items;
     std::string setname;
     std::mutex add_hash_mutex;

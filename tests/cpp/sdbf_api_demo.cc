@@ -5,7 +5,8 @@
 // usage: sdbf_api_demo <fileA> <fileB> <set.sdbf>
 //   prints: stream digest of A, 16 KiB block digest of B, A-vs-B score,
 //   the score after a to_string() / parse round trip, then the set's
-//   compare_all_quiet(threshold 1) and the too-small throw code.
+//   compare_all_quiet(threshold 1), the same with --fast (folds the set's
+//   items), a folded digest's text, and the too-small throw code.
 #include <fstream>
 #include <iostream>
 #include <stdint.h>
@@ -28,6 +29,8 @@ int main(int argc, char** argv) {
     std::cout << "istream equal " << (a3->to_string() == a->to_string()) << "\n";
     sdbf_set* set = new sdbf_set(argv[3]);
     std::cout << set->compare_all_quiet(1, 1, false);
+    std::cout << set->compare_all_quiet(1, 1, true);
+    std::cout << set->at(0);
     char small[100] = {0};
     try {
         sdbf tiny("tiny", small, 0, sizeof small, NULL);

@@ -36,5 +36,8 @@ def test_cpp_compat_demo(tmp_path, native, oracle):
     s = oracle.score(oa, ob)
     expect += f"a vs b {s}\na2 vs b2 {s}\nistream equal 1\n"
     expect += oracle.compare_all([oracle.parse(x) for x in lines], 1)
+    folded = [oracle.fast(oracle.parse(x)) for x in lines]
+    expect += oracle.compare_all(folded, 1)
+    expect += folded[0].to_string()
     expect += "tiny throws -3\n"
     assert out == expect
