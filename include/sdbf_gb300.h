@@ -228,7 +228,9 @@ int sdbfg_compare_autotune(sdbfg_ctx *ctx, const sdbfg_set *a, const sdbfg_set *
  * sdbf/sdbf_set.cc:318-346; no counterpart as a service in the reference).
  * A worker thread admits queued query digests into batch slots (one CUDA
  * stream each) as slots free up, in arrival order, while their filters fit
- * the slot's share of memory_budget; every query is scored against every
+ * the slot's share of memory_budget and the batch's filter pairs stay within
+ * max_batch_pairs (a bound on the batch's GPU time, hence on latency); a
+ * query larger than that runs in a batch of its own.  Every query is scored against every
  * target exactly as sdbfg_compare_to would score it.  The context must not
  * be used from other threads while its server runs; the target set must
  * outlive the server. */
@@ -238,6 +240,8 @@ typedef struct {
     uint32_t max_batch_queries;  /* queries per batch (default 256) */
     uint64_t memory_budget;      /* device bytes for batches in flight (default 256 MiB) */
     int32_t threshold;           /* a target matches at score >= threshold (default 1) */
+    uint32_t pad;
+    uint64_t max_batch_pairs;    /* filter pairs per batch, i.e. GPU work per batch (0: 2^31) */
 } sdbfg_server_config;
 typedef struct {
     uint64_t tag;                /* as submitted */

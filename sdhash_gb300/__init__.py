@@ -53,7 +53,7 @@ class DigestResult(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_uint32), ("max_batch_queries", C.c_uint32), ("memory_budget", C.c_uint64),
-                ("threshold", C.c_int32)]
+                ("threshold", C.c_int32), ("pad", C.c_uint32), ("max_batch_pairs", C.c_uint64)]
 
 
 class ServerResult(C.Structure):
@@ -472,9 +472,9 @@ class Server:
     query digests from any thread, poll finished ones with their score rows."""
 
     def __init__(self, ctx: "Context", targets: DeviceSet, slots: int = 3, max_batch_queries: int = 256,
-                 memory_budget: int = 256 << 20, threshold: int = 1):
+                 memory_budget: int = 256 << 20, threshold: int = 1, max_batch_pairs: int = 1 << 31):
         self.ctx, self.targets = ctx, targets
-        cfg = ServerConfig(slots, max_batch_queries, memory_budget, threshold)
+        cfg = ServerConfig(slots, max_batch_queries, memory_budget, threshold, 0, max_batch_pairs)
         h = C.c_void_p()
         ctx._check(lib().sdbfg_server_create(ctx.h, targets.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -42,6 +42,7 @@ extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint3
     std::vector<uint32_t> meta(total);
     std::vector<uint8_t> filt(total * 256);
     s->names.resize(n);
+    s->fast.assign(n, 0);
     s->bf_count.resize(n);
     s->last_elem.resize(n);
     for (uint32_t i = 0; i < n; i++) {
@@ -78,6 +79,18 @@ extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint3
     return SDBFG_OK;
 }
 
+static void drop_plans(sdbfg_ctx* c, uint64_t serial) {
+    auto& plans = c->plans;
+    for (size_t k = 0; k < plans.size();) {
+        if (plans[k]->serial_a == serial || plans[k]->serial_b == serial) {
+            delete plans[k];
+            plans.erase(plans.begin() + k);
+        } else {
+            k++;
+        }
+    }
+}
+
 extern "C" int sdbfg_set_fast(sdbfg_ctx* c, sdbfg_set* s, uint32_t first, uint32_t count) {
     if (!c || !s || first > s->n || count > s->n - first) return SDBFG_ERR_ARG;
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -85,21 +98,15 @@ extern "C" int sdbfg_set_fast(sdbfg_ctx* c, sdbfg_set* s, uint32_t first, uint32
     TIMED_LAUNCH(c, "k_fold", launch_fold(s->d_filters.as<uint32_t>(), s->d_meta.as<uint32_t>(),
                                           s->d_digests.as<CmpDigest>(), first, count, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    for (uint32_t i = first; i < first + count; i++) s->fast[i] = 1;
+    drop_plans(c, s->serial);  // group units are formed per fast mode
     return SDBFG_OK;
 }
 
 extern "C" void sdbfg_set_free(sdbfg_set* s) {
     if (!s) return;
     cudaSetDevice(s->ctx->device);
-    auto& plans = s->ctx->plans;
-    for (size_t k = 0; k < plans.size();) {
-        if (plans[k]->serial_a == s->serial || plans[k]->serial_b == s->serial) {
-            delete plans[k];
-            plans.erase(plans.begin() + k);
-        } else {
-            k++;
-        }
-    }
+    drop_plans(s->ctx, s->serial);
     s->d_filters.release();
     s->d_meta.release();
     s->d_digests.release();
@@ -189,6 +196,10 @@ static int upload_plan(sdbfg_ctx* c, MatPlan* p, UnitBuilder& ub, const std::vec
     CUDA_TRY(c, p->d_units.ensure(std::max<size_t>(1, units.size()) * sizeof(MatUnit)));
     CUDA_TRY(c, p->d_targets.ensure(std::max<size_t>(1, targets.size()) * 4));
     CUDA_TRY(c, p->d_split.ensure(std::max<size_t>(1, ub.split.size()) * sizeof(MatSplit)));
+    CUDA_TRY(c, p->d_refs.ensure(std::max<size_t>(1, ub.refs.size()) * 4));
+    if (!ub.refs.empty())
+        CUDA_TRY(c, cudaMemcpyAsync(p->d_refs.p, ub.refs.data(), ub.refs.size() * 4, cudaMemcpyHostToDevice,
+                                    c->stream));
     CUDA_TRY(c, p->d_slots.ensure(std::max<uint64_t>(1, ub.slots) * 8));
     CUDA_TRY(c, p->d_counter.ensure(64));
     cudaStream_t st = c->stream;
@@ -221,13 +232,19 @@ static int build_plan_all(sdbfg_ctx* c, const sdbfg_set* s, MatPlan* p) {
         sum2 += (uint64_t)s->bf_count[i] * s->bf_count[i];
     }
     const uint64_t ctas = (uint64_t)c->sms * matrix_ctas_per_sm(c->mat_variant);
-    UnitBuilder ub(effective_unit_budget(c->mat_unit_work, (sum * sum - sum2) / 2, ctas));
+    UnitBuilder ub(effective_unit_budget(c->mat_unit_work, (sum * sum - sum2) / 2, ctas),
+                   (uint32_t)kMatVariantTable[c->mat_variant].rows);
     const auto nf = [&](uint32_t e) { return s->bf_count[targets[e]]; };
     const auto id = [&](uint32_t e) { return targets[e]; };
+    const auto nf_ref = [&](uint32_t d) { return s->bf_count[d]; };
     uint32_t g0 = 0;
     while (g0 < n) {
         uint32_t g1 = g0;
         while (g1 < n && s->bf_count[sorted[g1]] == s->bf_count[sorted[g0]]) g1++;
+        // every digest of the group is the reference of the whole suffix
+        const std::vector<uint32_t> ids(sorted.begin() + g0, sorted.begin() + g1);
+        ub.add_shared(ids, nf_ref, [&](uint32_t d) { return (uint32_t)s->fast[d]; }, 0u, g1, n, nf, id);
+        // and of the equal-count digests the swap rule gives it
         for (uint32_t k = g0; k < g1; k++) {
             const uint32_t a = sorted[k];
             const uint32_t tie0 = (uint32_t)targets.size();
@@ -239,7 +256,6 @@ static int build_plan_all(sdbfg_ctx* c, const sdbfg_set* s, MatPlan* p) {
                 if (ref == a) targets.push_back(b);
             }
             ub.add(a, s->bf_count[a], 0u, tie0, (uint32_t)targets.size(), nf, id);
-            ub.add(a, s->bf_count[a], 0u, g1, n, nf, id);
         }
         g0 = g1;
     }
@@ -249,35 +265,16 @@ static int build_plan_all(sdbfg_ctx* c, const sdbfg_set* s, MatPlan* p) {
 
 // Every query of set q against every target of set t (sdbf_score(q_i, t_j)).
 static int build_plan_cross(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_set* t, MatPlan* p) {
-    // per reference digest its targets on the other side
-    std::vector<uint32_t> cnt_q(q->n, 0), cnt_t(t->n, 0);
-    for (uint32_t i = 0; i < q->n; i++)
-        for (uint32_t j = 0; j < t->n; j++) {
-            if (swaps(q, i, t, j)) cnt_t[j]++;
-            else cnt_q[i]++;
-        }
-    std::vector<uint64_t> off_q(q->n + 1, 0), off_t(t->n + 1, 0);
-    for (uint32_t i = 0; i < q->n; i++) off_q[i + 1] = off_q[i] + cnt_q[i];
-    for (uint32_t j = 0; j < t->n; j++) off_t[j + 1] = off_t[j] + cnt_t[j];
-    const uint64_t total = off_q[q->n] + off_t[t->n];
-    if (total >= (1ull << 32)) return fail(c, SDBFG_ERR_ARG, "compare_to: too many pairs for one plan");
-    std::vector<uint32_t> targets(total);
-    std::vector<uint64_t> fill_q(off_q.begin(), off_q.end() - 1), fill_t(off_t.begin(), off_t.end() - 1);
-    for (uint32_t i = 0; i < q->n; i++)
-        for (uint32_t j = 0; j < t->n; j++) {
-            if (swaps(q, i, t, j)) targets[off_q[q->n] + fill_t[j]++] = i;
-            else targets[fill_q[i]++] = j;
-        }
+    if ((uint64_t)q->n * t->n + q->n + t->n >= (1ull << 32))
+        return fail(c, SDBFG_ERR_ARG, "compare_to: too many pairs for one plan");
     const uint64_t ctas = (uint64_t)c->sms * matrix_ctas_per_sm(c->mat_variant);
-    UnitBuilder ub(effective_unit_budget(c->mat_unit_work, (uint64_t)q->total_filters * t->total_filters, ctas));
-    const auto id = [&](uint32_t e) { return targets[e]; };
-    const auto nf_t = [&](uint32_t e) { return t->bf_count[targets[e]]; };
-    const auto nf_q = [&](uint32_t e) { return q->bf_count[targets[e]]; };
-    for (uint32_t i = 0; i < q->n; i++)
-        ub.add(i, q->bf_count[i], kUnitTgtSide1, (uint32_t)off_q[i], (uint32_t)off_q[i + 1], nf_t, id);
-    const uint32_t base = (uint32_t)off_q[q->n];
-    for (uint32_t j = 0; j < t->n; j++)
-        ub.add(j, t->bf_count[j], kUnitRefSide1, base + (uint32_t)off_t[j], base + (uint32_t)off_t[j + 1], nf_q, id);
+    UnitBuilder ub(effective_unit_budget(c->mat_unit_work, (uint64_t)q->total_filters * t->total_filters, ctas),
+                   (uint32_t)kMatVariantTable[c->mat_variant].rows);
+    std::vector<uint32_t> targets;
+    build_cross_units(
+        ub, targets, q->n, t->n, [&](uint32_t i, uint32_t j) { return swaps(q, i, t, j); },
+        [&](uint32_t i) { return q->bf_count[i]; }, [&](uint32_t j) { return t->bf_count[j]; },
+        [&](uint32_t i) { return (uint32_t)q->fast[i]; }, [&](uint32_t j) { return (uint32_t)t->fast[j]; });
     p->nscores = (uint64_t)q->n * t->n;
     return upload_plan(c, p, ub, targets);
 }
@@ -324,6 +321,7 @@ static MatParams plan_params(sdbfg_ctx* c, const MatPlan* p, const sdbfg_set* a,
     P.nunits = p->nunits;
     P.next_unit = p->d_counter.as<uint32_t>();
     P.targets = p->d_targets.as<uint32_t>();
+    P.refs = p->d_refs.as<uint32_t>();
     P.split = p->d_split.as<MatSplit>();
     P.nsplit = p->nsplit;
     P.slots = p->d_slots.as<double>();

@@ -381,7 +381,10 @@ struct MatSmem {
     uint32_t gidx[TJ];            // global filter index per slot
     uint32_t comp[TJ];            // local target index of the k-th completed target
     double mv[R][TJ + 1];         // per row and completed target: the filter's maximum
-    double run[kMatMaxTargets];   // running sums per target of the unit
+    double run[kMatMaxTargets];   // running sums per target of the unit (multi-pass units)
+    uint32_t gref[R];             // group units: reference digest ids,
+    uint32_t gstart[R + 1];       //   first row of each,
+    uint32_t gsparse[R];          //   and its count of sparse filters
     uint16_t cut_sum[1024];       // CUTOFFS256[4096 / (s1 + s2)] by s1 + s2
     uint16_t cut64_sum[1024];     // CUTOFFS64[1024 / (s1 + s2)] by s1 + s2
     uint16_t cut256[SDBF_CUTOFF_BINS];
@@ -415,22 +418,64 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
         const MatUnit U = S.unit;
         const uint32_t rs = U.flags & kUnitRefSide1 ? 1 : 0, ts = U.flags & kUnitTgtSide1 ? 1 : 0;
         const bool split = (U.flags & kUnitSplit) != 0;
-        const CmpDigest A = P.digests[rs][U.ref];
-        const bool fastA = (A.flags & kDigestFast) != 0;  // the reference digest's fastmode decides
+        const bool group = (U.flags & kUnitGroup) != 0;
+        const uint32_t nref = group ? U.nref : 1;
         const uint32_t nT = U.t1 - U.t0;
-        for (uint32_t k = tid; k < nT && !split; k += R) S.run[k] = -1.0;
+        if (group) {
+            // reference digests of the group and their first rows (warp 0)
+            if (tid < 32) {
+                uint32_t base_row = 0;
+                for (uint32_t b = 0; b < nref; b += 32) {
+                    const uint32_t k = b + lane;
+                    uint32_t n = 0, id = 0;
+                    if (k < nref) {
+                        id = P.refs[U.ref + k];
+                        n = P.digests[rs][id].nfilters;
+                    }
+                    uint32_t incl = n;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+                        if (lane >= (uint32_t)d) incl += v;
+                    }
+                    if (k < nref) {
+                        S.gref[k] = id;
+                        S.gstart[k] = base_row + incl - n;
+                        S.gsparse[k] = 0;
+                    }
+                    base_row += __shfl_sync(0xffffffffu, incl, 31);
+                }
+                if (lane == 0) S.gstart[nref] = base_row;
+            }
+        } else {
+            for (uint32_t k = tid; k < nT && !split; k += R) S.run[k] = -1.0;
+        }
         if (tid == 0) S.sparse = 0;
         __syncthreads();
+        const CmpDigest A = P.digests[rs][group ? S.gref[0] : U.ref];
+        const bool fastA = (A.flags & kDigestFast) != 0;  // the reference digest's fastmode decides
         for (uint32_t rc = U.r0; rc < U.r1; rc += R) {
             const uint32_t row = rc + tid;
             const bool have = row < U.r1;
             uint32_t a[64];
             uint32_t s1 = 0, e1 = 0;
+            uint32_t gk = 0;  // group units: this row's digest in the group
+            uint32_t fidx = A.first + row;
+            if (group && have) {
+                uint32_t lo = 0, hi = nref;  // largest k with gstart[k] <= row
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (S.gstart[mid] <= row) lo = mid;
+                    else hi = mid;
+                }
+                gk = lo;
+                fidx = P.digests[rs][S.gref[gk]].first + (row - S.gstart[gk]);
+            }
             if (have) {
-                const uint32_t m = P.meta[rs][A.first + row];
+                const uint32_t m = P.meta[rs][fidx];
                 s1 = m & 0xFFFFu;
                 e1 = m >> 16;
-                const uint4* src = reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)(A.first + row) * 64);
+                const uint4* src = reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)fidx * 64);
 #pragma unroll
                 for (int q = 0; q < 16; q++) {
                     const uint4 v = __ldg(src + q);
@@ -441,6 +486,7 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
                 for (int q = 0; q < 64; q++) a[q] = 0;
             }
             const bool active = have && s1 >= (uint32_t)kMinElem;
+            if (group && have && !active) atomicAdd(&S.gsparse[gk], 1u);
             const uint32_t nsparse = __syncthreads_count(have && !active);
             if (tid == 0) {
                 S.sparse += nsparse;
@@ -569,7 +615,21 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
                 }
                 __syncthreads();
                 // ---- fold the completed targets' maxima in filter order
-                if (!split) {
+                if (group) {  // every (reference, completed target) pair is finished here
+                    const uint32_t ncomp = S.ncomp;
+                    for (uint32_t t = tid; t < ncomp * nref; t += R) {
+                        const uint32_t k = t % nref, col = t / nref;
+                        double sum = -1.0;
+                        for (uint32_t r = S.gstart[k]; r < S.gstart[k + 1]; r++) {
+                            const double m = S.mv[r][col];
+                            if (sum < 0) sum = m;
+                            else if (m != 0.0) sum = __dadd_rn(sum, m);
+                        }
+                        const uint32_t tgt = P.targets[U.t0 + S.comp[col]];
+                        P.scores[out_index(P, rs != 0, S.gref[k], tgt)] =
+                            final_score(sum, S.gstart[k + 1] - S.gstart[k], S.gsparse[k]);
+                    }
+                } else if (!split) {
                     for (uint32_t k = tid; k < S.ncomp; k += R) {
                         double sum = S.run[S.comp[k]];
                         for (uint32_t r = 0; r < nrows; r++) {
@@ -583,7 +643,7 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
                 __syncthreads();
             }
         }
-        if (!split) {
+        if (!split && !group) {
             for (uint32_t k = tid; k < nT; k += R) {
                 const uint32_t tgt = P.targets[U.t0 + k];
                 P.scores[out_index(P, rs != 0, U.ref, tgt)] = final_score(S.run[k], A.nfilters, S.sparse);

@@ -58,15 +58,24 @@ namespace sdbfg {
 constexpr uint32_t kMatMaxTargets = 512;  // targets per unit (running sums in shared memory)
 
 enum : uint32_t { kMatModeAll = 0, kMatModeCross = 1 };
-enum : uint32_t { kUnitRefSide1 = 1u, kUnitTgtSide1 = 2u, kUnitSplit = 4u };
+enum : uint32_t { kUnitRefSide1 = 1u, kUnitTgtSide1 = 2u, kUnitSplit = 4u, kUnitGroup = 8u };
 
+// Three kinds of unit:
+//  * group (kUnitGroup): nref reference digests listed at refs[ref ..
+//    ref+nref), all their filters together fit one pass of the CTA's rows;
+//    every (reference, target) score is finished inside the unit;
+//  * multi-pass: one reference digest with more filters than the CTA has
+//    rows (ref = digest id, rows [r0, r1) = all its filters), running sums
+//    per target in shared memory;
+//  * split (kUnitSplit): rows [r0, r1) of one reference digest against one
+//    target; maxima to the slot array, summed by k_matrix_finalize.
 struct MatUnit {
-    uint32_t ref;     // reference digest (side: flags & kUnitRefSide1)
-    uint32_t r0, r1;  // its filters [r0, r1)
+    uint32_t ref;     // digest id, or (group) position in MatParams::refs
+    uint32_t r0, r1;  // rows [r0, r1) (group: 0 .. total filters of its digests)
     uint32_t t0, t1;  // target list entries [t0, t1); one entry for split units
     uint32_t flags;
     uint32_t split;   // split units: index into MatParams::split
-    uint32_t pad;
+    uint32_t nref;    // group units: digests in the group
 };
 
 struct MatSplit {
@@ -84,6 +93,7 @@ struct MatParams {
     uint32_t nunits;
     uint32_t* next_unit;       // work counter (zero before the launch)
     const uint32_t* targets;   // target list (digest ids)
+    const uint32_t* refs;      // reference digest ids of group units
     const MatSplit* split;
     uint32_t nsplit;
     double* slots;

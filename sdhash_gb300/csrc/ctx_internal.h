@@ -129,6 +129,7 @@ struct sdbfg_set {
     std::vector<std::string> names;
     std::vector<uint32_t> bf_count;
     std::vector<uint32_t> last_elem;  // element count of the last filter (swap rule)
+    std::vector<uint8_t> fast;         // per digest: folded by sdbfg_set_fast
     uint64_t serial = 0;               // identifies the set in cached comparison plans
     uint64_t total_filters = 0;
     DevBuf d_filters, d_meta, d_digests;
@@ -145,14 +146,14 @@ struct MatPlan {
     uint32_t nunits = 0, nsplit = 0;
     uint64_t nscores = 0;
     uint64_t filter_pairs = 0;  // sum over scored pairs of n_ref * n_tgt
-    DevBuf d_units, d_targets, d_split, d_slots, d_counter;
+    DevBuf d_units, d_targets, d_refs, d_split, d_slots, d_counter;
     cudaGraphExec_t graph = nullptr;
     int32_t* graph_out = nullptr;
     cudaStream_t graph_stream = nullptr;
     uint64_t last_use = 0;
     ~MatPlan() {
         if (graph) cudaGraphExecDestroy(graph);
-        for (DevBuf* b : {&d_units, &d_targets, &d_split, &d_slots, &d_counter}) b->release();
+        for (DevBuf* b : {&d_units, &d_targets, &d_refs, &d_split, &d_slots, &d_counter}) b->release();
     }
 };
 

@@ -78,9 +78,9 @@ struct sdbfg_server {
         bool busy = false;
         std::vector<Request> batch;
         uint32_t nunits = 0, nsplit = 0;
-        HostBuf h_filters, h_meta, h_dig, h_units, h_targets, h_split, h_scores;
-        DevBuf d_filters, d_meta, d_dig, d_units, d_targets, d_split, d_slots, d_counter, d_scores;
-        uint64_t cap_units = 0, cap_targets = 0, cap_split = 0, cap_slots = 0;
+        HostBuf h_filters, h_meta, h_dig, h_units, h_targets, h_refs, h_split, h_scores;
+        DevBuf d_filters, d_meta, d_dig, d_units, d_targets, d_refs, d_split, d_slots, d_counter, d_scores;
+        uint64_t cap_units = 0, cap_targets = 0, cap_refs = 0, cap_split = 0, cap_slots = 0;
     };
     std::vector<Slot> slots;
 };
@@ -114,36 +114,22 @@ static cudaError_t launch_batch(sdbfg_server* sv, sdbfg_server::Slot& S) {
         dig[i] = CmpDigest{(uint32_t)tot, r.nf};
         tot += r.nf;
     }
-    // work units: query i against every target, orientation by the swap rule
-    std::vector<uint32_t> targets;
-    targets.reserve((size_t)nq * nt);
-    std::vector<std::pair<uint32_t, uint32_t>> qlist(nq), tlist(nt);  // [start, end) in targets
-    std::vector<std::vector<uint32_t>> by_t(nt);
-    for (uint32_t i = 0; i < nq; i++) {
-        const uint32_t s0 = (uint32_t)targets.size();
-        for (uint32_t j = 0; j < nt; j++) {
-            if (server_swaps(S.batch[i], T, j)) by_t[j].push_back(i);
-            else targets.push_back(j);
-        }
-        qlist[i] = {s0, (uint32_t)targets.size()};
-    }
-    for (uint32_t j = 0; j < nt; j++) {
-        const uint32_t s0 = (uint32_t)targets.size();
-        targets.insert(targets.end(), by_t[j].begin(), by_t[j].end());
-        tlist[j] = {s0, (uint32_t)targets.size()};
-    }
+    // work units: every query against every target, orientation by the swap rule
     const uint64_t ctas = (uint64_t)sv->ctx->sms * matrix_ctas_per_sm(sv->ctx->mat_variant);
-    UnitBuilder ub(effective_unit_budget(sv->ctx->mat_unit_work, tot * T->total_filters, ctas));
-    const auto id = [&](uint32_t e) { return targets[e]; };
-    const auto nf_t = [&](uint32_t e) { return T->bf_count[targets[e]]; };
-    const auto nf_q = [&](uint32_t e) { return S.batch[targets[e]].nf; };
-    for (uint32_t i = 0; i < nq; i++) ub.add(i, S.batch[i].nf, kUnitTgtSide1, qlist[i].first, qlist[i].second, nf_t, id);
-    for (uint32_t j = 0; j < nt; j++) ub.add(j, T->bf_count[j], kUnitRefSide1, tlist[j].first, tlist[j].second, nf_q, id);
+    UnitBuilder ub(effective_unit_budget(sv->ctx->mat_unit_work, tot * T->total_filters, ctas),
+                   (uint32_t)kMatVariantTable[sv->ctx->mat_variant].rows);
+    std::vector<uint32_t> targets;
+    build_cross_units(
+        ub, targets, nq, nt, [&](uint32_t i, uint32_t j) { return server_swaps(S.batch[i], T, j); },
+        [&](uint32_t i) { return S.batch[i].nf; }, [&](uint32_t j) { return T->bf_count[j]; },
+        [](uint32_t) { return 0u; }, [&](uint32_t j) { return (uint32_t)T->fast[j]; });
     const std::vector<MatUnit> units = ub.sorted_units();
     cudaError_t e;
     if ((e = grow(S.d_units, &S.h_units, S.cap_units, units.size() + 1, sizeof(MatUnit)))) return e;
     if ((e = grow(S.d_targets, &S.h_targets, S.cap_targets, targets.size() + 1, 4))) return e;
     if ((e = grow(S.d_split, &S.h_split, S.cap_split, ub.split.size() + 1, sizeof(MatSplit)))) return e;
+    if ((e = grow(S.d_refs, &S.h_refs, S.cap_refs, ub.refs.size() + 1, 4))) return e;
+    memcpy(S.h_refs.p, ub.refs.data(), ub.refs.size() * 4);
     if ((e = grow(S.d_slots, nullptr, S.cap_slots, ub.slots + 1, 8))) return e;
     memcpy(S.h_units.p, units.data(), units.size() * sizeof(MatUnit));
     memcpy(S.h_targets.p, targets.data(), targets.size() * 4);
@@ -157,6 +143,9 @@ static cudaError_t launch_batch(sdbfg_server* sv, sdbfg_server::Slot& S) {
     if ((e = cudaMemcpyAsync(S.d_units.p, S.h_units.p, units.size() * sizeof(MatUnit), cudaMemcpyHostToDevice, st)))
         return e;
     if ((e = cudaMemcpyAsync(S.d_targets.p, S.h_targets.p, targets.size() * 4, cudaMemcpyHostToDevice, st))) return e;
+    if (!ub.refs.empty() &&
+        (e = cudaMemcpyAsync(S.d_refs.p, S.h_refs.p, ub.refs.size() * 4, cudaMemcpyHostToDevice, st)))
+        return e;
     if (S.nsplit &&
         (e = cudaMemcpyAsync(S.d_split.p, S.h_split.p, S.nsplit * sizeof(MatSplit), cudaMemcpyHostToDevice, st)))
         return e;
@@ -172,6 +161,7 @@ static cudaError_t launch_batch(sdbfg_server* sv, sdbfg_server::Slot& S) {
     P.nunits = S.nunits;
     P.next_unit = S.d_counter.as<uint32_t>();
     P.targets = S.d_targets.as<uint32_t>();
+    P.refs = S.d_refs.as<uint32_t>();
     P.split = S.d_split.as<MatSplit>();
     P.nsplit = S.nsplit;
     P.slots = S.d_slots.as<double>();
@@ -251,8 +241,10 @@ static void worker_loop(sdbfg_server* sv) {
                 if (sv->pending.empty()) break;
                 uint64_t f = 0;
                 const uint64_t t = now_ns();
+                const uint64_t tf = sv->refs->total_filters;
                 while (!sv->pending.empty() && S.batch.size() < sv->cfg.max_batch_queries &&
-                       (S.batch.empty() || f + sv->pending.front().nf <= sv->slot_filters)) {
+                       (S.batch.empty() || (f + sv->pending.front().nf <= sv->slot_filters &&
+                                            (f + sv->pending.front().nf) * tf <= sv->cfg.max_batch_pairs))) {
                     f += sv->pending.front().nf;
                     S.batch.push_back(std::move(sv->pending.front()));
                     S.batch.back().start_ns = t;
@@ -295,8 +287,9 @@ extern "C" int sdbfg_server_create(sdbfg_ctx* c, const sdbfg_set* refs, const sd
     auto* sv = new sdbfg_server();
     sv->ctx = c;
     sv->refs = refs;
-    sdbfg_server_config d{3, 256, 256ull << 20, 1};
+    sdbfg_server_config d{3, 256, 256ull << 20, 1, 0, 1ull << 31};
     if (cfg) d = *cfg;
+    if (d.max_batch_pairs == 0) d.max_batch_pairs = 1ull << 31;
     if (d.slots == 0 || d.slots > 8 || d.max_batch_queries == 0 || d.memory_budget < (1ull << 20)) {
         delete sv;
         return fail(c, SDBFG_ERR_ARG, "server config out of range");
@@ -321,7 +314,9 @@ extern "C" int sdbfg_server_create(sdbfg_ctx* c, const sdbfg_set* refs, const sd
         }
         if (e == cudaSuccess) e = S.d_counter.ensure(64);
         if (e == cudaSuccess) e = grow(S.d_units, &S.h_units, S.cap_units, 1 << 16, sizeof(MatUnit));
-        if (e == cudaSuccess) e = grow(S.d_targets, &S.h_targets, S.cap_targets, (uint64_t)nq * refs->n + 1, 4);
+        if (e == cudaSuccess)
+            e = grow(S.d_targets, &S.h_targets, S.cap_targets, (uint64_t)nq * refs->n + nq + refs->n + 1, 4);
+        if (e == cudaSuccess) e = grow(S.d_refs, &S.h_refs, S.cap_refs, (uint64_t)nq + refs->n + 1, 4);
         if (e == cudaSuccess) e = grow(S.d_split, &S.h_split, S.cap_split, (uint64_t)nq * refs->n + 1, sizeof(MatSplit));
         if (e == cudaSuccess) e = grow(S.d_slots, nullptr, S.cap_slots, (uint64_t)nf * refs->n + 1, 8);
         if (e != cudaSuccess) {
@@ -412,10 +407,11 @@ extern "C" void sdbfg_server_destroy(sdbfg_server* sv) {
     if (sv->worker.joinable()) sv->worker.join();
     cudaSetDevice(sv->ctx->device);
     for (auto& S : sv->slots) {
-        for (DevBuf* b : {&S.d_filters, &S.d_meta, &S.d_dig, &S.d_units, &S.d_targets, &S.d_split, &S.d_slots,
-                          &S.d_counter, &S.d_scores})
+        for (DevBuf* b : {&S.d_filters, &S.d_meta, &S.d_dig, &S.d_units, &S.d_targets, &S.d_refs, &S.d_split,
+                          &S.d_slots, &S.d_counter, &S.d_scores})
             b->release();
-        for (HostBuf* b : {&S.h_filters, &S.h_meta, &S.h_dig, &S.h_units, &S.h_targets, &S.h_split, &S.h_scores})
+        for (HostBuf* b : {&S.h_filters, &S.h_meta, &S.h_dig, &S.h_units, &S.h_targets, &S.h_refs, &S.h_split,
+                           &S.h_scores})
             b->release();
         if (S.st) cudaStreamDestroy(S.st);
         if (S.ev) cudaEventDestroy(S.ev);
