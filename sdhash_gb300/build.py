@@ -23,9 +23,10 @@ SYNTH = os.path.join(HERE, "libsdbf_synth.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = os.environ.get("SDBFG_ARCH", "-gencode=arch=compute_103a,code=sm_103a")
-CU_SOURCES = ["gen_kernels.cu", "compare_kernels.cu", "sdbf_api.cu", "compare_api.cu", "serve.cu", "noalloc.cu"]
+CU_SOURCES = ["gen_kernels.cu", "compare_kernels.cu", "matrix_tc.cu", "sdbf_api.cu", "compare_api.cu", "serve.cu",
+              "noalloc.cu"]
 CPP_SOURCES = ["sdbf_text.cpp", "../compat/sdbf_compat.cpp"]
-HEADERS = ["gen_kernels.h", "compare_kernels.h", "ctx_internal.h", "matrix_plan.h", "sdbf_device.cuh", "sdbf_tables.h", "../compat/sdbf_class.h",
+HEADERS = ["gen_kernels.h", "compare_kernels.h", "compare_device.cuh", "ctx_internal.h", "matrix_plan.h", "sdbf_device.cuh", "sdbf_tables.h", "../compat/sdbf_class.h",
            "../compat/sdbf_set.h", "../compat/sdbf_conf.h"]
 
 

@@ -330,11 +330,12 @@ static MatParams plan_params(sdbfg_ctx* c, const MatPlan* p, const sdbfg_set* a,
     P.n = p->mode == kMatModeAll ? a->n : b->n;
     P.cutoffs = c->d_cut.as<uint16_t>();
     P.cutoffs64 = c->d_cut64.as<uint16_t>();
+    P.error = p->d_counter.as<uint32_t>() + 1;
     return P;
 }
 
 static int enqueue_plan(sdbfg_ctx* c, const MatPlan* p, const MatParams& P, cudaStream_t st) {
-    CUDA_TRY(c, cudaMemsetAsync(p->d_counter.p, 0, 4, st));
+    CUDA_TRY(c, cudaMemsetAsync(p->d_counter.p, 0, 8, st));  // work counter, error flag
     const uint32_t grid = (uint32_t)(c->sms * matrix_ctas_per_sm(p->variant));
     TIMED_LAUNCH_ON(c, "k_matrix", st, launch_matrix(P, p->variant, std::max(1u, std::min(grid, P.nunits)), st));
     if (P.nsplit) TIMED_LAUNCH_ON(c, "k_matrix_finalize", st, launch_matrix_finalize(P, st));
@@ -379,6 +380,15 @@ static int run_plan(sdbfg_ctx* c, MatPlan* p, const sdbfg_set* a, const sdbfg_se
     return SDBFG_OK;
 }
 
+// waits for the plan's launches and reports a bounded wait that gave up
+static int check_plan_error(sdbfg_ctx* c, const MatPlan* p) {
+    uint32_t err = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(&err, p->d_counter.as<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (err) return fail(c, SDBFG_ERR_CUDA, "comparison kernel: %u CTAs gave up waiting for the tensor cores", err);
+    return SDBFG_OK;
+}
+
 extern "C" int sdbfg_compare_all_device(sdbfg_ctx* c, const sdbfg_set* s, int32_t* dev_scores) {
     if (!c || !s || (!dev_scores && s->n > 1)) return SDBFG_ERR_ARG;
     CUDA_TRY(c, cudaSetDevice(c->device));
@@ -410,8 +420,7 @@ extern "C" int sdbfg_compare_all(sdbfg_ctx* c, const sdbfg_set* s, int32_t* out)
     rc = run_plan(c, p, s, nullptr, c->d_scores.as<int32_t>());
     if (rc) return rc;
     CUDA_TRY(c, cudaMemcpyAsync(out, c->d_scores.p, p->nscores * 4, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    return SDBFG_OK;
+    return check_plan_error(c, p);
 }
 
 extern "C" int sdbfg_compare_to(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_set* t, int32_t* out) {
@@ -425,8 +434,7 @@ extern "C" int sdbfg_compare_to(sdbfg_ctx* c, const sdbfg_set* q, const sdbfg_se
     rc = run_plan(c, p, q, t, c->d_scores.as<int32_t>());
     if (rc) return rc;
     CUDA_TRY(c, cudaMemcpyAsync(out, c->d_scores.p, p->nscores * 4, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    return SDBFG_OK;
+    return check_plan_error(c, p);
 }
 
 // scores (already queued into c->d_scores) -> matches on the host
@@ -467,6 +475,7 @@ extern "C" int sdbfg_compare_all_matches(sdbfg_ctx* c, const sdbfg_set* s, int32
     CUDA_TRY(c, c->d_scores.ensure(p->nscores * 4));
     rc = run_plan(c, p, s, nullptr, c->d_scores.as<int32_t>());
     if (rc) return rc;
+    if ((rc = check_plan_error(c, p))) return rc;
     return collect_matches(c, p->nscores, kMatModeAll, s->n, threshold, out, cap, count);
 }
 
@@ -482,6 +491,7 @@ extern "C" int sdbfg_compare_to_matches(sdbfg_ctx* c, const sdbfg_set* q, const 
     CUDA_TRY(c, c->d_scores.ensure(p->nscores * 4));
     rc = run_plan(c, p, q, t, c->d_scores.as<int32_t>());
     if (rc) return rc;
+    if ((rc = check_plan_error(c, p))) return rc;
     return collect_matches(c, p->nscores, kMatModeCross, t->n, threshold, out, cap, count);
 }
 
@@ -568,7 +578,7 @@ extern "C" int sdbfg_compare_autotune(sdbfg_ctx* c, const sdbfg_set* a, const sd
             cudaStream_t st = c->stream;
             float best_ms = 1e30f;
             for (int rep = 0; rep < 2; rep++) {
-                CUDA_TRY(c, cudaMemsetAsync(p->d_counter.p, 0, 4, st));
+                CUDA_TRY(c, cudaMemsetAsync(p->d_counter.p, 0, 8, st));
                 CUDA_TRY(c, cudaEventRecord(e0, st));
                 const uint32_t grid = (uint32_t)(c->sms * matrix_ctas_per_sm(v));
                 CUDA_TRY(c, launch_matrix(P, v, std::max(1u, std::min(grid, P.nunits)), st));

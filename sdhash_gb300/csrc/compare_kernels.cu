@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "compare_device.cuh"
 #include "compare_kernels.h"
 #include "sdbf_device.cuh"
 
@@ -161,22 +162,6 @@ __device__ __forceinline__ bool staged_exit(const uint32_t (&a)[64], const uint3
     return 2 * c + 48 < cut;
 }
 
-__device__ __forceinline__ uint32_t cut_for(const uint16_t* cut_sum, const uint16_t* cut256, uint32_t s1,
-                                            uint32_t s2) {
-    const uint32_t sum = s1 + s2;
-    return sum < 1024 ? cut_sum[sum] : cut256[4096u / sum];
-}
-
-// A filter's maximum against one target as the reference's double:
-// -1 when no target filter has >= 16 elements, else num / den (den is the
-// reference's uint32 max_est - cut, which wraps when the hamming weights do
-// not describe the compared bits -- mixed --fast comparisons).
-__device__ __forceinline__ double max_value(bool active, uint32_t bnum, uint32_t bden, bool counted) {
-    if (!active) return 0.0;
-    if (!counted) return -1.0;
-    return bnum == 0 ? 0.0 : __ddiv_rn((double)bnum, (double)bden);
-}
-
 // popcount(a & t) over the first 16 words (64 bytes) for two targets, and
 // the 8-word partial counts for the fast-mode stage test.
 __device__ __forceinline__ void and_popc_16x2(const uint32_t (&a)[64], const uint32_t* t0, const uint32_t* t1,
@@ -198,22 +183,6 @@ __device__ __forceinline__ void and_popc_16x2(const uint32_t (&a)[64], const uin
     }
     f0 = c0;
     f1 = c1;
-}
-
-__device__ __forceinline__ uint64_t out_index(const MatParams& P, bool ref_side1, uint32_t ref, uint32_t tgt) {
-    if (P.mode == kMatModeAll) {
-        const uint64_t i = min(ref, tgt), j = max(ref, tgt);
-        return i * (2ull * P.n - i - 1) / 2 + (j - i - 1);
-    }
-    const uint64_t q = ref_side1 ? tgt : ref, t = ref_side1 ? ref : tgt;
-    return q * P.n + t;
-}
-
-__device__ __forceinline__ int32_t final_score(double sum, uint32_t n1, uint32_t sparse) {
-    uint64_t denom = n1;
-    if (n1 > 1) denom -= sparse;
-    if (denom == 0 || sum < 0) return -1;
-    return (int32_t)floor(__dadd_rn(__ddiv_rn(__dmul_rn(100.0, sum), (double)denom), 0.5));
 }
 
 }  // namespace
@@ -371,7 +340,7 @@ cudaError_t launch_compare_pairs(const CmpParams& P, uint32_t grid, cudaStream_t
 // ---------------------------------------------------------- matrix engine
 namespace sdbfg {
 
-const MatVariant kMatVariantTable[kMatVariants] = {{128, 32}, {128, 16}, {128, 64}, {64, 32}, {256, 32}};
+const MatVariant kMatVariantTable[kMatVariants] = {{128, 32}, {128, 16}, {128, 64}, {64, 32}, {256, 32}, {128, 256}};
 
 template <int R, int TJ>
 struct MatSmem {
@@ -685,6 +654,7 @@ cudaError_t launch_matrix(const MatParams& P, int variant, uint32_t grid, cudaSt
         case 2: return launch_variant<128, 64>(P, grid, st);
         case 3: return launch_variant<64, 32>(P, grid, st);
         case 4: return launch_variant<256, 32>(P, grid, st);
+        case kMatVariantTc: return launch_matrix_tc(P, grid, st);
     }
     return cudaErrorInvalidValue;
 }
@@ -703,7 +673,7 @@ static int occupancy() {
 }
 
 int matrix_ctas_per_sm(int variant) {
-    static int cached[kMatVariants] = {0, 0, 0, 0, 0};
+    static int cached[kMatVariants] = {0, 0, 0, 0, 0, 0};
     if (variant >= 0 && variant < kMatVariants && cached[variant]) return cached[variant];
     int n = 1;
     switch (variant) {
@@ -712,6 +682,7 @@ int matrix_ctas_per_sm(int variant) {
         case 2: n = occupancy<128, 64>(); break;
         case 3: n = occupancy<64, 32>(); break;
         case 4: n = occupancy<256, 32>(); break;
+        case kMatVariantTc: n = matrix_tc_ctas_per_sm(); break;
         default: return 1;
     }
     cached[variant] = n;

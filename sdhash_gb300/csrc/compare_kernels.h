@@ -102,17 +102,23 @@ struct MatParams {
     uint32_t n;                // set size (all) / number of targets (cross)
     const uint16_t* cutoffs;   // CUTOFFS256
     const uint16_t* cutoffs64; // CUTOFFS64 (fast mode)
+    uint32_t* error;           // tensor-core kernel: set when a bounded wait gave up
 };
 
-// Kernel variants (rows per CTA x target filters per shared-memory tile),
-// chosen by the autotuner.
+// Kernel variants (rows per CTA x target filters per tile), chosen by the
+// autotuner.  Variants 0-4 count on the CUDA cores (carry-save AND-popcount);
+// variant 5 counts on the tensor cores (tcgen05, fp8 0/1 operands, fp32
+// accumulators in TMEM: the count is an exact dot product) and needs sm_100+.
 struct MatVariant {
     int rows, tile;
 };
-constexpr int kMatVariants = 5;
+constexpr int kMatVariants = 6;
+constexpr int kMatVariantTc = 5;
 extern const MatVariant kMatVariantTable[kMatVariants];
 
 cudaError_t launch_matrix(const MatParams& P, int variant, uint32_t grid, cudaStream_t st);
+cudaError_t launch_matrix_tc(const MatParams& P, uint32_t grid, cudaStream_t st);
+int matrix_tc_ctas_per_sm();
 cudaError_t launch_matrix_finalize(const MatParams& P, cudaStream_t st);
 int matrix_ctas_per_sm(int variant);
 

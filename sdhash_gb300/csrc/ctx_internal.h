@@ -116,7 +116,7 @@ struct sdbfg_ctx {
     cudaEvent_t ev_scan[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev_start = nullptr;
     // comparison engine: tuning and cached plans (work units + CUDA graph)
-    int mat_variant = 0;
+    int mat_variant = kMatVariantTc;  // tensor-core counting
     uint64_t mat_unit_work = 1ull << 22;
     bool mat_graphs = true;
     std::vector<struct MatPlan*> plans;

@@ -1,0 +1,484 @@
+// matrix_tc.cu -- the filter-matrix comparison counted on the tensor cores.
+//
+// popcount(a & b) of two 2048-bit filters is the dot product of their bit
+// vectors.  With each bit widened to an e4m3 byte (1.0 = 0x38 or 0) and fp32
+// accumulation, tcgen05.mma computes it exactly (every partial sum is an
+// integer <= 2048).  One CTA multiplies 128 reference filters (TMEM lanes)
+// by up to 256 target filters (TMEM columns) over K = 2048 in 16 chunks of
+// 128: all 256 threads widen the chunk's bits into a 128-byte-swizzled
+// shared-memory stage (two stages, so widening overlaps the MMAs of the
+// previous chunk), one thread issues the four K=32 MMAs and commits them to
+// the stage's mbarrier.  The 128 row threads then read their row of counts
+// from TMEM and score the tile exactly as the CUDA-core kernel does
+// (compare_kernels.cu k_matrix): a pair can score above 0 only if its full
+// count exceeds the cut, and for those rare pairs the reference's staged
+// exits (bf_utils.cc:114-206) are rechecked from the filters in memory.
+// Work units, group units, running sums and split pairs are those of
+// k_matrix.
+//
+// The widening permutes K inside each 32-bit word (output word k of a word
+// w holds bits k, k+8, k+16, k+24 of w), identically for both operands, so
+// the dot product is unchanged; one shift and one mask per output word, the
+// x0x38 on the FMA pipe.  --fast digests count only chunks 0-3 (their first
+// 64 bytes).
+//
+// Every mbarrier wait is bounded; a wait that gives up sets P.error, all
+// threads leave together (the decision is made by __syncthreads_and), the
+// MMAs still in flight are waited for and the TMEM is released.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "compare_device.cuh"
+#include "compare_kernels.h"
+#include "sdbf_device.cuh"
+
+namespace sdbfg {
+
+namespace {
+
+constexpr int kTcRows = 128;       // reference rows per pass = TMEM lanes
+constexpr int kTcCols = 256;       // target filters per tile = MMA N (max)
+constexpr int kTcThreads = 256;
+constexpr int kTcChunk = 128;      // K elements (bits) per stage
+constexpr int kTcChunks = 2048 / kTcChunk;
+constexpr int kTcMaxComp = 32;     // targets completed per tile
+constexpr uint32_t kTcAStage = kTcRows * kTcChunk;   // 16 KB of e4m3
+constexpr uint32_t kTcBStage = kTcCols * kTcChunk;   // 32 KB
+constexpr uint32_t kTcStage = kTcAStage + kTcBStage;
+constexpr uint32_t kTcWaitSpins = 1u << 22;
+
+struct TcSmem {
+    uint32_t gidx[kTcCols], tmeta[kTcCols], tinfo[kTcCols];
+    uint32_t rowf[kTcRows];           // filter index of each reference row (~0: none)
+    uint32_t comp[kTcMaxComp];
+    double mv[kTcRows][kTcMaxComp + 1];
+    double run[kMatMaxTargets];
+    uint32_t gref[kTcRows], gstart[kTcRows + 1], gsparse[kTcRows];
+    uint16_t cut_sum[1024], cut64_sum[1024], cut256[SDBF_CUTOFF_BINS], cut64[SDBF_CUTOFF_BINS];
+    MatUnit unit;
+    uint32_t unit_id, ntile, ncomp, cur_t, cur_f, sparse, tmem;
+    alignas(8) uint64_t mbar[3];      // stage 0, stage 1, accumulator complete
+};
+
+constexpr size_t kTcSmemBytes = 1024 /* alignment */ + 2 * kTcStage + sizeof(TcSmem);
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+    for (uint32_t i = 0; i < kTcWaitSpins; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+// row r's 128 e4m3 bytes of one chunk from its 128 filter bits (4 words):
+// 8 granules of 16 bytes at their swizzled places
+__device__ __forceinline__ void widen_row(uint8_t* stage, uint32_t r, uint4 bits) {
+    const uint32_t w[4] = {bits.x, bits.y, bits.z, bits.w};
+    uint8_t* row = stage + (r >> 3) * 1024 + (r & 7) * 128;
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            uint4 g;
+            g.x = ((w[m] >> (4 * h + 0)) & 0x01010101u) * 0x38u;
+            g.y = ((w[m] >> (4 * h + 1)) & 0x01010101u) * 0x38u;
+            g.z = ((w[m] >> (4 * h + 2)) & 0x01010101u) * 0x38u;
+            g.w = ((w[m] >> (4 * h + 3)) & 0x01010101u) * 0x38u;
+            const uint32_t gi = 2 * m + h;
+            *reinterpret_cast<uint4*>(row + ((gi ^ (r & 7)) << 4)) = g;
+        }
+    }
+}
+
+// the reference's staged exits for a pair above the cut, from memory
+__device__ __forceinline__ bool staged_exit_mem(const uint32_t* a, const uint32_t* t, uint32_t cut) {
+    const uint4* a4 = reinterpret_cast<const uint4*>(a);
+    const uint4* t4 = reinterpret_cast<const uint4*>(t);
+    uint32_t c = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const uint4 x = __ldg(a4 + q), y = __ldg(t4 + q);
+        c += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
+        if (q == 1 && 8 * c + 48 < cut) return true;
+        if (q == 3 && 4 * c + 48 < cut) return true;
+    }
+    return 2 * c + 48 < cut;
+}
+
+__device__ __forceinline__ uint32_t popc8_mem(const uint32_t* a, const uint32_t* t) {
+    const uint4* a4 = reinterpret_cast<const uint4*>(a);
+    const uint4* t4 = reinterpret_cast<const uint4*>(t);
+    uint32_t c = 0;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const uint4 x = __ldg(a4 + q), y = __ldg(t4 + q);
+        c += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
+    }
+    return c;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
+    extern __shared__ uint8_t tc_smem_raw[];
+    const uint32_t raw = smem_addr(tc_smem_raw);
+    uint8_t* stages = tc_smem_raw + (((raw + 1023) & ~1023u) - raw);
+    TcSmem& S = *reinterpret_cast<TcSmem*>(stages + 2 * kTcStage);
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    for (uint32_t i = tid; i < 1024; i += kTcThreads) {
+        S.cut_sum[i] = P.cutoffs[i >= 32 ? 4096u / i : (uint32_t)SDBF_CUTOFF_BINS - 1];
+        S.cut64_sum[i] = P.cutoffs64[i >= 8 ? 1024u / i : (uint32_t)SDBF_CUTOFF_BINS - 1];
+    }
+    for (uint32_t i = tid; i < SDBF_CUTOFF_BINS; i += kTcThreads) {
+        S.cut256[i] = P.cutoffs[i];
+        S.cut64[i] = P.cutoffs64[i];
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 3; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&S.mbar[i])));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem)),
+                     "r"(kTcCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = S.tmem;
+
+    uint32_t uses[2] = {0, 0};  // commits to each stage barrier so far
+    uint32_t done_phase = 0;     // commits to the accumulator barrier so far
+    bool ok = true;
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t u = atomicAdd(P.next_unit, 1u);
+            S.unit_id = u;
+            if (u < P.nunits) S.unit = P.units[u];
+        }
+        __syncthreads();
+        if (S.unit_id >= P.nunits) break;
+        const MatUnit U = S.unit;
+        const uint32_t rs = U.flags & kUnitRefSide1 ? 1 : 0, ts = U.flags & kUnitTgtSide1 ? 1 : 0;
+        const bool split = (U.flags & kUnitSplit) != 0;
+        const bool group = (U.flags & kUnitGroup) != 0;
+        const uint32_t nref = group ? U.nref : 1;
+        const uint32_t nT = U.t1 - U.t0;
+        if (group) {
+            if (tid < 32) {
+                uint32_t base_row = 0;
+                for (uint32_t b = 0; b < nref; b += 32) {
+                    const uint32_t k = b + lane;
+                    uint32_t n = 0, id = 0;
+                    if (k < nref) {
+                        id = P.refs[U.ref + k];
+                        n = P.digests[rs][id].nfilters;
+                    }
+                    uint32_t incl = n;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+                        if (lane >= (uint32_t)d) incl += v;
+                    }
+                    if (k < nref) {
+                        S.gref[k] = id;
+                        S.gstart[k] = base_row + incl - n;
+                        S.gsparse[k] = 0;
+                    }
+                    base_row += __shfl_sync(0xffffffffu, incl, 31);
+                }
+                if (lane == 0) S.gstart[nref] = base_row;
+            }
+        } else {
+            for (uint32_t k = tid; k < nT && !split; k += kTcThreads) S.run[k] = -1.0;
+        }
+        if (tid == 0) S.sparse = 0;
+        __syncthreads();
+        const CmpDigest A = P.digests[rs][group ? S.gref[0] : U.ref];
+        const bool fastA = (A.flags & kDigestFast) != 0;
+        const uint32_t nch = fastA ? 4 : kTcChunks;  // fast mode: the first 64 bytes
+
+        for (uint32_t rc = U.r0; rc < U.r1 && ok; rc += kTcRows) {
+            // ---- reference rows of this pass (threads 0..127)
+            const uint32_t row = rc + tid;
+            const bool have = tid < kTcRows && row < U.r1;
+            uint32_t s1 = 0, e1 = 0, gk = 0;
+            uint32_t fidx = A.first + row;
+            if (group && have) {
+                uint32_t lo = 0, hi = nref;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (S.gstart[mid] <= row) lo = mid;
+                    else hi = mid;
+                }
+                gk = lo;
+                fidx = P.digests[rs][S.gref[gk]].first + (row - S.gstart[gk]);
+            }
+            if (have) {
+                const uint32_t m = P.meta[rs][fidx];
+                s1 = m & 0xFFFFu;
+                e1 = m >> 16;
+            }
+            if (tid < kTcRows) S.rowf[tid] = have ? fidx : 0xFFFFFFFFu;
+            const bool active = have && s1 >= (uint32_t)kMinElem;
+            if (group && have && !active) atomicAdd(&S.gsparse[gk], 1u);
+            const uint32_t nsparse = __syncthreads_count(have && !active);
+            if (tid == 0) {
+                S.sparse += nsparse;
+                S.cur_t = 0;
+                S.cur_f = 0;
+            }
+            uint32_t bnum = 0, bden = 1;
+            bool counted = false;
+            const uint32_t nrows = min((uint32_t)kTcRows, U.r1 - rc);
+            const uint32_t* arow = P.filters[rs] + (size_t)fidx * 64;
+            __syncthreads();
+            for (;;) {
+                const bool more = S.cur_t < nT;
+                __syncthreads();
+                if (!more) break;
+                // ---- tile composition (warp 0): up to 32 targets, up to 256 filters
+                if (tid < 32) {
+                    const uint32_t te = S.cur_t + lane;
+                    const uint32_t f0 = lane == 0 ? S.cur_f : 0;
+                    uint32_t rem = 0, first = 0;
+                    if (te < nT) {
+                        const CmpDigest B = P.digests[ts][P.targets[U.t0 + te]];
+                        rem = B.nfilters - f0;
+                        first = B.first + f0;
+                    }
+                    uint32_t incl = rem;
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+                        if (lane >= (uint32_t)d) incl += v;
+                    }
+                    const uint32_t excl = incl - rem;
+                    const bool done_here = rem > 0 && incl <= (uint32_t)kTcCols;
+                    for (uint32_t s = excl; s < min(incl, (uint32_t)kTcCols); s++) {
+                        const uint32_t f = first + (s - excl);
+                        S.gidx[s] = f;
+                        S.tmeta[s] = P.meta[ts][f];
+                        S.tinfo[s] = te | (lane << 16) | ((done_here && s + 1 == incl) ? 0x80000000u : 0u);
+                    }
+                    if (done_here) S.comp[lane] = te;
+                    const uint32_t done_mask = __ballot_sync(0xffffffffu, done_here);
+                    const uint32_t over_mask = __ballot_sync(0xffffffffu, rem > 0 && incl > (uint32_t)kTcCols);
+                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                    const uint32_t l = over_mask ? (uint32_t)(__ffs(over_mask) - 1) : 32u;
+                    const uint32_t ex_l = __shfl_sync(0xffffffffu, excl, l & 31);
+                    const uint32_t f0_l = __shfl_sync(0xffffffffu, f0, l & 31);
+                    if (lane == 0) {
+                        S.ncomp = __popc(done_mask);
+                        S.ntile = min(total, (uint32_t)kTcCols);
+                        if (l < 32) {
+                            S.cur_t += l;
+                            S.cur_f = f0_l + ((uint32_t)kTcCols - ex_l);
+                        } else {
+                            S.cur_t = min(S.cur_t + 32u, nT);
+                            S.cur_f = 0;
+                        }
+                    }
+                }
+                __syncthreads();
+                const uint32_t nt = S.ntile;
+                const uint32_t ncols = (nt + 15) & ~15u;  // MMA N: multiple of 16
+                const uint32_t idesc = (1u << 4) | ((ncols >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+                // ---- counts: widen chunk c into a stage, MMA it
+                for (uint32_t c = 0; c < nch; c++) {
+                    const uint32_t s = (uses[0] + uses[1]) & 1;
+                    if (uses[s] > 0) ok = mbar_wait(smem_addr(&S.mbar[s]), (uses[s] - 1) & 1);
+                    ok = __syncthreads_and(ok);
+                    if (!ok) break;
+                    uint8_t* sa = stages + s * kTcStage;
+                    uint8_t* sb = sa + kTcAStage;
+                    for (uint32_t i = tid; i < kTcRows + ncols; i += kTcThreads) {
+                        uint4 bits = make_uint4(0, 0, 0, 0);
+                        if (i < kTcRows) {
+                            const uint32_t f = S.rowf[i];
+                            if (f != 0xFFFFFFFFu)
+                                bits = __ldg(reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)f * 64) + c);
+                            widen_row(sa, i, bits);
+                        } else {
+                            const uint32_t j = i - kTcRows;
+                            if (j < nt) bits = __ldg(reinterpret_cast<const uint4*>(P.filters[ts] + (size_t)S.gidx[j] * 64) + c);
+                            widen_row(sb, j, bits);
+                        }
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncthreads();
+                    if (tid == 0) {
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        const uint32_t a0 = smem_addr(sa), b0 = smem_addr(sb);
+#pragma unroll
+                        for (uint32_t kk = 0; kk < kTcChunk / 32; kk++) {
+                            const uint64_t ad = sw128_desc(a0 + kk * 32), bd = sw128_desc(b0 + kk * 32);
+                            const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+                            asm volatile(
+                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                        }
+                        mma_commit(smem_addr(&S.mbar[s]));
+                    }
+                    uses[s]++;
+                }
+                if (!ok) break;
+                if (tid == 0) mma_commit(smem_addr(&S.mbar[2]));
+                ok = mbar_wait(smem_addr(&S.mbar[2]), done_phase & 1);
+                done_phase++;
+                ok = __syncthreads_and(ok);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                // ---- score the tile: row threads read their counts from TMEM
+                if (warp < 4) {
+                    auto consume = [&](uint32_t j, uint32_t cnt) {
+                        const uint32_t tm = S.tmeta[j];
+                        const uint32_t s2 = tm & 0xFFFFu;
+                        if (active && s2 >= (uint32_t)kMinElem) {
+                            uint32_t cut, match = cnt;
+                            const uint32_t* trow = P.filters[ts] + (size_t)S.gidx[j] * 64;
+                            if (!fastA) {
+                                cut = cut_for(S.cut_sum, S.cut256, s1, s2);
+                                if (match > cut && staged_exit_mem(arow, trow, cut)) match = 0;
+                            } else {
+                                const uint32_t sum = s1 + s2;
+                                cut = sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum];
+                                if (match > cut && 2 * popc8_mem(arow, trow) + 48 < cut) match = 0;
+                            }
+                            uint32_t num = 0, den = 1;
+                            if (match > cut) {
+                                num = match - cut;
+                                den = min(e1, tm >> 16) - cut;
+                            }
+                            if (!counted || (uint64_t)num * bden > (uint64_t)bnum * den) {
+                                bnum = num;
+                                bden = den;
+                                counted = true;
+                            }
+                        }
+                        const uint32_t info = S.tinfo[j];
+                        if (info & 0x80000000u) {
+                            const double m = max_value(active, bnum, bden, counted);
+                            if (split) {
+                                if (have) P.slots[P.split[U.split].slot_base + row] = m;
+                            } else {
+                                S.mv[tid][(info >> 16) & 0x7FFFu] = m;
+                            }
+                            bnum = 0;
+                            bden = 1;
+                            counted = false;
+                        }
+                    };
+                    for (uint32_t c0 = 0; c0 < nt; c0 += 32) {
+                        uint32_t v[32];
+                        const uint32_t taddr = tmem + ((warp * 32) << 16) + c0;
+                        asm volatile(
+                            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+                            "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+                              "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+                              "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+                              "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+                              "=r"(v[31])
+                            : "r"(taddr));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;");
+                        const uint32_t lim = min(32u, nt - c0);
+#pragma unroll
+                        for (uint32_t k = 0; k < 32; k++)
+                            if (k < lim) consume(c0 + k, (uint32_t)__uint_as_float(v[k]));
+                    }
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                __syncthreads();
+                // ---- fold the completed targets' maxima in filter order
+                if (group) {
+                    const uint32_t ncomp = S.ncomp;
+                    for (uint32_t t = tid; t < ncomp * nref; t += kTcThreads) {
+                        const uint32_t k = t % nref, col = t / nref;
+                        double sum = -1.0;
+                        for (uint32_t r = S.gstart[k]; r < S.gstart[k + 1]; r++) {
+                            const double m = S.mv[r][col];
+                            if (sum < 0) sum = m;
+                            else if (m != 0.0) sum = __dadd_rn(sum, m);
+                        }
+                        const uint32_t tgt = P.targets[U.t0 + S.comp[col]];
+                        P.scores[out_index(P, rs != 0, S.gref[k], tgt)] =
+                            final_score(sum, S.gstart[k + 1] - S.gstart[k], S.gsparse[k]);
+                    }
+                } else if (!split) {
+                    for (uint32_t k = tid; k < S.ncomp; k += kTcThreads) {
+                        double sum = S.run[S.comp[k]];
+                        for (uint32_t r = 0; r < nrows; r++) {
+                            const double m = S.mv[r][k];
+                            if (sum < 0) sum = m;
+                            else if (m != 0.0) sum = __dadd_rn(sum, m);
+                        }
+                        S.run[S.comp[k]] = sum;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        if (!ok) break;
+        if (!split && !group) {
+            for (uint32_t k = tid; k < nT; k += kTcThreads) {
+                const uint32_t tgt = P.targets[U.t0 + k];
+                P.scores[out_index(P, rs != 0, U.ref, tgt)] = final_score(S.run[k], A.nfilters, S.sparse);
+            }
+        }
+    }
+    if (!ok) {
+        if (tid == 0) {
+            atomicAdd(P.error, 1u);
+            // wait (bounded) for any MMA still reading shared memory or writing TMEM
+            mma_commit(smem_addr(&S.mbar[2]));
+            mbar_wait(smem_addr(&S.mbar[2]), done_phase & 1);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
+}
+
+cudaError_t launch_matrix_tc(const MatParams& P, uint32_t grid, cudaStream_t st) {
+    if (P.nunits == 0) return cudaSuccess;
+    k_matrix_tc<<<grid, kTcThreads, kTcSmemBytes, st>>>(P);
+    return cudaGetLastError();
+}
+
+int matrix_tc_ctas_per_sm() {
+    cudaFuncSetAttribute(k_matrix_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemBytes);
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_matrix_tc, kTcThreads, kTcSmemBytes);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace sdbfg

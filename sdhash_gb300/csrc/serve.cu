@@ -149,7 +149,7 @@ static cudaError_t launch_batch(sdbfg_server* sv, sdbfg_server::Slot& S) {
     if (S.nsplit &&
         (e = cudaMemcpyAsync(S.d_split.p, S.h_split.p, S.nsplit * sizeof(MatSplit), cudaMemcpyHostToDevice, st)))
         return e;
-    if ((e = cudaMemsetAsync(S.d_counter.p, 0, 4, st))) return e;
+    if ((e = cudaMemsetAsync(S.d_counter.p, 0, 8, st))) return e;  // work counter, error flag
     MatParams P{};
     P.filters[0] = S.d_filters.as<uint32_t>();
     P.meta[0] = S.d_meta.as<uint32_t>();
@@ -170,6 +170,7 @@ static cudaError_t launch_batch(sdbfg_server* sv, sdbfg_server::Slot& S) {
     P.n = nt;
     P.cutoffs = sv->ctx->d_cut.as<uint16_t>();
     P.cutoffs64 = sv->ctx->d_cut64.as<uint16_t>();
+    P.error = S.d_counter.as<uint32_t>() + 1;
     const uint32_t grid = (uint32_t)std::min<uint64_t>(ctas, std::max(1u, S.nunits));
     if ((e = launch_matrix(P, sv->ctx->mat_variant, grid, st))) return e;
     if ((e = launch_matrix_finalize(P, st))) return e;

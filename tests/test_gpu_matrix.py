@@ -30,7 +30,7 @@ def uneven(ctx, oracle):
     return ds, ods, want_all[iu]
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("unit_work", [1 << 12, 1 << 22])
 def test_all_pairs_every_variant_and_budget(ctx, uneven, variant, unit_work):
     ds, ods, want = uneven
@@ -39,23 +39,52 @@ def test_all_pairs_every_variant_and_budget(ctx, uneven, variant, unit_work):
         dev = ctx.upload(ds)
         got = ctx.compare_all(dev)
     finally:
-        ctx.set_compare_tuning(0, 1 << 22, True)
+        ctx.set_compare_tuning(5, 1 << 22, True)
     assert np.array_equal(got, want)
     assert (want > 0).sum() > 20  # related pairs present
 
 
-def test_cross_with_split_pairs(ctx, oracle, uneven):
+@pytest.mark.parametrize("variant", [3, 5])
+def test_cross_with_split_pairs(ctx, oracle, uneven, variant):
     """A unit budget below single-pair sizes row-splits pairs; the maxima go
     through the slot array and the finalize kernel."""
     ds, ods, _ = uneven
     q, t = ds[::3], ds[1::2]
     want = oracle.score_cross_matrix([ods[i] for i in range(0, len(ds), 3)], [ods[i] for i in range(1, len(ds), 2)])
-    ctx.set_compare_tuning(3, 1 << 10, True)
+    ctx.set_compare_tuning(variant, 1 << 10, True)
     try:
         got = ctx.compare_to(ctx.upload(q), ctx.upload(t))
     finally:
-        ctx.set_compare_tuning(0, 1 << 22, True)
+        ctx.set_compare_tuning(5, 1 << 22, True)
     assert np.array_equal(got, want)
+
+
+def test_tensor_core_counts_on_dense_and_sparse_filters(ctx, oracle):
+    """Counts near the extremes (all-ones, empty and single-bit filters) and
+    tiles of every width 1..256 through the tensor-core variant."""
+    import sdhash_gb300 as g
+    rng = np.random.default_rng(9)
+    ds = []
+    for i, n in enumerate([1, 2, 15, 16, 17, 31, 33, 100, 255, 256, 257, 300]):
+        f = (rng.random((n, 256)) < rng.uniform(0.05, 0.6)).astype(np.uint8) * rng.integers(1, 256, (n, 256),
+                                                                                           dtype=np.uint8)
+        if i == 3:
+            f[0] = 0xFF
+        if i == 4:
+            f[:] = 0
+            f[:, 7] = 1
+        counts = rng.integers(0, 193, n).astype(np.uint16)
+        ds.append(g.Digest(f"x{i:02d}", 0, n, 0, 192, 16384, f.reshape(-1), counts))
+    ods = [oracle.parse(d.to_string()) for d in ds]
+    want = oracle.score_all_matrix(ods)
+    iu = np.triu_indices(len(ds), 1)
+    dev = ctx.upload(ds)
+    for v in (0, 5):
+        ctx.set_compare_tuning(v, 1 << 22, False)
+        try:
+            assert np.array_equal(ctx.compare_all(dev), want[iu]), v
+        finally:
+            ctx.set_compare_tuning(5, 1 << 22, True)
 
 
 def test_graph_replay_and_device_output(ctx, uneven):
@@ -82,11 +111,11 @@ def test_autotuner_keeps_results(ctx, uneven):
     dev = ctx.upload(ds)
     v, w, rate = ctx.autotune_compare(dev, sample_pairs=1 << 20)
     try:
-        assert 0 <= v < 5 and w in (1 << 20, 1 << 22, 1 << 24) and rate > 0
+        assert 0 <= v < 6 and w in (1 << 20, 1 << 22, 1 << 24) and rate > 0
         assert ctx.compare_tuning() == (v, w)
         assert np.array_equal(ctx.compare_all(dev), want)
     finally:
-        ctx.set_compare_tuning(0, 1 << 22, True)
+        ctx.set_compare_tuning(5, 1 << 22, True)
 
 
 def test_plain_per_pair_path_agrees(ctx, uneven):
