@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
     ap.add_argument("--plain-pairs", type=int, default=400, help="allpairs: pairs timed one call each")
     ap.add_argument("--cpu-pairs", type=int, default=256, help="allpairs: pairs timed on the host (oracle)")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="comparison kernel variant (0-4 CUDA cores, 5 tensor cores); -1: autotune")
     return ap.parse_args()
 
 
@@ -309,7 +311,11 @@ def main_allpairs(args):
     out = torch.empty(npairs, dtype=torch.int32, device="cuda")
     # autotuner on a sample of the job's units (also the warm-up)
     t0 = time.perf_counter()
-    variant, unit_work, tuned_rate = ctx.autotune_compare(dev, sample_pairs=1 << 35)
+    if args.variant < 0:
+        variant, unit_work, tuned_rate = ctx.autotune_compare(dev, sample_pairs=1 << 35)
+    else:
+        ctx.set_compare_tuning(args.variant, 1 << 22, True)
+        (variant, unit_work), tuned_rate = ctx.compare_tuning(), None
     t_tune = time.perf_counter() - t0
     for _ in range(args.warmup):  # a capture-and-replay run of the full job
         ctx.compare_all_device(dev, out.data_ptr())
@@ -502,7 +508,11 @@ def main_image(args):
     fpairs = ctx.filter_pairs(qset, iset)
     scores_dev = torch.empty(args.queries * nseg, dtype=torch.int32, device="cuda")
     t0 = time.perf_counter()
-    variant, unit_work, tuned = ctx.autotune_compare(qset, iset, sample_pairs=1 << 33)
+    if args.variant < 0:
+        variant, unit_work, tuned = ctx.autotune_compare(qset, iset, sample_pairs=1 << 33)
+    else:
+        ctx.set_compare_tuning(args.variant, 1 << 22, True)
+        variant, unit_work = ctx.compare_tuning()
     t_tune = time.perf_counter() - t0
     runc = lambda: ctx.compare_to_device(qset, iset, scores_dev.data_ptr())
     for _ in range(max(1, args.warmup)):
@@ -685,7 +695,13 @@ def main_serve(args):
     ref_filters = sum(d.bf_count for d in refs)
     qf = np.array([q.bf_count for q in pool])
     # solo scores of every pool query (one batched compare_to): the served rows must equal them
-    solo = ctx.compare_to(ctx.upload(pool), tset)
+    poolset = ctx.upload(pool)
+    if args.variant < 0:
+        tuned = ctx.autotune_compare(poolset, tset, sample_pairs=1 << 33)
+    else:
+        ctx.set_compare_tuning(args.variant, 1 << 22, True)
+        tuned = ctx.compare_tuning()
+    solo = ctx.compare_to(poolset, tset)
     srv = g.Server(ctx, tset, slots=3, max_batch_queries=64, memory_budget=1 << 30, threshold=1)
     try:
         warm, _, _ = poisson_run(srv, pool, args.rate, 64, seed=1)
@@ -747,7 +763,7 @@ def main_serve(args):
                        "query_pool": len(pool), "query_filters": f"{int(qf.min())}..{int(qf.max())} "
                        f"(mean {qf.mean():.0f}, median {np.median(qf):.0f})", "offered_rate_qps": args.rate,
                        "queries": args.serve_queries, "slots": 3, "max_batch_queries": 64, "memory_budget": 1 << 30,
-                       "threshold": 1, "build_s": round(t_build, 1)},
+                       "threshold": 1, "build_s": round(t_build, 1), "tuning": list(tuned)},
             "latency_at_offered_rate": sa,
             "latency_at_70pct_of_capacity": dict(sb, offered_rate_qps=rate_b),
             "filter_pairs_per_s": float(qf[order_a].sum()) * ref_filters / (

@@ -46,8 +46,11 @@ constexpr uint32_t kTcAStage = kTcRows * kTcChunk;   // 16 KB of e4m3
 constexpr uint32_t kTcBStage = kTcCols * kTcChunk;   // 32 KB
 constexpr uint32_t kTcStage = kTcAStage + kTcBStage;
 constexpr uint32_t kTcWaitSpins = 1u << 22;
+constexpr int kTcBitSlots = 3;  // chunks of filter bits in flight (cp.async ring)
 
 struct TcSmem {
+    uint4 bits[kTcBitSlots][kTcRows + kTcCols];  // 16 filter bytes per row per chunk
+    uint32_t lastmask[kTcCols / 32];           // columns where a target ends
     uint32_t gidx[kTcCols], tmeta[kTcCols], tinfo[kTcCols];
     uint32_t rowf[kTcRows];           // filter index of each reference row (~0: none)
     uint32_t comp[kTcMaxComp];
@@ -138,6 +141,36 @@ __device__ __forceinline__ uint32_t popc8_mem(const uint32_t* a, const uint32_t*
         c += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
     }
     return c;
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait2() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
+
+// filter bits of chunk c for the rows this thread widens (the same thread
+// copies and widens a row, so only its own copies need to have landed)
+__device__ __forceinline__ void fetch_chunk(const MatParams& P, TcSmem& S, uint32_t rs, uint32_t ts, uint32_t c,
+                                            uint32_t nt, uint32_t ncols, uint32_t tid) {
+    uint4* slot = S.bits[c % kTcBitSlots];
+    for (uint32_t i = tid; i < kTcRows + ncols; i += kTcThreads) {
+        if (i < kTcRows) {
+            const uint32_t f = S.rowf[i];
+            if (f != 0xFFFFFFFFu) cp_async16(slot + i, P.filters[rs] + (size_t)f * 64 + c * 4);
+        } else if (i - kTcRows < nt) {
+            cp_async16(slot + i, P.filters[ts] + (size_t)S.gidx[i - kTcRows] * 64 + c * 4);
+        }
+    }
+    cp_async_commit();
+}
+
+// a pair whose full count is above the cut: the reference's staged exits
+// (normal mode) or its 32-byte stage (fast mode), from the filters in memory
+__device__ __noinline__ uint32_t candidate_match(const uint32_t* arow, const uint32_t* trow, uint32_t cnt,
+                                                 uint32_t cut, bool fast) {
+    if (!fast) return staged_exit_mem(arow, trow, cut) ? 0u : cnt;
+    return 2 * popc8_mem(arow, trow) + 48 < cut ? 0u : cnt;
 }
 
 }  // namespace
@@ -310,24 +343,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                 const uint32_t nt = S.ntile;
                 const uint32_t ncols = (nt + 15) & ~15u;  // MMA N: multiple of 16
                 const uint32_t idesc = (1u << 4) | ((ncols >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
-                // ---- counts: widen chunk c into a stage, MMA it
+                if (tid < kTcCols / 32) {
+                    uint32_t m = 0;
+                    for (uint32_t b = 0; b < 32; b++) {
+                        const uint32_t j = tid * 32 + b;
+                        if (j < nt && (S.tinfo[j] & 0x80000000u)) m |= 1u << b;
+                    }
+                    S.lastmask[tid] = m;
+                }
+                // ---- counts: widen chunk c into a stage, MMA it; bits of chunks
+                // c+1, c+2 are on their way (cp.async ring)
+                fetch_chunk(P, S, rs, ts, 0, nt, ncols, tid);
+                if (nch > 1) fetch_chunk(P, S, rs, ts, 1, nt, ncols, tid);
                 for (uint32_t c = 0; c < nch; c++) {
+                    if (c + 2 < nch) fetch_chunk(P, S, rs, ts, c + 2, nt, ncols, tid);
+                    else cp_async_commit();  // keep one group per chunk
+                    cp_async_wait2();        // this thread's copies of chunk c have landed
                     const uint32_t s = (uses[0] + uses[1]) & 1;
                     if (uses[s] > 0) ok = mbar_wait(smem_addr(&S.mbar[s]), (uses[s] - 1) & 1);
                     ok = __syncthreads_and(ok);
                     if (!ok) break;
                     uint8_t* sa = stages + s * kTcStage;
                     uint8_t* sb = sa + kTcAStage;
+                    const uint4* slot = S.bits[c % kTcBitSlots];
                     for (uint32_t i = tid; i < kTcRows + ncols; i += kTcThreads) {
                         uint4 bits = make_uint4(0, 0, 0, 0);
                         if (i < kTcRows) {
-                            const uint32_t f = S.rowf[i];
-                            if (f != 0xFFFFFFFFu)
-                                bits = __ldg(reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)f * 64) + c);
+                            if (S.rowf[i] != 0xFFFFFFFFu) bits = slot[i];
                             widen_row(sa, i, bits);
                         } else {
                             const uint32_t j = i - kTcRows;
-                            if (j < nt) bits = __ldg(reinterpret_cast<const uint4*>(P.filters[ts] + (size_t)S.gidx[j] * 64) + c);
+                            if (j < nt) bits = slot[i];
                             widen_row(sb, j, bits);
                         }
                     }
@@ -358,38 +404,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 // ---- score the tile: row threads read their counts from TMEM
                 if (warp < 4) {
-                    auto consume = [&](uint32_t j, uint32_t cnt) {
+                    uint32_t cs2 = 0xFFFFFFFFu, ccut = 0;  // cut cached for the last s2 seen
+                    auto consume = [&](uint32_t j, uint32_t cnt, bool last) {
                         const uint32_t tm = S.tmeta[j];
                         const uint32_t s2 = tm & 0xFFFFu;
                         if (active && s2 >= (uint32_t)kMinElem) {
-                            uint32_t cut, match = cnt;
-                            const uint32_t* trow = P.filters[ts] + (size_t)S.gidx[j] * 64;
-                            if (!fastA) {
-                                cut = cut_for(S.cut_sum, S.cut256, s1, s2);
-                                if (match > cut && staged_exit_mem(arow, trow, cut)) match = 0;
-                            } else {
+                            if (s2 != cs2) {
+                                cs2 = s2;
                                 const uint32_t sum = s1 + s2;
-                                cut = sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum];
-                                if (match > cut && 2 * popc8_mem(arow, trow) + 48 < cut) match = 0;
+                                ccut = !fastA ? cut_for(S.cut_sum, S.cut256, s1, s2)
+                                              : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
                             }
-                            uint32_t num = 0, den = 1;
-                            if (match > cut) {
-                                num = match - cut;
-                                den = min(e1, tm >> 16) - cut;
-                            }
-                            if (!counted || (uint64_t)num * bden > (uint64_t)bnum * den) {
-                                bnum = num;
-                                bden = den;
-                                counted = true;
+                            counted = true;  // a counted target filter scores at least 0
+                            if (cnt > ccut) {
+                                const uint32_t match = candidate_match(arow, P.filters[ts] + (size_t)S.gidx[j] * 64,
+                                                                       cnt, ccut, fastA);
+                                if (match > ccut) {
+                                    const uint32_t num = match - ccut, den = min(e1, tm >> 16) - ccut;
+                                    if ((uint64_t)num * bden > (uint64_t)bnum * den) {
+                                        bnum = num;
+                                        bden = den;
+                                    }
+                                }
                             }
                         }
-                        const uint32_t info = S.tinfo[j];
-                        if (info & 0x80000000u) {
+                        if (last) {
                             const double m = max_value(active, bnum, bden, counted);
                             if (split) {
                                 if (have) P.slots[P.split[U.split].slot_base + row] = m;
                             } else {
-                                S.mv[tid][(info >> 16) & 0x7FFFu] = m;
+                                S.mv[tid][(S.tinfo[j] >> 16) & 0x7FFFu] = m;
                             }
                             bnum = 0;
                             bden = 1;
@@ -411,9 +455,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             : "r"(taddr));
                         asm volatile("tcgen05.wait::ld.sync.aligned;");
                         const uint32_t lim = min(32u, nt - c0);
+                        const uint32_t lm = S.lastmask[c0 >> 5];
 #pragma unroll
                         for (uint32_t k = 0; k < 32; k++)
-                            if (k < lim) consume(c0 + k, (uint32_t)__uint_as_float(v[k]));
+                            if (k < lim) consume(c0 + k, (uint32_t)__uint_as_float(v[k]), (lm >> k) & 1u);
                     }
                 }
                 asm volatile("tcgen05.fence::before_thread_sync;");
@@ -455,6 +500,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
             }
         }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     if (!ok) {
         if (tid == 0) {
             atomicAdd(P.error, 1u);
