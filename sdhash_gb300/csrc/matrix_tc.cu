@@ -4,17 +4,20 @@
 // vectors.  With each bit widened to an e4m3 byte (1.0 = 0x38 or 0) and fp32
 // accumulation, tcgen05.mma computes it exactly (every partial sum is an
 // integer <= 2048).  One CTA multiplies 128 reference filters (TMEM lanes)
-// by up to 256 target filters (TMEM columns) over K = 2048 in 16 chunks of
-// 128: all 256 threads widen the chunk's bits into a 128-byte-swizzled
-// shared-memory stage (two stages, so widening overlaps the MMAs of the
-// previous chunk), one thread issues the four K=32 MMAs and commits them to
-// the stage's mbarrier.  The 128 row threads then read their row of counts
-// from TMEM and score the tile exactly as the CUDA-core kernel does
-// (compare_kernels.cu k_matrix): a pair can score above 0 only if its full
-// count exceeds the cut, and for those rare pairs the reference's staged
-// exits (bf_utils.cc:114-206) are rechecked from the filters in memory.
-// Work units, group units, running sums and split pairs are those of
-// k_matrix.
+// by tiles of up to 256 target filters (TMEM columns) over K = 2048 in 16
+// chunks of 128.  The CTA is a two-stage software pipeline: warps 4-7
+// compose tile g, fetch its filter bits with cp.async, widen each chunk into
+// a 128-byte-swizzled shared-memory stage (two stages, so widening overlaps
+// the MMAs of the previous chunk) and issue the four K=32 MMAs per chunk into
+// accumulator g & 1 (512 TMEM columns hold two); meanwhile warps 0-3 read
+// tile g-1's counts from the other accumulator, one row per thread, and
+// score it exactly as the CUDA-core kernel does (compare_kernels.cu
+// k_matrix): a pair can score above 0 only if its full count exceeds the
+// cut, and for those rare pairs the reference's staged exits
+// (bf_utils.cc:114-206) are rechecked from the filters in memory.  Maxima of
+// completed targets collect in a 32-column ring and are summed in filter
+// order as it fills.  Work units, group units, running sums and split pairs
+// are those of k_matrix.
 //
 // The widening permutes K inside each 32-bit word (output word k of a word
 // w holds bits k, k+8, k+16, k+24 of w), identically for both operands, so
@@ -38,29 +41,35 @@ namespace {
 
 constexpr int kTcRows = 128;       // reference rows per pass = TMEM lanes
 constexpr int kTcCols = 256;       // target filters per tile = MMA N (max)
-constexpr int kTcThreads = 256;
+constexpr int kTcThreads = 256;    // warps 0-3 score (one row each), warps 4-7 widen and issue
 constexpr int kTcChunk = 128;      // K elements (bits) per stage
 constexpr int kTcChunks = 2048 / kTcChunk;
-constexpr int kTcMaxComp = 32;     // targets completed per tile
+constexpr int kTcRing = 32;        // completed targets held before their maxima are summed
 constexpr uint32_t kTcAStage = kTcRows * kTcChunk;   // 16 KB of e4m3
 constexpr uint32_t kTcBStage = kTcCols * kTcChunk;   // 32 KB
 constexpr uint32_t kTcStage = kTcAStage + kTcBStage;
 constexpr uint32_t kTcWaitSpins = 1u << 22;
-constexpr int kTcBitSlots = 3;  // chunks of filter bits in flight (cp.async ring)
+constexpr int kTcBitSlots = 3;     // chunks of filter bits in flight (cp.async ring)
+
+// one tile's composition (double-buffered: warps 4-7 compose and count tile
+// k while warps 0-3 score tile k-1)
+struct TcTile {
+    uint32_t gidx[kTcCols], tmeta[kTcCols], tinfo[kTcCols], comp[kTcCols];
+    uint32_t lastmask[kTcCols / 32];
+    uint32_t ntile, ncomp, produced, pad;
+};
 
 struct TcSmem {
     uint4 bits[kTcBitSlots][kTcRows + kTcCols];  // 16 filter bytes per row per chunk
-    uint32_t lastmask[kTcCols / 32];           // columns where a target ends
-    uint32_t gidx[kTcCols], tmeta[kTcCols], tinfo[kTcCols];
+    TcTile tile[2];
     uint32_t rowf[kTcRows];           // filter index of each reference row (~0: none)
-    uint32_t comp[kTcMaxComp];
-    double mv[kTcRows][kTcMaxComp + 1];
+    double mv[kTcRows][kTcRing + 1];  // row maxima of completed targets (ring)
     double run[kMatMaxTargets];
     uint32_t gref[kTcRows], gstart[kTcRows + 1], gsparse[kTcRows];
     uint16_t cut_sum[1024], cut64_sum[1024], cut256[SDBF_CUTOFF_BINS], cut64[SDBF_CUTOFF_BINS];
     MatUnit unit;
-    uint32_t unit_id, ntile, ncomp, cur_t, cur_f, sparse, tmem;
-    alignas(8) uint64_t mbar[3];      // stage 0, stage 1, accumulator complete
+    uint32_t unit_id, cur_t, cur_f, sparse, tmem;
+    alignas(8) uint64_t mbar[5];      // stage 0, stage 1 emptied; accumulator 0, 1 full; drain
 };
 
 constexpr size_t kTcSmemBytes = 1024 /* alignment */ + 2 * kTcStage + sizeof(TcSmem);
@@ -149,22 +158,6 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait2() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
 
-// filter bits of chunk c for the rows this thread widens (the same thread
-// copies and widens a row, so only its own copies need to have landed)
-__device__ __forceinline__ void fetch_chunk(const MatParams& P, TcSmem& S, uint32_t rs, uint32_t ts, uint32_t c,
-                                            uint32_t nt, uint32_t ncols, uint32_t tid) {
-    uint4* slot = S.bits[c % kTcBitSlots];
-    for (uint32_t i = tid; i < kTcRows + ncols; i += kTcThreads) {
-        if (i < kTcRows) {
-            const uint32_t f = S.rowf[i];
-            if (f != 0xFFFFFFFFu) cp_async16(slot + i, P.filters[rs] + (size_t)f * 64 + c * 4);
-        } else if (i - kTcRows < nt) {
-            cp_async16(slot + i, P.filters[ts] + (size_t)S.gidx[i - kTcRows] * 64 + c * 4);
-        }
-    }
-    cp_async_commit();
-}
-
 // a pair whose full count is above the cut: the reference's staged exits
 // (normal mode) or its 32-byte stage (fast mode), from the filters in memory
 __device__ __noinline__ uint32_t candidate_match(const uint32_t* arow, const uint32_t* trow, uint32_t cnt,
@@ -175,12 +168,31 @@ __device__ __noinline__ uint32_t candidate_match(const uint32_t* arow, const uin
 
 }  // namespace
 
+// AND-reduction of a predicate over one 128-thread group (named barrier id)
+template <int ID>
+__device__ __forceinline__ bool group_and(bool v) {
+    uint32_t r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, 128, p;\n"
+                 " selp.u32 %0, 1, 0, q;\n}\n"
+                 : "=r"(r)
+                 : "r"((uint32_t)v), "n"(ID)
+                 : "memory");
+    return r != 0;
+}
+
+template <int ID>
+__device__ __forceinline__ void group_sync() {
+    asm volatile("bar.sync %0, 128;" ::"n"(ID) : "memory");
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
     extern __shared__ uint8_t tc_smem_raw[];
     const uint32_t raw = smem_addr(tc_smem_raw);
     uint8_t* stages = tc_smem_raw + (((raw + 1023) & ~1023u) - raw);
     TcSmem& S = *reinterpret_cast<TcSmem*>(stages + 2 * kTcStage);
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool producer = warp >= 4;
+    const uint32_t ptid = tid - 128;  // producers: 0..127
 
     for (uint32_t i = tid; i < 1024; i += kTcThreads) {
         S.cut_sum[i] = P.cutoffs[i >= 32 ? 4096u / i : (uint32_t)SDBF_CUTOFF_BINS - 1];
@@ -191,12 +203,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
         S.cut64[i] = P.cutoffs64[i];
     }
     if (tid == 0) {
-        for (int i = 0; i < 3; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&S.mbar[i])));
+        for (int i = 0; i < 5; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&S.mbar[i])));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    if (warp == 0) {
+    if (warp == 0) {  // two accumulators of 256 columns
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&S.tmem)),
-                     "r"(kTcCols));
+                     "r"(2 * kTcCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -204,8 +216,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = S.tmem;
 
-    uint32_t uses[2] = {0, 0};  // commits to each stage barrier so far
-    uint32_t done_phase = 0;     // commits to the accumulator barrier so far
+    uint32_t suses[2] = {0, 0};  // producers: commits to each stage barrier
+    uint32_t gtile = 0;          // tiles counted so far (all threads keep the same count)
     bool ok = true;
 
     for (;;) {
@@ -286,210 +298,255 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                 S.sparse += nsparse;
                 S.cur_t = 0;
                 S.cur_f = 0;
+                S.tile[0].produced = 0;
+                S.tile[1].produced = 0;
             }
             uint32_t bnum = 0, bden = 1;
             bool counted = false;
             const uint32_t nrows = min((uint32_t)kTcRows, U.r1 - rc);
             const uint32_t* arow = P.filters[rs] + (size_t)fidx * 64;
             __syncthreads();
+            // ---- software pipeline: each step counts tile g (producers) and
+            // scores tile g-1 (consumers); one CTA barrier per step.  Tile g
+            // uses accumulator and tile slot g & 1, so accumulator b's n-th use
+            // is tile 2n + b and its barrier parity is (g >> 1) & 1.
+            bool pending = false;  // a counted tile waits to be scored
             for (;;) {
-                const bool more = S.cur_t < nT;
-                __syncthreads();
-                if (!more) break;
-                // ---- tile composition (warp 0): up to 32 targets, up to 256 filters
-                if (tid < 32) {
-                    const uint32_t te = S.cur_t + lane;
-                    const uint32_t f0 = lane == 0 ? S.cur_f : 0;
-                    uint32_t rem = 0, first = 0;
-                    if (te < nT) {
-                        const CmpDigest B = P.digests[ts][P.targets[U.t0 + te]];
-                        rem = B.nfilters - f0;
-                        first = B.first + f0;
-                    }
-                    uint32_t incl = rem;
-#pragma unroll
-                    for (int d = 1; d < 32; d <<= 1) {
-                        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
-                        if (lane >= (uint32_t)d) incl += v;
-                    }
-                    const uint32_t excl = incl - rem;
-                    const bool done_here = rem > 0 && incl <= (uint32_t)kTcCols;
-                    for (uint32_t s = excl; s < min(incl, (uint32_t)kTcCols); s++) {
-                        const uint32_t f = first + (s - excl);
-                        S.gidx[s] = f;
-                        S.tmeta[s] = P.meta[ts][f];
-                        S.tinfo[s] = te | (lane << 16) | ((done_here && s + 1 == incl) ? 0x80000000u : 0u);
-                    }
-                    if (done_here) S.comp[lane] = te;
-                    const uint32_t done_mask = __ballot_sync(0xffffffffu, done_here);
-                    const uint32_t over_mask = __ballot_sync(0xffffffffu, rem > 0 && incl > (uint32_t)kTcCols);
-                    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-                    const uint32_t l = over_mask ? (uint32_t)(__ffs(over_mask) - 1) : 32u;
-                    const uint32_t ex_l = __shfl_sync(0xffffffffu, excl, l & 31);
-                    const uint32_t f0_l = __shfl_sync(0xffffffffu, f0, l & 31);
-                    if (lane == 0) {
-                        S.ncomp = __popc(done_mask);
-                        S.ntile = min(total, (uint32_t)kTcCols);
-                        if (l < 32) {
-                            S.cur_t += l;
-                            S.cur_f = f0_l + ((uint32_t)kTcCols - ex_l);
-                        } else {
-                            S.cur_t = min(S.cur_t + 32u, nT);
-                            S.cur_f = 0;
-                        }
-                    }
-                }
-                __syncthreads();
-                const uint32_t nt = S.ntile;
-                const uint32_t ncols = (nt + 15) & ~15u;  // MMA N: multiple of 16
-                const uint32_t idesc = (1u << 4) | ((ncols >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
-                if (tid < kTcCols / 32) {
-                    uint32_t m = 0;
-                    for (uint32_t b = 0; b < 32; b++) {
-                        const uint32_t j = tid * 32 + b;
-                        if (j < nt && (S.tinfo[j] & 0x80000000u)) m |= 1u << b;
-                    }
-                    S.lastmask[tid] = m;
-                }
-                // ---- counts: widen chunk c into a stage, MMA it; bits of chunks
-                // c+1, c+2 are on their way (cp.async ring)
-                fetch_chunk(P, S, rs, ts, 0, nt, ncols, tid);
-                if (nch > 1) fetch_chunk(P, S, rs, ts, 1, nt, ncols, tid);
-                for (uint32_t c = 0; c < nch; c++) {
-                    if (c + 2 < nch) fetch_chunk(P, S, rs, ts, c + 2, nt, ncols, tid);
-                    else cp_async_commit();  // keep one group per chunk
-                    cp_async_wait2();        // this thread's copies of chunk c have landed
-                    const uint32_t s = (uses[0] + uses[1]) & 1;
-                    if (uses[s] > 0) ok = mbar_wait(smem_addr(&S.mbar[s]), (uses[s] - 1) & 1);
-                    ok = __syncthreads_and(ok);
-                    if (!ok) break;
-                    uint8_t* sa = stages + s * kTcStage;
-                    uint8_t* sb = sa + kTcAStage;
-                    const uint4* slot = S.bits[c % kTcBitSlots];
-                    for (uint32_t i = tid; i < kTcRows + ncols; i += kTcThreads) {
-                        uint4 bits = make_uint4(0, 0, 0, 0);
-                        if (i < kTcRows) {
-                            if (S.rowf[i] != 0xFFFFFFFFu) bits = slot[i];
-                            widen_row(sa, i, bits);
-                        } else {
-                            const uint32_t j = i - kTcRows;
-                            if (j < nt) bits = slot[i];
-                            widen_row(sb, j, bits);
-                        }
-                    }
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    __syncthreads();
-                    if (tid == 0) {
-                        asm volatile("tcgen05.fence::after_thread_sync;");
-                        const uint32_t a0 = smem_addr(sa), b0 = smem_addr(sb);
-#pragma unroll
-                        for (uint32_t kk = 0; kk < kTcChunk / 32; kk++) {
-                            const uint64_t ad = sw128_desc(a0 + kk * 32), bd = sw128_desc(b0 + kk * 32);
-                            const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
-                            asm volatile(
-                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                                " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-                        }
-                        mma_commit(smem_addr(&S.mbar[s]));
-                    }
-                    uses[s]++;
-                }
-                if (!ok) break;
-                if (tid == 0) mma_commit(smem_addr(&S.mbar[2]));
-                ok = mbar_wait(smem_addr(&S.mbar[2]), done_phase & 1);
-                done_phase++;
-                ok = __syncthreads_and(ok);
-                if (!ok) break;
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                // ---- score the tile: row threads read their counts from TMEM
-                if (warp < 4) {
-                    uint32_t cs2 = 0xFFFFFFFFu, ccut = 0;  // cut cached for the last s2 seen
-                    auto consume = [&](uint32_t j, uint32_t cnt, bool last) {
-                        const uint32_t tm = S.tmeta[j];
-                        const uint32_t s2 = tm & 0xFFFFu;
-                        if (active && s2 >= (uint32_t)kMinElem) {
-                            if (s2 != cs2) {
-                                cs2 = s2;
-                                const uint32_t sum = s1 + s2;
-                                ccut = !fastA ? cut_for(S.cut_sum, S.cut256, s1, s2)
-                                              : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                const uint32_t b = gtile & 1;  // tile gtile is counted into accumulator / tile slot b
+                if (producer) {
+                    TcTile& T = S.tile[b];
+                    if (warp == 4) {  // compose tile k: up to 256 filters of up to 256 targets
+                        uint32_t filled = 0, ncomp = 0, ct = S.cur_t, cf = S.cur_f;
+                        while (filled < (uint32_t)kTcCols && ct < nT) {
+                            const uint32_t te = ct + lane;
+                            const uint32_t f0 = lane == 0 ? cf : 0;
+                            uint32_t rem = 0, first = 0;
+                            if (te < nT) {
+                                const CmpDigest B = P.digests[ts][P.targets[U.t0 + te]];
+                                rem = B.nfilters - f0;
+                                first = B.first + f0;
                             }
-                            counted = true;  // a counted target filter scores at least 0
-                            if (cnt > ccut) {
-                                const uint32_t match = candidate_match(arow, P.filters[ts] + (size_t)S.gidx[j] * 64,
-                                                                       cnt, ccut, fastA);
-                                if (match > ccut) {
-                                    const uint32_t num = match - ccut, den = min(e1, tm >> 16) - ccut;
-                                    if ((uint64_t)num * bden > (uint64_t)bnum * den) {
-                                        bnum = num;
-                                        bden = den;
-                                    }
+                            uint32_t incl = rem;
+#pragma unroll
+                            for (int d = 1; d < 32; d <<= 1) {
+                                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+                                if (lane >= (uint32_t)d) incl += v;
+                            }
+                            const uint32_t excl = incl - rem, room = (uint32_t)kTcCols - filled;
+                            const bool done_here = rem > 0 && incl <= room;
+                            for (uint32_t s = excl; s < min(incl, room); s++) {
+                                const uint32_t slot = filled + s, f = first + (s - excl);
+                                T.gidx[slot] = f;
+                                T.tmeta[slot] = P.meta[ts][f];
+                                T.tinfo[slot] = te | ((ncomp + lane) << 16) |
+                                                ((done_here && s + 1 == incl) ? 0x80000000u : 0u);
+                            }
+                            if (done_here) T.comp[ncomp + lane] = te;
+                            const uint32_t done_mask = __ballot_sync(0xffffffffu, done_here);
+                            const uint32_t over_mask = __ballot_sync(0xffffffffu, rem > 0 && incl > room);
+                            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+                            ncomp += __popc(done_mask);
+                            if (over_mask) {
+                                const uint32_t l = __ffs(over_mask) - 1;
+                                const uint32_t ex_l = __shfl_sync(0xffffffffu, excl, l);
+                                const uint32_t f0_l = __shfl_sync(0xffffffffu, f0, l);
+                                ct += l;
+                                cf = f0_l + (room - ex_l);
+                                filled = kTcCols;
+                            } else {
+                                ct = min(ct + 32u, nT);
+                                cf = 0;
+                                filled += total;
+                            }
+                        }
+                        __syncwarp();
+                        if (lane < kTcCols / 32) {
+                            uint32_t m = 0;
+                            for (uint32_t q = 0; q < 32; q++) {
+                                const uint32_t j = lane * 32 + q;
+                                if (j < filled && (T.tinfo[j] & 0x80000000u)) m |= 1u << q;
+                            }
+                            T.lastmask[lane] = m;
+                        }
+                        if (lane == 0) {
+                            S.cur_t = ct;
+                            S.cur_f = cf;
+                            T.ntile = filled;
+                            T.ncomp = ncomp;
+                            T.produced = filled > 0;
+                        }
+                    }
+                    group_sync<2>();
+                    if (T.produced) {
+                        const uint32_t nt = T.ntile;
+                        const uint32_t ncols = (nt + 15) & ~15u;  // MMA N: multiple of 16
+                        const uint32_t idesc = (1u << 4) | ((ncols >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+                        const uint32_t dacc = tmem + b * kTcCols;
+                        auto fetch = [&](uint32_t c) {
+                            uint4* slot = S.bits[c % kTcBitSlots];
+                            for (uint32_t i = ptid; i < kTcRows + ncols; i += 128) {
+                                if (i < kTcRows) {
+                                    const uint32_t f = S.rowf[i];
+                                    if (f != 0xFFFFFFFFu) cp_async16(slot + i, P.filters[rs] + (size_t)f * 64 + c * 4);
+                                } else if (i - kTcRows < nt) {
+                                    cp_async16(slot + i, P.filters[ts] + (size_t)T.gidx[i - kTcRows] * 64 + c * 4);
                                 }
                             }
-                        }
-                        if (last) {
-                            const double m = max_value(active, bnum, bden, counted);
-                            if (split) {
-                                if (have) P.slots[P.split[U.split].slot_base + row] = m;
-                            } else {
-                                S.mv[tid][(S.tinfo[j] >> 16) & 0x7FFFu] = m;
+                            cp_async_commit();
+                        };
+                        fetch(0);
+                        if (nch > 1) fetch(1);
+                        for (uint32_t c = 0; c < nch; c++) {
+                            if (c + 2 < nch) fetch(c + 2);
+                            else cp_async_commit();
+                            cp_async_wait2();
+                            const uint32_t s = (suses[0] + suses[1]) & 1;
+                            bool w = true;
+                            if (suses[s] > 0) w = mbar_wait(smem_addr(&S.mbar[s]), (suses[s] - 1) & 1);
+                            ok = group_and<2>(ok && w);
+                            if (!ok) break;
+                            uint8_t* sa = stages + s * kTcStage;
+                            uint8_t* sb = sa + kTcAStage;
+                            const uint4* slot = S.bits[c % kTcBitSlots];
+                            for (uint32_t i = ptid; i < kTcRows + ncols; i += 128) {
+                                uint4 bits = make_uint4(0, 0, 0, 0);
+                                if (i < kTcRows) {
+                                    if (S.rowf[i] != 0xFFFFFFFFu) bits = slot[i];
+                                    widen_row(sa, i, bits);
+                                } else {
+                                    if (i - kTcRows < nt) bits = slot[i];
+                                    widen_row(sb, i - kTcRows, bits);
+                                }
                             }
-                            bnum = 0;
-                            bden = 1;
-                            counted = false;
-                        }
-                    };
-                    for (uint32_t c0 = 0; c0 < nt; c0 += 32) {
-                        uint32_t v[32];
-                        const uint32_t taddr = tmem + ((warp * 32) << 16) + c0;
-                        asm volatile(
-                            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-                            "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-                              "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
-                              "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
-                              "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
-                              "=r"(v[31])
-                            : "r"(taddr));
-                        asm volatile("tcgen05.wait::ld.sync.aligned;");
-                        const uint32_t lim = min(32u, nt - c0);
-                        const uint32_t lm = S.lastmask[c0 >> 5];
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            group_sync<2>();
+                            if (ptid == 0) {
+                                asm volatile("tcgen05.fence::after_thread_sync;");
+                                const uint32_t a0 = smem_addr(sa), b0 = smem_addr(sb);
 #pragma unroll
-                        for (uint32_t k = 0; k < 32; k++)
-                            if (k < lim) consume(c0 + k, (uint32_t)__uint_as_float(v[k]), (lm >> k) & 1u);
+                                for (uint32_t kk = 0; kk < kTcChunk / 32; kk++) {
+                                    const uint64_t ad = sw128_desc(a0 + kk * 32), bd = sw128_desc(b0 + kk * 32);
+                                    const uint32_t acc = (c > 0 || kk > 0) ? 1u : 0u;
+                                    asm volatile(
+                                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                                        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
+                                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+                                }
+                                mma_commit(smem_addr(&S.mbar[s]));
+                            }
+                            suses[s]++;
+                        }
+                        if (ok && ptid == 0) mma_commit(smem_addr(&S.mbar[2 + b]));
+                    }
+                } else if (pending) {
+                    // ---- consumers: score tile gtile-1 from accumulator 1-b
+                    const uint32_t pb = b ^ 1;
+                    const TcTile& T = S.tile[pb];
+                    const uint32_t g = gtile - 1;  // its tile number: the (g >> 1)-th use of accumulator pb
+                    bool w = mbar_wait(smem_addr(&S.mbar[2 + pb]), (g >> 1) & 1);
+                    ok = group_and<1>(ok && w);
+                    if (ok) {
+                        asm volatile("tcgen05.fence::after_thread_sync;");
+                        uint32_t cs2 = 0xFFFFFFFFu, ccut = 0;  // cut cached for the last s2 seen
+                        uint32_t ring_base = 0;                 // completion index of ring slot 0
+                        const uint32_t nt = T.ntile;
+                        for (uint32_t c0 = 0; c0 < nt; c0 += 32) {
+                            uint32_t v[32];
+                            const uint32_t taddr = tmem + ((warp * 32) << 16) + pb * kTcCols + c0;
+                            asm volatile(
+                                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+                                "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                                  "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+                                  "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+                                  "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+                                  "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+                                  "=r"(v[31])
+                                : "r"(taddr));
+                            asm volatile("tcgen05.wait::ld.sync.aligned;");
+                            const uint32_t lim = min(32u, nt - c0);
+                            const uint32_t lm = T.lastmask[c0 >> 5];
+#pragma unroll
+                            for (uint32_t q = 0; q < 32; q++) {
+                                if (q >= lim) break;
+                                const uint32_t j = c0 + q;
+                                const uint32_t cnt = (uint32_t)__uint_as_float(v[q]);
+                                const uint32_t tm = T.tmeta[j];
+                                const uint32_t s2 = tm & 0xFFFFu;
+                                if (active && s2 >= (uint32_t)kMinElem) {
+                                    if (s2 != cs2) {
+                                        cs2 = s2;
+                                        const uint32_t sum = s1 + s2;
+                                        ccut = !fastA ? cut_for(S.cut_sum, S.cut256, s1, s2)
+                                                      : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                                    }
+                                    counted = true;  // a counted target filter scores at least 0
+                                    if (cnt > ccut) {
+                                        const uint32_t match = candidate_match(
+                                            arow, P.filters[ts] + (size_t)T.gidx[j] * 64, cnt, ccut, fastA);
+                                        if (match > ccut) {
+                                            const uint32_t num = match - ccut, den = min(e1, tm >> 16) - ccut;
+                                            if ((uint64_t)num * bden > (uint64_t)bnum * den) {
+                                                bnum = num;
+                                                bden = den;
+                                            }
+                                        }
+                                    }
+                                }
+                                if ((lm >> q) & 1u) {
+                                    const double m = max_value(active, bnum, bden, counted);
+                                    if (split) {
+                                        if (have) P.slots[P.split[U.split].slot_base + row] = m;
+                                    } else {
+                                        S.mv[tid][((T.tinfo[j] >> 16) & 0xFFu) % kTcRing] = m;
+                                    }
+                                    bnum = 0;
+                                    bden = 1;
+                                    counted = false;
+                                }
+                            }
+                            // sum the maxima of the targets completed in these 32 columns
+                            const uint32_t done_now = __popc(lm & (lim == 32 ? 0xFFFFFFFFu : ((1u << lim) - 1)));
+                            if (done_now && !split) {
+                                group_sync<1>();
+                                if (group) {
+                                    for (uint32_t t = tid; t < done_now * nref; t += 128) {
+                                        const uint32_t kk = t % nref, ci = ring_base + t / nref;
+                                        double sum = -1.0;
+                                        for (uint32_t r = S.gstart[kk]; r < S.gstart[kk + 1]; r++) {
+                                            const double m = S.mv[r][ci % kTcRing];
+                                            if (sum < 0) sum = m;
+                                            else if (m != 0.0) sum = __dadd_rn(sum, m);
+                                        }
+                                        const uint32_t tgt = P.targets[U.t0 + T.comp[ci]];
+                                        P.scores[out_index(P, rs != 0, S.gref[kk], tgt)] =
+                                            final_score(sum, S.gstart[kk + 1] - S.gstart[kk], S.gsparse[kk]);
+                                    }
+                                } else {
+                                    for (uint32_t t = tid; t < done_now; t += 128) {
+                                        const uint32_t ci = ring_base + t;
+                                        double sum = S.run[T.comp[ci]];
+                                        for (uint32_t r = 0; r < nrows; r++) {
+                                            const double m = S.mv[r][ci % kTcRing];
+                                            if (sum < 0) sum = m;
+                                            else if (m != 0.0) sum = __dadd_rn(sum, m);
+                                        }
+                                        S.run[T.comp[ci]] = sum;
+                                    }
+                                }
+                                group_sync<1>();
+                            }
+                            ring_base += done_now;
+                        }
+                        asm volatile("tcgen05.fence::before_thread_sync;");
                     }
                 }
-                asm volatile("tcgen05.fence::before_thread_sync;");
-                __syncthreads();
-                // ---- fold the completed targets' maxima in filter order
-                if (group) {
-                    const uint32_t ncomp = S.ncomp;
-                    for (uint32_t t = tid; t < ncomp * nref; t += kTcThreads) {
-                        const uint32_t k = t % nref, col = t / nref;
-                        double sum = -1.0;
-                        for (uint32_t r = S.gstart[k]; r < S.gstart[k + 1]; r++) {
-                            const double m = S.mv[r][col];
-                            if (sum < 0) sum = m;
-                            else if (m != 0.0) sum = __dadd_rn(sum, m);
-                        }
-                        const uint32_t tgt = P.targets[U.t0 + S.comp[col]];
-                        P.scores[out_index(P, rs != 0, S.gref[k], tgt)] =
-                            final_score(sum, S.gstart[k + 1] - S.gstart[k], S.gsparse[k]);
-                    }
-                } else if (!split) {
-                    for (uint32_t k = tid; k < S.ncomp; k += kTcThreads) {
-                        double sum = S.run[S.comp[k]];
-                        for (uint32_t r = 0; r < nrows; r++) {
-                            const double m = S.mv[r][k];
-                            if (sum < 0) sum = m;
-                            else if (m != 0.0) sum = __dadd_rn(sum, m);
-                        }
-                        S.run[S.comp[k]] = sum;
-                    }
-                }
-                __syncthreads();
+                ok = __syncthreads_and(ok);
+                if (!ok) break;
+                const bool produced = S.tile[b].produced != 0;
+                if (produced) gtile++;
+                pending = produced;
+                if (!produced) break;  // no tile counted in this step: the pass is done
             }
         }
         if (!ok) break;
@@ -501,17 +558,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
         }
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
-    if (!ok) {
-        if (tid == 0) {
-            atomicAdd(P.error, 1u);
-            // wait (bounded) for any MMA still reading shared memory or writing TMEM
-            mma_commit(smem_addr(&S.mbar[2]));
-            mbar_wait(smem_addr(&S.mbar[2]), done_phase & 1);
-        }
+    if (!ok && tid == 0) {
+        atomicAdd(P.error, 1u);
+        // wait (bounded) for any MMA still reading shared memory or writing TMEM
+        mma_commit(smem_addr(&S.mbar[4]));
+        mbar_wait(smem_addr(&S.mbar[4]), 0);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kTcCols));
 }
 
 cudaError_t launch_matrix_tc(const MatParams& P, uint32_t grid, cudaStream_t st) {
