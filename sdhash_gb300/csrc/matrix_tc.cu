@@ -48,7 +48,7 @@ constexpr int kTcRing = 32;        // completed targets held before their maxima
 constexpr uint32_t kTcAStage = kTcRows * kTcChunk;   // 16 KB of e4m3
 constexpr uint32_t kTcBStage = kTcCols * kTcChunk;   // 32 KB
 constexpr uint32_t kTcStage = kTcAStage + kTcBStage;
-constexpr uint32_t kTcWaitSpins = 1u << 22;
+constexpr uint32_t kTcWaitSpins = 1u << 20;
 constexpr int kTcBitSlots = 3;     // chunks of filter bits in flight (cp.async ring)
 
 // one tile's composition (double-buffered: warps 4-7 compose and count tile
