@@ -358,9 +358,21 @@ struct MatSmem {
     uint16_t cut64_sum[1024];     // CUTOFFS64[1024 / (s1 + s2)] by s1 + s2
     uint16_t cut256[SDBF_CUTOFF_BINS];
     uint16_t cut64[SDBF_CUTOFF_BINS];
+    uint32_t seg_first[32], seg_start[33], seg_te[32];  // tile composition: one segment per target
     MatUnit unit;
-    uint32_t unit_id, ntile, ncomp, cur_t, cur_f, sparse;
+    uint32_t unit_id, ntile, ncomp, cur_t, cur_f, sparse, nseg, last_open;
 };
+
+// slot j of a composed tile: its segment k (seg_start[k] <= j < seg_start[k+1])
+__device__ __forceinline__ uint32_t find_segment(const uint32_t* seg_start, uint32_t nseg, uint32_t j) {
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (seg_start[mid] <= j) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 
 template <int R, int TJ>
 __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
@@ -488,19 +500,25 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
                     }
                     const uint32_t excl = incl - rem;
                     const bool done_here = rem > 0 && incl <= (uint32_t)TJ;
-                    for (uint32_t s = excl; s < min(incl, (uint32_t)TJ); s++) {
-                        const uint32_t f = first + (s - excl);
-                        S.gidx[s] = f;
-                        S.tmeta[s] = P.meta[ts][f];
-                        S.tinfo[s] = te | (lane << 16) | ((done_here && s + 1 == incl) ? 0x80000000u : 0u);
+                    // segment of this lane's target (slots are filled by all threads below)
+                    const bool has = rem > 0 && excl < (uint32_t)TJ;
+                    if (has) {
+                        S.seg_first[lane] = first;
+                        S.seg_start[lane] = excl;
+                        S.seg_te[lane] = te;
                     }
                     if (done_here) S.comp[lane] = te;
                     const uint32_t done_mask = __ballot_sync(0xffffffffu, done_here);
+                    const uint32_t has_mask = __ballot_sync(0xffffffffu, has);
                     const uint32_t over_mask = __ballot_sync(0xffffffffu, rem > 0 && incl > (uint32_t)TJ);
+                    const uint32_t open_mask = __ballot_sync(0xffffffffu, has && incl > (uint32_t)TJ);
                     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
                     if (lane == 0) {
                         S.ncomp = __popc(done_mask);
                         S.ntile = min(total, (uint32_t)TJ);
+                        S.nseg = __popc(has_mask);
+                        S.seg_start[__popc(has_mask)] = min(total, (uint32_t)TJ);
+                        S.last_open = open_mask != 0;  // the last segment continues in the next tile
                     }
                     // cursor update: first lane whose target does not fit
                     const uint32_t l = over_mask ? (uint32_t)(__ffs(over_mask) - 1) : 32u;
@@ -514,6 +532,19 @@ __global__ void __launch_bounds__(R, 512 / R) k_matrix(MatParams P) {
                             S.cur_t = min(S.cur_t + 32u, nT);
                             S.cur_f = 0;
                         }
+                    }
+                }
+                __syncthreads();
+                // ---- slots of the tile, filled in parallel
+                {
+                    const uint32_t nseg = S.nseg;
+                    for (uint32_t j = tid; j < S.ntile; j += R) {
+                        const uint32_t k = find_segment(S.seg_start, nseg, j);
+                        const uint32_t f = S.seg_first[k] + (j - S.seg_start[k]);
+                        const bool last = j + 1 == S.seg_start[k + 1] && !(k + 1 == nseg && S.last_open);
+                        S.gidx[j] = f;
+                        S.tmeta[j] = P.meta[ts][f];
+                        S.tinfo[j] = S.seg_te[k] | (k << 16) | (last ? 0x80000000u : 0u);
                     }
                 }
                 __syncthreads();

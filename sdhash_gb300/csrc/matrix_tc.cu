@@ -55,8 +55,9 @@ constexpr int kTcBitSlots = 3;     // chunks of filter bits in flight (cp.async 
 // k while warps 0-3 score tile k-1)
 struct TcTile {
     uint32_t gidx[kTcCols], tmeta[kTcCols], tinfo[kTcCols], comp[kTcCols];
+    uint32_t seg_first[kTcCols], seg_start[kTcCols + 1], seg_te[kTcCols];  // one segment per target
     uint32_t lastmask[kTcCols / 32];
-    uint32_t ntile, ncomp, produced, pad;
+    uint32_t ntile, ncomp, produced, nseg, last_open;
 };
 
 struct TcSmem {
@@ -157,6 +158,17 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait2() { asm volatile("cp.async.wait_group 2;" ::: "memory"); }
+
+// slot j of a composed tile: its segment k (seg_start[k] <= j < seg_start[k+1])
+__device__ __forceinline__ uint32_t find_segment(const uint32_t* seg_start, uint32_t nseg, uint32_t j) {
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (seg_start[mid] <= j) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 
 // a pair whose full count is above the cut: the reference's staged exits
 // (normal mode) or its 32-byte stage (fast mode), from the filters in memory
@@ -315,8 +327,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                 const uint32_t b = gtile & 1;  // tile gtile is counted into accumulator / tile slot b
                 if (producer) {
                     TcTile& T = S.tile[b];
-                    if (warp == 4) {  // compose tile k: up to 256 filters of up to 256 targets
-                        uint32_t filled = 0, ncomp = 0, ct = S.cur_t, cf = S.cur_f;
+                    if (warp == 4) {  // compose tile g: up to 256 filters of up to 256 targets
+                        uint32_t filled = 0, ncomp = 0, nseg = 0, ct = S.cur_t, cf = S.cur_f;
+                        bool open = false;
                         while (filled < (uint32_t)kTcCols && ct < nT) {
                             const uint32_t te = ct + lane;
                             const uint32_t f0 = lane == 0 ? cf : 0;
@@ -334,18 +347,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             }
                             const uint32_t excl = incl - rem, room = (uint32_t)kTcCols - filled;
                             const bool done_here = rem > 0 && incl <= room;
-                            for (uint32_t s = excl; s < min(incl, room); s++) {
-                                const uint32_t slot = filled + s, f = first + (s - excl);
-                                T.gidx[slot] = f;
-                                T.tmeta[slot] = P.meta[ts][f];
-                                T.tinfo[slot] = te | ((ncomp + lane) << 16) |
-                                                ((done_here && s + 1 == incl) ? 0x80000000u : 0u);
+                            const bool has = rem > 0 && excl < room;
+                            if (has) {  // every earlier segment of this tile completed, so index nseg + lane
+                                T.seg_first[nseg + lane] = first;
+                                T.seg_start[nseg + lane] = filled + excl;
+                                T.seg_te[nseg + lane] = te;
                             }
                             if (done_here) T.comp[ncomp + lane] = te;
                             const uint32_t done_mask = __ballot_sync(0xffffffffu, done_here);
+                            const uint32_t has_mask = __ballot_sync(0xffffffffu, has);
                             const uint32_t over_mask = __ballot_sync(0xffffffffu, rem > 0 && incl > room);
+                            const uint32_t open_mask = __ballot_sync(0xffffffffu, has && incl > room);
                             const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
                             ncomp += __popc(done_mask);
+                            nseg += __popc(has_mask);
                             if (over_mask) {
                                 const uint32_t l = __ffs(over_mask) - 1;
                                 const uint32_t ex_l = __shfl_sync(0xffffffffu, excl, l);
@@ -353,27 +368,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                 ct += l;
                                 cf = f0_l + (room - ex_l);
                                 filled = kTcCols;
+                                open = open_mask != 0;
                             } else {
                                 ct = min(ct + 32u, nT);
                                 cf = 0;
                                 filled += total;
                             }
                         }
-                        __syncwarp();
-                        if (lane < kTcCols / 32) {
-                            uint32_t m = 0;
-                            for (uint32_t q = 0; q < 32; q++) {
-                                const uint32_t j = lane * 32 + q;
-                                if (j < filled && (T.tinfo[j] & 0x80000000u)) m |= 1u << q;
-                            }
-                            T.lastmask[lane] = m;
-                        }
+                        if (lane < kTcCols / 32) T.lastmask[lane] = 0;
                         if (lane == 0) {
                             S.cur_t = ct;
                             S.cur_f = cf;
                             T.ntile = filled;
                             T.ncomp = ncomp;
+                            T.nseg = nseg;
+                            T.seg_start[nseg] = filled;
+                            T.last_open = open;
                             T.produced = filled > 0;
+                        }
+                    }
+                    group_sync<2>();
+                    // slots of the tile, filled by all producers (loads in parallel)
+                    {
+                        const uint32_t nseg = T.nseg;
+                        for (uint32_t j = ptid; j < T.ntile; j += 128) {
+                            const uint32_t k = find_segment(T.seg_start, nseg, j);
+                            const uint32_t f = T.seg_first[k] + (j - T.seg_start[k]);
+                            const bool last = j + 1 == T.seg_start[k + 1] && !(k + 1 == nseg && T.last_open);
+                            T.gidx[j] = f;
+                            T.tmeta[j] = P.meta[ts][f];
+                            T.tinfo[j] = T.seg_te[k] | (k << 16) | (last ? 0x80000000u : 0u);
+                            if (last) atomicOr(&T.lastmask[j >> 5], 1u << (j & 31));
                         }
                     }
                     group_sync<2>();
