@@ -76,13 +76,30 @@ def test_served_results_equal_solo_results(ctx, serve_data):
             assert r.matches == int((solo[q] >= 1).sum())
             assert r.submit_ns <= r.start_ns <= r.done_ns
             sizes.add(int(r.batch_queries))
-        assert max(sizes) > 1       # queries were batched together
         st = srv.stats()
         assert st["served"] == len(order) and st["pending"] == 0 and st["batches"] >= 2
         # one query alone on an idle server
         srv.submit(queries[5], 10_000)
         (r, row), = _drain(srv, 1).values()
         assert r.batch_queries == 1 and np.array_equal(row, solo[5])
+    finally:
+        srv.close()
+
+
+def test_burst_is_batched_and_exact(ctx, serve_data):
+    """One slot and a burst of requests: queries arriving while a batch runs
+    are admitted together into the next one; every row is still exact."""
+    g, targets, queries, tset, solo = serve_data
+    srv = g.Server(ctx, tset, slots=1, max_batch_queries=16, memory_budget=4 << 20, threshold=1)
+    try:
+        order = list(range(len(queries))) * 4
+        for k, q in enumerate(order):
+            srv.submit(queries[q], k)
+        got = _drain(srv, len(order))
+        assert len(got) == len(order)
+        for k, (r, row) in got.items():
+            assert np.array_equal(row, solo[order[k]]), k
+        assert max(int(r.batch_queries) for r, _ in got.values()) > 1
     finally:
         srv.close()
 
