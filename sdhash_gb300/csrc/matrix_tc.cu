@@ -44,7 +44,7 @@ constexpr int kTcCols = 256;       // target filters per tile = MMA N (max)
 constexpr int kTcThreads = 256;    // warps 0-3 score (one row each), warps 4-7 widen and issue
 constexpr int kTcChunk = 128;      // K elements (bits) per stage
 constexpr int kTcChunks = 2048 / kTcChunk;
-constexpr int kTcRing = 32;        // completed targets held before their maxima are summed
+constexpr int kTcRing = 16;        // completed targets held before their maxima are summed
 constexpr uint32_t kTcAStage = kTcRows * kTcChunk;   // 16 KB of e4m3
 constexpr uint32_t kTcBStage = kTcCols * kTcChunk;   // 32 KB
 constexpr uint32_t kTcStage = kTcAStage + kTcBStage;
@@ -54,6 +54,7 @@ constexpr int kTcBitSlots = 3;     // chunks of filter bits in flight (cp.async 
 // one tile's composition (double-buffered: warps 4-7 compose and count tile
 // k while warps 0-3 score tile k-1)
 struct TcTile {
+    uint4 tw[kTcCols][8];  // first 128 bytes of each target filter (staged re-check of candidates)
     uint32_t gidx[kTcCols], tmeta[kTcCols], tinfo[kTcCols], comp[kTcCols];
     uint32_t seg_first[kTcCols], seg_start[kTcCols + 1], seg_te[kTcCols];  // one segment per target
     uint32_t lastmask[kTcCols / 32];
@@ -74,6 +75,7 @@ struct TcSmem {
 };
 
 constexpr size_t kTcSmemBytes = 1024 /* alignment */ + 2 * kTcStage + sizeof(TcSmem);
+static_assert(kTcSmemBytes <= 227 * 1024, "tensor-core kernel exceeds the shared memory of one CTA");
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -126,33 +128,6 @@ __device__ __forceinline__ void widen_row(uint8_t* stage, uint32_t r, uint4 bits
     }
 }
 
-// the reference's staged exits for a pair above the cut, from memory
-__device__ __forceinline__ bool staged_exit_mem(const uint32_t* a, const uint32_t* t, uint32_t cut) {
-    const uint4* a4 = reinterpret_cast<const uint4*>(a);
-    const uint4* t4 = reinterpret_cast<const uint4*>(t);
-    uint32_t c = 0;
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const uint4 x = __ldg(a4 + q), y = __ldg(t4 + q);
-        c += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
-        if (q == 1 && 8 * c + 48 < cut) return true;
-        if (q == 3 && 4 * c + 48 < cut) return true;
-    }
-    return 2 * c + 48 < cut;
-}
-
-__device__ __forceinline__ uint32_t popc8_mem(const uint32_t* a, const uint32_t* t) {
-    const uint4* a4 = reinterpret_cast<const uint4*>(a);
-    const uint4* t4 = reinterpret_cast<const uint4*>(t);
-    uint32_t c = 0;
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-        const uint4 x = __ldg(a4 + q), y = __ldg(t4 + q);
-        c += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
-    }
-    return c;
-}
-
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
@@ -171,11 +146,22 @@ __device__ __forceinline__ uint32_t find_segment(const uint32_t* seg_start, uint
 }
 
 // a pair whose full count is above the cut: the reference's staged exits
-// (normal mode) or its 32-byte stage (fast mode), from the filters in memory
-__device__ __noinline__ uint32_t candidate_match(const uint32_t* arow, const uint32_t* trow, uint32_t cnt,
-                                                 uint32_t cut, bool fast) {
-    if (!fast) return staged_exit_mem(arow, trow, cut) ? 0u : cnt;
-    return 2 * popc8_mem(arow, trow) + 48 < cut ? 0u : cnt;
+// (normal mode: after 8, 16, 32 words) or its 32-byte stage (fast mode),
+// from the row's first 128 bytes (registers) and the target's (shared memory)
+__device__ __forceinline__ uint32_t candidate_match(const uint4 (&aw)[8], const uint4* tw, uint32_t cnt,
+                                                   uint32_t cut, bool fast) {
+    uint32_t c = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const uint4 y = tw[q];
+        c += __popc(aw[q].x & y.x) + __popc(aw[q].y & y.y) + __popc(aw[q].z & y.z) + __popc(aw[q].w & y.w);
+        if (q == 1) {
+            if (fast) return 2 * c + 48 < cut ? 0u : cnt;
+            if (8 * c + 48 < cut) return 0;
+        }
+        if (q == 3 && 4 * c + 48 < cut) return 0;
+    }
+    return 2 * c + 48 < cut ? 0u : cnt;
 }
 
 }  // namespace
@@ -316,7 +302,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
             uint32_t bnum = 0, bden = 1;
             bool counted = false;
             const uint32_t nrows = min((uint32_t)kTcRows, U.r1 - rc);
-            const uint32_t* arow = P.filters[rs] + (size_t)fidx * 64;
+            uint4 aw[8];  // the row's first 128 bytes, for the staged re-check of candidates
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                aw[q] = have ? __ldg(reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)fidx * 64) + q)
+                             : make_uint4(0, 0, 0, 0);
             __syncthreads();
             // ---- software pipeline: each step counts tile g (producers) and
             // scores tile g-1 (consumers); one CTA barrier per step.  Tile g
@@ -439,7 +429,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                     if (S.rowf[i] != 0xFFFFFFFFu) bits = slot[i];
                                     widen_row(sa, i, bits);
                                 } else {
-                                    if (i - kTcRows < nt) bits = slot[i];
+                                    if (i - kTcRows < nt) {
+                                        bits = slot[i];
+                                        if (c < 8) T.tw[i - kTcRows][c] = bits;
+                                    }
                                     widen_row(sb, i - kTcRows, bits);
                                 }
                             }
@@ -490,78 +483,80 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                 : "r"(taddr));
                             asm volatile("tcgen05.wait::ld.sync.aligned;");
                             const uint32_t lim = min(32u, nt - c0);
-                            const uint32_t lm = T.lastmask[c0 >> 5];
+                            const uint32_t lm = T.lastmask[c0 >> 5] & (lim == 32 ? 0xFFFFFFFFu : ((1u << lim) - 1));
 #pragma unroll
-                            for (uint32_t q = 0; q < 32; q++) {
-                                if (q >= lim) break;
-                                const uint32_t j = c0 + q;
-                                const uint32_t cnt = (uint32_t)__uint_as_float(v[q]);
-                                const uint32_t tm = T.tmeta[j];
-                                const uint32_t s2 = tm & 0xFFFFu;
-                                if (active && s2 >= (uint32_t)kMinElem) {
-                                    if (s2 != cs2) {
-                                        cs2 = s2;
-                                        const uint32_t sum = s1 + s2;
-                                        ccut = !fastA ? cut_for(S.cut_sum, S.cut256, s1, s2)
-                                                      : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
-                                    }
-                                    counted = true;  // a counted target filter scores at least 0
-                                    if (cnt > ccut) {
-                                        const uint32_t match = candidate_match(
-                                            arow, P.filters[ts] + (size_t)T.gidx[j] * 64, cnt, ccut, fastA);
-                                        if (match > ccut) {
-                                            const uint32_t num = match - ccut, den = min(e1, tm >> 16) - ccut;
-                                            if ((uint64_t)num * bden > (uint64_t)bnum * den) {
-                                                bnum = num;
-                                                bden = den;
+                            for (uint32_t h = 0; h < 2; h++) {
+#pragma unroll
+                                for (uint32_t q = 16 * h; q < 16 * h + 16; q++) {
+                                    if (q >= lim) break;
+                                    const uint32_t j = c0 + q;
+                                    const uint32_t cnt = (uint32_t)__uint_as_float(v[q]);
+                                    const uint32_t tm = T.tmeta[j];
+                                    const uint32_t s2 = tm & 0xFFFFu;
+                                    if (active && s2 >= (uint32_t)kMinElem) {
+                                        if (s2 != cs2) {
+                                            cs2 = s2;
+                                            const uint32_t sum = s1 + s2;
+                                            ccut = !fastA ? cut_for(S.cut_sum, S.cut256, s1, s2)
+                                                          : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                                        }
+                                        counted = true;  // a counted target filter scores at least 0
+                                        if (cnt > ccut) {
+                                            const uint32_t match = candidate_match(aw, T.tw[j], cnt, ccut, fastA);
+                                            if (match > ccut) {
+                                                const uint32_t num = match - ccut, den = min(e1, tm >> 16) - ccut;
+                                                if ((uint64_t)num * bden > (uint64_t)bnum * den) {
+                                                    bnum = num;
+                                                    bden = den;
+                                                }
                                             }
                                         }
                                     }
+                                    if ((lm >> q) & 1u) {
+                                        const double m = max_value(active, bnum, bden, counted);
+                                        if (split) {
+                                            if (have) P.slots[P.split[U.split].slot_base + row] = m;
+                                        } else {
+                                            S.mv[tid][((T.tinfo[j] >> 16) & 0xFFu) % kTcRing] = m;
+                                        }
+                                        bnum = 0;
+                                        bden = 1;
+                                        counted = false;
+                                    }
                                 }
-                                if ((lm >> q) & 1u) {
-                                    const double m = max_value(active, bnum, bden, counted);
-                                    if (split) {
-                                        if (have) P.slots[P.split[U.split].slot_base + row] = m;
+                                // sum the maxima of the targets completed in these 16 columns
+                                const uint32_t done_now = __popc(lm & (0xFFFFu << (16 * h)));
+                                if (done_now && !split) {
+                                    group_sync<1>();
+                                    if (group) {
+                                        for (uint32_t t = tid; t < done_now * nref; t += 128) {
+                                            const uint32_t kk = t % nref, ci = ring_base + t / nref;
+                                            double sum = -1.0;
+                                            for (uint32_t r = S.gstart[kk]; r < S.gstart[kk + 1]; r++) {
+                                                const double m = S.mv[r][ci % kTcRing];
+                                                if (sum < 0) sum = m;
+                                                else if (m != 0.0) sum = __dadd_rn(sum, m);
+                                            }
+                                            const uint32_t tgt = P.targets[U.t0 + T.comp[ci]];
+                                            P.scores[out_index(P, rs != 0, S.gref[kk], tgt)] =
+                                                final_score(sum, S.gstart[kk + 1] - S.gstart[kk], S.gsparse[kk]);
+                                        }
                                     } else {
-                                        S.mv[tid][((T.tinfo[j] >> 16) & 0xFFu) % kTcRing] = m;
-                                    }
-                                    bnum = 0;
-                                    bden = 1;
-                                    counted = false;
-                                }
-                            }
-                            // sum the maxima of the targets completed in these 32 columns
-                            const uint32_t done_now = __popc(lm & (lim == 32 ? 0xFFFFFFFFu : ((1u << lim) - 1)));
-                            if (done_now && !split) {
-                                group_sync<1>();
-                                if (group) {
-                                    for (uint32_t t = tid; t < done_now * nref; t += 128) {
-                                        const uint32_t kk = t % nref, ci = ring_base + t / nref;
-                                        double sum = -1.0;
-                                        for (uint32_t r = S.gstart[kk]; r < S.gstart[kk + 1]; r++) {
-                                            const double m = S.mv[r][ci % kTcRing];
-                                            if (sum < 0) sum = m;
-                                            else if (m != 0.0) sum = __dadd_rn(sum, m);
+                                        for (uint32_t t = tid; t < done_now; t += 128) {
+                                            const uint32_t ci = ring_base + t;
+                                            double sum = S.run[T.comp[ci]];
+                                            for (uint32_t r = 0; r < nrows; r++) {
+                                                const double m = S.mv[r][ci % kTcRing];
+                                                if (sum < 0) sum = m;
+                                                else if (m != 0.0) sum = __dadd_rn(sum, m);
+                                            }
+                                            S.run[T.comp[ci]] = sum;
                                         }
-                                        const uint32_t tgt = P.targets[U.t0 + T.comp[ci]];
-                                        P.scores[out_index(P, rs != 0, S.gref[kk], tgt)] =
-                                            final_score(sum, S.gstart[kk + 1] - S.gstart[kk], S.gsparse[kk]);
                                     }
-                                } else {
-                                    for (uint32_t t = tid; t < done_now; t += 128) {
-                                        const uint32_t ci = ring_base + t;
-                                        double sum = S.run[T.comp[ci]];
-                                        for (uint32_t r = 0; r < nrows; r++) {
-                                            const double m = S.mv[r][ci % kTcRing];
-                                            if (sum < 0) sum = m;
-                                            else if (m != 0.0) sum = __dadd_rn(sum, m);
-                                        }
-                                        S.run[T.comp[ci]] = sum;
-                                    }
+                                    group_sync<1>();
                                 }
-                                group_sync<1>();
+                                ring_base += done_now;
                             }
-                            ring_base += done_now;
                         }
                         asm volatile("tcgen05.fence::before_thread_sync;");
                     }
