@@ -1,0 +1,214 @@
+"""Command-line front end with the reference's sdhash options
+(sdhash-src/sdhash.cc:100-640), over the GPU engine.
+
+    python -m sdhash_gb300.cli [options] files...
+
+Hashing: files below 16 MiB are digested in stream mode, larger ones in
+block mode with 16 KiB blocks and 128 MiB segments (sdhash.cc:487-605;
+`-b 0` keeps stream mode, `-b N` puts every file in N KiB block mode);
+digests are printed in the reference's order for `-p 1`: the small files,
+then the large ones, each in argument order.  `-g` compares all hashed
+pairs, `-c` compares the digests of one SDBF file (all pairs) or of two
+(every digest of the first against every digest of the second).  Result
+lines, separators, thresholds and `--fast` are the reference's.  Not
+offered: `-s` (filter sampling seeds rand() from time() in the reference),
+`--large`, `--index`, `--index-search`, `--details`.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+MB = 1 << 20
+KB = 1 << 10
+VERSION = "sdhash_gb300 (sdhash 4.0 digest format, SDBF v3)"
+
+
+def _segments(path: str, size: int, seg: int):
+    """sdbf_hash_files_dd's segmentation (sdhash-src/sdhash_threads.cc:300-373):
+    (name, offset, length) of each segment digest of a file."""
+    if not (size > seg and seg > 0):
+        return [(path, 0, size)]
+    chunks = size // seg
+    tail = False
+    if size - seg <= 512:
+        chunks = 0
+    if size - chunks * seg <= 512:
+        chunks -= 1
+        tail = True
+    out = []
+    for j in range(chunks + 1):
+        name = path if not (j > 0 or chunks > 0) else f"{path}.{j * seg // MB:04d}M"
+        if j == chunks:
+            csize = size - chunks * seg
+            if tail:
+                csize = csize + (size - (chunks + 1) * seg)
+        else:
+            csize = seg
+        out.append((name, j * seg, csize))
+    return out
+
+
+def _collect(inputs, deep: bool):
+    files = []
+    for p in inputs:
+        if deep and os.path.isdir(p):
+            for root, _dirs, names in os.walk(p):
+                for n in sorted(names):
+                    q = os.path.join(root, n)
+                    if os.path.isfile(q):
+                        files.append(q)
+        if os.path.isfile(p):
+            files.append(p)
+    return files
+
+
+def _hash(ctx, files, block_kb: int, seg: int, name_for_stdin=None, stdin_data=None):
+    import numpy as np
+    import sdhash_gb300 as g
+    digs = []
+    def seg_digests(data, name, dd):
+        # a segment digests csize bytes read from the stream, zero-filled past
+        # its end, and records the bytes actually read (sdbf_class.cc:71-88)
+        segs = _segments(name, len(data), seg)
+        bufs, got = [], []
+        for _, o, n in segs:
+            b = np.zeros(n, dtype=np.uint8)
+            part = np.frombuffer(bytes(data[o:o + n]), dtype=np.uint8) if not isinstance(data, np.ndarray) \
+                else data[o:o + n]
+            b[:len(part)] = part
+            bufs.append(b)
+            got.append(len(part))
+        out = ctx.digest_buffers(bufs, [nm for nm, _, _ in segs], dd)
+        res = []
+        for d, n in zip(out, got):
+            if d is not None and n >= 512:
+                d.orig_size = n
+                res.append(d)
+        return res
+
+    if stdin_data is not None:
+        dd = (block_kb if block_kb > 0 else 16) * KB
+        return [g.sdbf(_digest=d) for d in seg_digests(stdin_data, name_for_stdin or "stdin", dd)]
+    small = [f for f in files if os.path.getsize(f) < 16 * MB]
+    large = [f for f in files if os.path.getsize(f) >= 16 * MB]
+    for group, is_large in ((small, False), (large, True)):
+        if not group:
+            continue
+        if block_kb == 0 or (block_kb < 0 and not is_large):
+            # stream mode, the whole file
+            bufs = [open(f, "rb").read() for f in group]
+            for d in ctx.digest_buffers(bufs, group, 0):
+                if d is not None:
+                    digs.append(d)
+        else:
+            dd = (16 if block_kb < 0 else block_kb) * KB
+            for f in group:
+                digs += seg_digests(np.fromfile(f, dtype=np.uint8), f, dd)
+    return [g.sdbf(_digest=d) for d in digs]
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(prog="sdhash", add_help=True)
+    ap.add_argument("-r", "--deep", action="store_true", help="generate SDBFs from directories and files")
+    ap.add_argument("-f", "--target-list", action="store_true", help="generate SDBFs from list(s) of filenames")
+    ap.add_argument("-c", "--compare", action="store_true", help="compare SDBFs in file, or two SDBF files")
+    ap.add_argument("-g", "--gen-compare", action="store_true", help="compare all pairs in source data")
+    ap.add_argument("-t", "--threshold", type=int, default=1, help="only show results >=threshold")
+    ap.add_argument("-b", "--block-size", type=int, default=-1, help="hashes input files in nKB blocks")
+    ap.add_argument("-p", "--threads", type=int, default=0, help="accepted; the GPU does not use it")
+    ap.add_argument("-s", "--sample-size", type=int, default=0, help="not offered (must be 0)")
+    ap.add_argument("-z", "--segment-size", type=int, default=128, help="file segment size in MB")
+    ap.add_argument("-o", "--output", default=None, help="send output to files")
+    ap.add_argument("--separator", default="pipe", choices=["pipe", "csv", "tab", "tabs"])
+    ap.add_argument("--hash-name", default=None, help="set name of hash on stdin")
+    ap.add_argument("--fast", action="store_true", help="shrink sdbf filters for speedup")
+    ap.add_argument("--validate", action="store_true", help="parse SDBF file to check if it is valid")
+    ap.add_argument("--version", action="store_true")
+    ap.add_argument("files", nargs="*")
+    a = ap.parse_args(argv)
+    if a.version:
+        print(VERSION)
+        return 0
+    if a.sample_size:
+        print("sdhash: filter sampling (-s) is not offered by this engine", file=sys.stderr)
+        return -1
+    import sdhash_gb300 as g
+    sep = {"pipe": "|", "csv": ",", "tab": "\t", "tabs": "\t"}[a.separator]
+    block_kb = a.block_size
+    if block_kb > 16:
+        block_kb = 16          # sdhash.cc:215-219
+    if block_kb < -1:
+        block_kb = -1
+    out = sys.stdout
+
+    def emit(text: str, suffix: str):
+        if a.output:
+            with open(a.output + suffix, "w") as f:
+                f.write(text)
+        else:
+            out.write(text)
+
+    if a.compare:
+        if len(a.files) not in (1, 2):
+            print("sdhash: ERROR: Comparison requires 1 or 2 arguments.", file=sys.stderr)
+            return -1
+        sets = []
+        for p in a.files:
+            try:
+                s = g.sdbf_set(p)
+            except Exception:
+                print(f"sdhash: ERROR: Could not load SDBF file {p}. Exiting", file=sys.stderr)
+                return -1
+            s.set_separator(sep)
+            sets.append(s)
+        if len(sets) == 1:
+            emit(sets[0].compare_all_quiet(a.threshold, 0, a.fast), ".compare")
+        else:
+            emit(sets[0].compare_to_quiet(sets[1], a.threshold, 0, 0, a.fast), ".compare")
+        return 0
+    if a.validate:
+        for p in a.files:
+            if not os.path.isfile(p):
+                print(f"sdhash: ERROR file {p} not readable or not found.")
+                continue
+            try:
+                s = g.sdbf_set(p)
+            except Exception:
+                print(f"sdhash: ERROR: Could not load file of SDBFs, {p} is empty or invalid.", file=sys.stderr)
+                continue
+            print(f"sdhash: file {p} SDBFs valid, contains {s.size()} hashes.")
+            print(f"contains {sum(x.filter_count() for x in s.items)} bloom filters.")
+            print(f"{s.input_size()} total data size. ")
+        return 0
+    ctx = g.default_context()
+    seg = a.segment_size * MB
+    if a.files == ["-"]:
+        data = sys.stdin.buffer.read()
+        items = _hash(ctx, [], block_kb, seg, a.hash_name, data)
+    else:
+        inputs = a.files
+        if a.target_list:
+            inputs = []
+            for lst in a.files:
+                with open(lst) as f:
+                    inputs += [ln.rstrip("\n") for ln in f if ln.strip()]
+        files = _collect(inputs, a.deep)
+        if not files:
+            print(VERSION + "\n\nUsage: sdhash <options> <files>")
+            return 0
+        items = _hash(ctx, files, block_kb, seg)
+    s = g.sdbf_set()
+    s.set_separator(sep)
+    for it in items:
+        s.add(it)
+    if a.gen_compare:
+        emit(s.compare_all_quiet(a.threshold, 0, a.fast), ".compare")
+    else:
+        emit(s.to_string(), ".sdbf")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -88,3 +88,36 @@ def test_parse_rejects_malformed(native):
     assert g.Digest.from_string(good).bf_count == 1
     with pytest.raises(g.SdbfError):
         g.Digest.from_string(good.replace("A" * 342, "A" * 300 + "!" * 42))
+
+
+def test_cli_segments_follow_reference_rule():
+    """sdbf_hash_files_dd's segment sizes (sdhash-src/sdhash_threads.cc:312-340)."""
+    from sdhash_gb300.cli import _segments
+    M = 1 << 20
+
+    def ref(size, chunk):
+        if not (size > chunk and chunk > 0):
+            return [size]
+        chunks, tail = size // chunk, False
+        if size - chunk <= 512:
+            chunks = 0
+        if size - chunks * chunk <= 512:
+            chunks -= 1
+            tail = True
+        out = []
+        for j in range(chunks + 1):
+            if j == chunks:
+                c = size - chunks * chunk
+                if tail:
+                    c += size - (chunks + 1) * chunk
+            else:
+                c = chunk
+            out.append(c)
+        return out
+
+    for size in (100, 128 * M, 128 * M + 100, 128 * M + 512, 128 * M + 513, 256 * M + 512, 256 * M + 513, 300 * M):
+        got = _segments("f", size, 128 * M)
+        assert [n for _, _, n in got] == ref(size, 128 * M), size
+        assert [o for _, o, _ in got] == [j * 128 * M for j in range(len(got))]
+    names = [nm for nm, _, _ in _segments("img", 300 * M, 128 * M)]
+    assert names == ["img.0000M", "img.0128M", "img.0256M"]
