@@ -331,6 +331,7 @@ static MatParams plan_params(sdbfg_ctx* c, const MatPlan* p, const sdbfg_set* a,
     P.cutoffs = c->d_cut.as<uint16_t>();
     P.cutoffs64 = c->d_cut64.as<uint16_t>();
     P.error = p->d_counter.as<uint32_t>() + 1;
+    P.phase = c->profile ? c->d_mphase.as<unsigned long long>() : nullptr;
     return P;
 }
 

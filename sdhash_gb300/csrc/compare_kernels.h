@@ -103,6 +103,12 @@ struct MatParams {
     const uint16_t* cutoffs;   // CUTOFFS256
     const uint16_t* cutoffs64; // CUTOFFS64 (fast mode)
     uint32_t* error;           // tensor-core kernel: set when a bounded wait gave up
+    unsigned long long* phase; // tensor-core kernel: optional SM-cycle counters (kTcPh*), null = off
+};
+// phase counters of the tensor-core kernel (one producer and one consumer thread per CTA)
+enum : int {
+    kTcPhCompose = 0, kTcPhFill, kTcPhFetchWait, kTcPhStageWait, kTcPhWiden, kTcPhIssue, kTcPhProdStep,
+    kTcPhAccWait, kTcPhScore, kTcPhFold, kTcPhConsStep, kTcPhStepBarrier, kTcPhTiles, kTcPhCount
 };
 
 // Kernel variants (rows per CTA x target filters per tile), chosen by the

@@ -120,7 +120,7 @@ struct sdbfg_ctx {
     uint64_t mat_unit_work = 1ull << 22;
     bool mat_graphs = true;
     std::vector<struct MatPlan*> plans;
-    DevBuf d_match_counts, d_match_offs, d_matches;
+    DevBuf d_match_counts, d_match_offs, d_matches, d_mphase;
 };
 
 struct sdbfg_set {

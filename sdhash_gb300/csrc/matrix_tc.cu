@@ -183,6 +183,10 @@ __device__ __forceinline__ void group_sync() {
     asm volatile("bar.sync %0, 128;" ::"n"(ID) : "memory");
 }
 
+#define TC_STAMP(var) const long long var = P.phase ? clock64() : 0
+#define TC_ADD(ph, t0) \
+    do { if (P.phase) atomicAdd(P.phase + (ph), (unsigned long long)(clock64() - (t0))); } while (0)
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
     extern __shared__ uint8_t tc_smem_raw[];
     const uint32_t raw = smem_addr(tc_smem_raw);
@@ -315,8 +319,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
             bool pending = false;  // a counted tile waits to be scored
             for (;;) {
                 const uint32_t b = gtile & 1;  // tile gtile is counted into accumulator / tile slot b
+                TC_STAMP(t_step);
                 if (producer) {
                     TcTile& T = S.tile[b];
+                    TC_STAMP(t_comp);
                     if (warp == 4) {  // compose tile g: up to 256 filters of up to 256 targets
                         uint32_t filled = 0, ncomp = 0, nseg = 0, ct = S.cur_t, cf = S.cur_f;
                         bool open = false;
@@ -378,6 +384,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                         }
                     }
                     group_sync<2>();
+                    if (ptid == 0) TC_ADD(kTcPhCompose, t_comp);
+                    TC_STAMP(t_fill);
                     // slots of the tile, filled by all producers (loads in parallel)
                     {
                         const uint32_t nseg = T.nseg;
@@ -392,7 +400,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                         }
                     }
                     group_sync<2>();
+                    if (ptid == 0) TC_ADD(kTcPhFill, t_fill);
                     if (T.produced) {
+                        if (ptid == 0 && P.phase) atomicAdd(P.phase + kTcPhTiles, 1ull);
                         const uint32_t nt = T.ntile;
                         const uint32_t ncols = (nt + 15) & ~15u;  // MMA N: multiple of 16
                         const uint32_t idesc = (1u << 4) | ((ncols >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
@@ -412,14 +422,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                         fetch(0);
                         if (nch > 1) fetch(1);
                         for (uint32_t c = 0; c < nch; c++) {
+                            TC_STAMP(t_fw);
                             if (c + 2 < nch) fetch(c + 2);
                             else cp_async_commit();
                             cp_async_wait2();
+                            if (ptid == 0) TC_ADD(kTcPhFetchWait, t_fw);
+                            TC_STAMP(t_sw);
                             const uint32_t s = (suses[0] + suses[1]) & 1;
                             bool w = true;
                             if (suses[s] > 0) w = mbar_wait(smem_addr(&S.mbar[s]), (suses[s] - 1) & 1);
                             ok = group_and<2>(ok && w);
+                            if (ptid == 0) TC_ADD(kTcPhStageWait, t_sw);
                             if (!ok) break;
+                            TC_STAMP(t_wd);
                             uint8_t* sa = stages + s * kTcStage;
                             uint8_t* sb = sa + kTcAStage;
                             const uint4* slot = S.bits[c % kTcBitSlots];
@@ -438,6 +453,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             }
                             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                             group_sync<2>();
+                            if (ptid == 0) TC_ADD(kTcPhWiden, t_wd);
+                            TC_STAMP(t_is);
                             if (ptid == 0) {
                                 asm volatile("tcgen05.fence::after_thread_sync;");
                                 const uint32_t a0 = smem_addr(sa), b0 = smem_addr(sb);
@@ -451,18 +468,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                         "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
                                 }
                                 mma_commit(smem_addr(&S.mbar[s]));
+                                TC_ADD(kTcPhIssue, t_is);
                             }
                             suses[s]++;
                         }
                         if (ok && ptid == 0) mma_commit(smem_addr(&S.mbar[2 + b]));
                     }
+                    if (ptid == 0) TC_ADD(kTcPhProdStep, t_step);
                 } else if (pending) {
                     // ---- consumers: score tile gtile-1 from accumulator 1-b
                     const uint32_t pb = b ^ 1;
                     const TcTile& T = S.tile[pb];
                     const uint32_t g = gtile - 1;  // its tile number: the (g >> 1)-th use of accumulator pb
+                    TC_STAMP(t_aw);
                     bool w = mbar_wait(smem_addr(&S.mbar[2 + pb]), (g >> 1) & 1);
                     ok = group_and<1>(ok && w);
+                    if (tid == 0) TC_ADD(kTcPhAccWait, t_aw);
+                    TC_STAMP(t_sc);
                     if (ok) {
                         asm volatile("tcgen05.fence::after_thread_sync;");
                         uint32_t cs2 = 0xFFFFFFFFu, ccut = 0;  // cut cached for the last s2 seen
@@ -560,8 +582,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                         }
                         asm volatile("tcgen05.fence::before_thread_sync;");
                     }
+                    if (tid == 0) TC_ADD(kTcPhScore, t_sc);
+                    if (tid == 0) TC_ADD(kTcPhConsStep, t_step);
                 }
+                TC_STAMP(t_bar);
                 ok = __syncthreads_and(ok);
+                if (tid == 0) TC_ADD(kTcPhStepBarrier, t_bar);
                 if (!ok) break;
                 const bool produced = S.tile[b].produced != 0;
                 if (produced) gtile++;

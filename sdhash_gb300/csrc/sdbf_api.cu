@@ -61,7 +61,7 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
                       &c->d_order, &c->d_tile_out, &c->d_features, &c->d_work_filters, &c->d_info,
                       &c->d_counters, &c->d_pack_src, &c->d_pack_dst_off, &c->d_out_filters, &c->d_out_counts,
                       &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase,
-                      &c->d_match_counts, &c->d_match_offs, &c->d_matches})
+                      &c->d_match_counts, &c->d_match_offs, &c->d_matches, &c->d_mphase})
         b->release();
     for (auto& S : c->slot) {
         for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work,
@@ -104,6 +104,8 @@ extern "C" int sdbfg_ctx_profile(sdbfg_ctx* c, int enable) {
         c->stats.clear();
         CUDA_TRY(c, c->d_phase.ensure(kPhCount * sizeof(unsigned long long)));
         CUDA_TRY(c, cudaMemset(c->d_phase.p, 0, kPhCount * sizeof(unsigned long long)));
+        CUDA_TRY(c, c->d_mphase.ensure(kTcPhCount * sizeof(unsigned long long)));
+        CUDA_TRY(c, cudaMemset(c->d_mphase.p, 0, kTcPhCount * sizeof(unsigned long long)));
     }
     return SDBFG_OK;
 }
@@ -125,6 +127,19 @@ extern "C" int sdbfg_ctx_kernel_time(sdbfg_ctx* c, const char* name, double* tot
             CUDA_TRY(c, cudaMemcpy(v, c->d_phase.p, sizeof v, cudaMemcpyDeviceToHost));
             if (total_ms) *total_ms = (double)v[k];
             if (launches) *launches = v[kPhTiles];
+            return SDBFG_OK;
+        }
+    static const char* kTcNames[kTcPhCount] = {
+        "k_matrix_tc.compose", "k_matrix_tc.fill", "k_matrix_tc.fetch_wait", "k_matrix_tc.stage_wait",
+        "k_matrix_tc.widen", "k_matrix_tc.issue", "k_matrix_tc.producer_step", "k_matrix_tc.acc_wait",
+        "k_matrix_tc.score", "k_matrix_tc.fold", "k_matrix_tc.consumer_step", "k_matrix_tc.step_barrier",
+        "k_matrix_tc.tiles"};
+    for (int k = 0; k < kTcPhCount; k++)
+        if (!strcmp(name, kTcNames[k]) && c->d_mphase.p) {
+            unsigned long long v[kTcPhCount];
+            CUDA_TRY(c, cudaMemcpy(v, c->d_mphase.p, sizeof v, cudaMemcpyDeviceToHost));
+            if (total_ms) *total_ms = (double)v[k];
+            if (launches) *launches = v[kTcPhTiles];
             return SDBFG_OK;
         }
     for (const KernelStat& k : c->stats)
