@@ -491,6 +491,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                         uint32_t ring_base = 0;                 // completion index of ring slot 0
                         const uint32_t nt = T.ntile;
                         for (uint32_t c0 = 0; c0 < nt; c0 += 32) {
+                            TC_STAMP(t_ld);
                             uint32_t v[32];
                             const uint32_t taddr = tmem + ((warp * 32) << 16) + pb * kTcCols + c0;
                             asm volatile(
@@ -504,6 +505,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                   "=r"(v[31])
                                 : "r"(taddr));
                             asm volatile("tcgen05.wait::ld.sync.aligned;");
+                            if (tid == 0) TC_ADD(kTcPhLd, t_ld);
                             const uint32_t lim = min(32u, nt - c0);
                             const uint32_t lm = T.lastmask[c0 >> 5] & (lim == 32 ? 0xFFFFFFFFu : ((1u << lim) - 1));
 #pragma unroll
@@ -548,6 +550,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                 }
                                 // sum the maxima of the targets completed in these 16 columns
                                 const uint32_t done_now = __popc(lm & (0xFFFFu << (16 * h)));
+                                TC_STAMP(t_fo);
                                 if (done_now && !split) {
                                     group_sync<1>();
                                     if (group) {
@@ -577,6 +580,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                     }
                                     group_sync<1>();
                                 }
+                                if (tid == 0) TC_ADD(kTcPhFold, t_fo);
                                 ring_base += done_now;
                             }
                         }
