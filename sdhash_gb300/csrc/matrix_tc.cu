@@ -145,23 +145,82 @@ __device__ __forceinline__ uint32_t find_segment(const uint32_t* seg_start, uint
     return lo;
 }
 
-// a pair whose full count is above the cut: the reference's staged exits
-// (normal mode: after 8, 16, 32 words) or its 32-byte stage (fast mode),
-// from the row's first 128 bytes (registers) and the target's (shared memory)
-__device__ __forceinline__ uint32_t candidate_match(const uint4 (&aw)[8], const uint4* tw, uint32_t cnt,
-                                                   uint32_t cut, bool fast) {
+// the row's first 128 bytes (the staged re-check needs words 0..31)
+struct RowHead {
+    uint4 w[8];
+};
+
+// A pair whose full count is above the cut (rare): the reference's staged
+// exits (normal mode: after 8, 16, 32 words) or its 32-byte stage (fast
+// mode), from the row's first 128 bytes and the target's (shared memory).
+// Returns (num << 32) | den of the pair's score (0 / 1 when it scores 0).
+// Out of line: the scoring loop is unrolled over 32 columns and must stay
+// small enough for the instruction cache.
+__device__ __noinline__ uint64_t candidate_fraction(RowHead aw, const uint4* tw, uint32_t cnt, uint32_t cut,
+                                                    bool fast, uint32_t max_est) {
     uint32_t c = 0;
+    bool exit = false;
 #pragma unroll
     for (int q = 0; q < 8; q++) {
         const uint4 y = tw[q];
-        c += __popc(aw[q].x & y.x) + __popc(aw[q].y & y.y) + __popc(aw[q].z & y.z) + __popc(aw[q].w & y.w);
+        c += __popc(aw.w[q].x & y.x) + __popc(aw.w[q].y & y.y) + __popc(aw.w[q].z & y.z) + __popc(aw.w[q].w & y.w);
         if (q == 1) {
-            if (fast) return 2 * c + 48 < cut ? 0u : cnt;
-            if (8 * c + 48 < cut) return 0;
+            if (fast) {
+                exit = 2 * c + 48 < cut;
+                break;
+            }
+            if (8 * c + 48 < cut) {
+                exit = true;
+                break;
+            }
         }
-        if (q == 3 && 4 * c + 48 < cut) return 0;
+        if (q == 3 && 4 * c + 48 < cut) {
+            exit = true;
+            break;
+        }
+        if (q == 7) exit = 2 * c + 48 < cut;
     }
-    return 2 * c + 48 < cut ? 0u : cnt;
+    if (exit || cnt <= cut) return 1;
+    return ((uint64_t)(cnt - cut) << 32) | (uint32_t)(max_est - cut);
+}
+
+__device__ __noinline__ double row_maximum(bool active, uint32_t bnum, uint32_t bden, bool counted) {
+    return max_value(active, bnum, bden, counted);
+}
+
+// Sums the maxima of `done` completed targets (completion indices from
+// ring_base) in filter order: group units finish their (reference, target)
+// scores, multi-pass units extend the running sums.  All 128 consumer threads.
+__device__ __noinline__ void fold_ring(const MatParams& P, TcSmem& S, const TcTile& T, uint32_t ring_base,
+                                       uint32_t done, bool group, uint32_t nref, uint32_t nrows, uint32_t t0,
+                                       uint32_t rs, uint32_t tid) {
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (group) {
+        for (uint32_t t = tid; t < done * nref; t += 128) {
+            const uint32_t kk = t % nref, ci = ring_base + t / nref;
+            double sum = -1.0;
+            for (uint32_t r = S.gstart[kk]; r < S.gstart[kk + 1]; r++) {
+                const double m = S.mv[r][ci % kTcRing];
+                if (sum < 0) sum = m;
+                else if (m != 0.0) sum = __dadd_rn(sum, m);
+            }
+            const uint32_t tgt = P.targets[t0 + T.comp[ci]];
+            P.scores[out_index(P, rs != 0, S.gref[kk], tgt)] =
+                final_score(sum, S.gstart[kk + 1] - S.gstart[kk], S.gsparse[kk]);
+        }
+    } else {
+        for (uint32_t t = tid; t < done; t += 128) {
+            const uint32_t ci = ring_base + t;
+            double sum = S.run[T.comp[ci]];
+            for (uint32_t r = 0; r < nrows; r++) {
+                const double m = S.mv[r][ci % kTcRing];
+                if (sum < 0) sum = m;
+                else if (m != 0.0) sum = __dadd_rn(sum, m);
+            }
+            S.run[T.comp[ci]] = sum;
+        }
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
 }
 
 }  // namespace
@@ -306,11 +365,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
             uint32_t bnum = 0, bden = 1;
             bool counted = false;
             const uint32_t nrows = min((uint32_t)kTcRows, U.r1 - rc);
-            uint4 aw[8];  // the row's first 128 bytes, for the staged re-check of candidates
+            RowHead aw;  // the row's first 128 bytes, for the staged re-check of candidates
 #pragma unroll
             for (int q = 0; q < 8; q++)
-                aw[q] = have ? __ldg(reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)fidx * 64) + q)
-                             : make_uint4(0, 0, 0, 0);
+                aw.w[q] = have ? __ldg(reinterpret_cast<const uint4*>(P.filters[rs] + (size_t)fidx * 64) + q)
+                               : make_uint4(0, 0, 0, 0);
             __syncthreads();
             // ---- software pipeline: each step counts tile g (producers) and
             // scores tile g-1 (consumers); one CTA barrier per step.  Tile g
@@ -512,74 +571,47 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             for (uint32_t h = 0; h < 2; h++) {
 #pragma unroll
                                 for (uint32_t q = 16 * h; q < 16 * h + 16; q++) {
-                                    if (q >= lim) break;
-                                    const uint32_t j = c0 + q;
-                                    const uint32_t cnt = (uint32_t)__uint_as_float(v[q]);
-                                    const uint32_t tm = T.tmeta[j];
-                                    const uint32_t s2 = tm & 0xFFFFu;
-                                    if (active && s2 >= (uint32_t)kMinElem) {
-                                        if (s2 != cs2) {
-                                            cs2 = s2;
-                                            const uint32_t sum = s1 + s2;
-                                            ccut = !fastA ? cut_for(S.cut_sum, S.cut256, s1, s2)
-                                                          : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
-                                        }
-                                        counted = true;  // a counted target filter scores at least 0
-                                        if (cnt > ccut) {
-                                            const uint32_t match = candidate_match(aw, T.tw[j], cnt, ccut, fastA);
-                                            if (match > ccut) {
-                                                const uint32_t num = match - ccut, den = min(e1, tm >> 16) - ccut;
+                                    if (q < lim) {
+                                        const uint32_t j = c0 + q;
+                                        const uint32_t tm = T.tmeta[j];
+                                        const uint32_t s2 = tm & 0xFFFFu;
+                                        if (active && s2 >= (uint32_t)kMinElem) {
+                                            if (s2 != cs2) {
+                                                cs2 = s2;
+                                                const uint32_t sum = s1 + s2;
+                                                ccut = !fastA ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
+                                                              : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                                            }
+                                            counted = true;  // a counted target filter scores at least 0
+                                            const uint32_t cnt = (uint32_t)__uint_as_float(v[q]);
+                                            if (cnt > ccut) {
+                                                const uint64_t fr = candidate_fraction(aw, T.tw[j], cnt, ccut, fastA,
+                                                                                       min(e1, tm >> 16));
+                                                const uint32_t num = (uint32_t)(fr >> 32), den = (uint32_t)fr;
                                                 if ((uint64_t)num * bden > (uint64_t)bnum * den) {
                                                     bnum = num;
                                                     bden = den;
                                                 }
                                             }
                                         }
-                                    }
-                                    if ((lm >> q) & 1u) {
-                                        const double m = max_value(active, bnum, bden, counted);
-                                        if (split) {
-                                            if (have) P.slots[P.split[U.split].slot_base + row] = m;
-                                        } else {
-                                            S.mv[tid][((T.tinfo[j] >> 16) & 0xFFu) % kTcRing] = m;
+                                        if ((lm >> q) & 1u) {
+                                            const double m = row_maximum(active, bnum, bden, counted);
+                                            if (split) {
+                                                if (have) P.slots[P.split[U.split].slot_base + row] = m;
+                                            } else {
+                                                S.mv[tid][((T.tinfo[j] >> 16) & 0xFFu) % kTcRing] = m;
+                                            }
+                                            bnum = 0;
+                                            bden = 1;
+                                            counted = false;
                                         }
-                                        bnum = 0;
-                                        bden = 1;
-                                        counted = false;
                                     }
                                 }
                                 // sum the maxima of the targets completed in these 16 columns
                                 const uint32_t done_now = __popc(lm & (0xFFFFu << (16 * h)));
                                 TC_STAMP(t_fo);
-                                if (done_now && !split) {
-                                    group_sync<1>();
-                                    if (group) {
-                                        for (uint32_t t = tid; t < done_now * nref; t += 128) {
-                                            const uint32_t kk = t % nref, ci = ring_base + t / nref;
-                                            double sum = -1.0;
-                                            for (uint32_t r = S.gstart[kk]; r < S.gstart[kk + 1]; r++) {
-                                                const double m = S.mv[r][ci % kTcRing];
-                                                if (sum < 0) sum = m;
-                                                else if (m != 0.0) sum = __dadd_rn(sum, m);
-                                            }
-                                            const uint32_t tgt = P.targets[U.t0 + T.comp[ci]];
-                                            P.scores[out_index(P, rs != 0, S.gref[kk], tgt)] =
-                                                final_score(sum, S.gstart[kk + 1] - S.gstart[kk], S.gsparse[kk]);
-                                        }
-                                    } else {
-                                        for (uint32_t t = tid; t < done_now; t += 128) {
-                                            const uint32_t ci = ring_base + t;
-                                            double sum = S.run[T.comp[ci]];
-                                            for (uint32_t r = 0; r < nrows; r++) {
-                                                const double m = S.mv[r][ci % kTcRing];
-                                                if (sum < 0) sum = m;
-                                                else if (m != 0.0) sum = __dadd_rn(sum, m);
-                                            }
-                                            S.run[T.comp[ci]] = sum;
-                                        }
-                                    }
-                                    group_sync<1>();
-                                }
+                                if (done_now && !split)
+                                    fold_ring(P, S, T, ring_base, done_now, group, nref, nrows, U.t0, rs, tid);
                                 if (tid == 0) TC_ADD(kTcPhFold, t_fo);
                                 ring_base += done_now;
                             }
