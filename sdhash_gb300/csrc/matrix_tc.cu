@@ -44,7 +44,7 @@ constexpr int kTcCols = 256;       // target filters per tile = MMA N (max)
 constexpr int kTcThreads = 256;    // warps 0-3 score (one row each), warps 4-7 widen and issue
 constexpr int kTcChunk = 128;      // K elements (bits) per stage
 constexpr int kTcChunks = 2048 / kTcChunk;
-constexpr int kTcRing = 16;        // completed targets held before their maxima are summed
+constexpr int kTcRing = 8;         // completed targets held before their maxima are summed
 constexpr uint32_t kTcAStage = kTcRows * kTcChunk;   // 16 KB of e4m3
 constexpr uint32_t kTcBStage = kTcCols * kTcChunk;   // 32 KB
 constexpr uint32_t kTcStage = kTcAStage + kTcBStage;
@@ -66,6 +66,7 @@ struct TcSmem {
     TcTile tile[2];
     uint32_t rowf[kTcRows];           // filter index of each reference row (~0: none)
     double mv[kTcRows][kTcRing + 1];  // row maxima of completed targets (ring)
+    uint16_t cstage[32][kTcRows];     // one 32-column slice of counts, column-major per row thread
     double run[kMatMaxTargets];
     uint32_t gref[kTcRows], gstart[kTcRows + 1], gsparse[kTcRows];
     uint16_t cut_sum[1024], cut64_sum[1024], cut256[SDBF_CUTOFF_BINS], cut64[SDBF_CUTOFF_BINS];
@@ -154,10 +155,8 @@ struct RowHead {
 // exits (normal mode: after 8, 16, 32 words) or its 32-byte stage (fast
 // mode), from the row's first 128 bytes and the target's (shared memory).
 // Returns (num << 32) | den of the pair's score (0 / 1 when it scores 0).
-// Out of line: the scoring loop is unrolled over 32 columns and must stay
-// small enough for the instruction cache.
-__device__ __noinline__ uint64_t candidate_fraction(RowHead aw, const uint4* tw, uint32_t cnt, uint32_t cut,
-                                                    bool fast, uint32_t max_est) {
+__device__ __forceinline__ uint64_t candidate_fraction(const RowHead& aw, const uint4* tw, uint32_t cnt,
+                                                      uint32_t cut, bool fast, uint32_t max_est) {
     uint32_t c = 0;
     bool exit = false;
 #pragma unroll
@@ -546,9 +545,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                     TC_STAMP(t_sc);
                     if (ok) {
                         asm volatile("tcgen05.fence::after_thread_sync;");
-                        uint32_t cs2 = 0xFFFFFFFFu, ccut = 0;  // cut cached for the last s2 seen
                         uint32_t ring_base = 0;                 // completion index of ring slot 0
                         const uint32_t nt = T.ntile;
+                        uint32_t pend = 0;  // completed targets in the ring, not yet summed
                         for (uint32_t c0 = 0; c0 < nt; c0 += 32) {
                             TC_STAMP(t_ld);
                             uint32_t v[32];
@@ -564,57 +563,58 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                   "=r"(v[31])
                                 : "r"(taddr));
                             asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+                            for (int q = 0; q < 32; q++) S.cstage[q][tid] = (uint16_t)__uint_as_float(v[q]);
                             if (tid == 0) TC_ADD(kTcPhLd, t_ld);
                             const uint32_t lim = min(32u, nt - c0);
-                            const uint32_t lm = T.lastmask[c0 >> 5] & (lim == 32 ? 0xFFFFFFFFu : ((1u << lim) - 1));
-#pragma unroll
-                            for (uint32_t h = 0; h < 2; h++) {
-#pragma unroll
-                                for (uint32_t q = 16 * h; q < 16 * h + 16; q++) {
-                                    if (q < lim) {
-                                        const uint32_t j = c0 + q;
-                                        const uint32_t tm = T.tmeta[j];
-                                        const uint32_t s2 = tm & 0xFFFFu;
-                                        if (active && s2 >= (uint32_t)kMinElem) {
-                                            if (s2 != cs2) {
-                                                cs2 = s2;
-                                                const uint32_t sum = s1 + s2;
-                                                ccut = !fastA ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
-                                                              : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
-                                            }
-                                            counted = true;  // a counted target filter scores at least 0
-                                            const uint32_t cnt = (uint32_t)__uint_as_float(v[q]);
-                                            if (cnt > ccut) {
-                                                const uint64_t fr = candidate_fraction(aw, T.tw[j], cnt, ccut, fastA,
-                                                                                       min(e1, tm >> 16));
-                                                const uint32_t num = (uint32_t)(fr >> 32), den = (uint32_t)fr;
-                                                if ((uint64_t)num * bden > (uint64_t)bnum * den) {
-                                                    bnum = num;
-                                                    bden = den;
-                                                }
-                                            }
-                                        }
-                                        if ((lm >> q) & 1u) {
-                                            const double m = row_maximum(active, bnum, bden, counted);
-                                            if (split) {
-                                                if (have) P.slots[P.split[U.split].slot_base + row] = m;
-                                            } else {
-                                                S.mv[tid][((T.tinfo[j] >> 16) & 0xFFu) % kTcRing] = m;
-                                            }
-                                            bnum = 0;
-                                            bden = 1;
-                                            counted = false;
+                            const uint32_t lm = T.lastmask[c0 >> 5];
+                            // columns in order (a rolled loop: one copy of the code)
+#pragma unroll 1
+                            for (uint32_t q = 0; q < lim; q++) {
+                                const uint32_t j = c0 + q;
+                                const uint32_t tm = T.tmeta[j];
+                                const uint32_t s2 = tm & 0xFFFFu;
+                                if (active && s2 >= (uint32_t)kMinElem) {
+                                    const uint32_t sum = s1 + s2;
+                                    const uint32_t cut = !fastA
+                                        ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
+                                        : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                                    counted = true;  // a counted target filter scores at least 0
+                                    const uint32_t cnt = S.cstage[q][tid];
+                                    if (cnt > cut) {
+                                        const uint64_t fr =
+                                            candidate_fraction(aw, T.tw[j], cnt, cut, fastA, min(e1, tm >> 16));
+                                        const uint32_t num = (uint32_t)(fr >> 32), den = (uint32_t)fr;
+                                        if ((uint64_t)num * bden > (uint64_t)bnum * den) {
+                                            bnum = num;
+                                            bden = den;
                                         }
                                     }
                                 }
-                                // sum the maxima of the targets completed in these 16 columns
-                                const uint32_t done_now = __popc(lm & (0xFFFFu << (16 * h)));
-                                TC_STAMP(t_fo);
-                                if (done_now && !split)
-                                    fold_ring(P, S, T, ring_base, done_now, group, nref, nrows, U.t0, rs, tid);
-                                if (tid == 0) TC_ADD(kTcPhFold, t_fo);
-                                ring_base += done_now;
+                                if ((lm >> q) & 1u) {
+                                    const double m = row_maximum(active, bnum, bden, counted);
+                                    if (split) {
+                                        if (have) P.slots[P.split[U.split].slot_base + row] = m;
+                                    } else {
+                                        S.mv[tid][((T.tinfo[j] >> 16) & 0xFFu) % kTcRing] = m;
+                                    }
+                                    bnum = 0;
+                                    bden = 1;
+                                    counted = false;
+                                    if (!split && ++pend == (uint32_t)kTcRing) {  // ring full: sum it
+                                        TC_STAMP(t_fo);
+                                        fold_ring(P, S, T, ring_base, pend, group, nref, nrows, U.t0, rs, tid);
+                                        if (tid == 0) TC_ADD(kTcPhFold, t_fo);
+                                        ring_base += pend;
+                                        pend = 0;
+                                    }
+                                }
                             }
+                        }
+                        if (pend) {  // the tile's last completed targets
+                            TC_STAMP(t_fo);
+                            fold_ring(P, S, T, ring_base, pend, group, nref, nrows, U.t0, rs, tid);
+                            if (tid == 0) TC_ADD(kTcPhFold, t_fo);
                         }
                         asm volatile("tcgen05.fence::before_thread_sync;");
                     }
