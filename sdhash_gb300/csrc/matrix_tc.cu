@@ -568,19 +568,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             if (tid == 0) TC_ADD(kTcPhLd, t_ld);
                             const uint32_t lim = min(32u, nt - c0);
                             const uint32_t lm = T.lastmask[c0 >> 5];
-                            // columns in order (a rolled loop: one copy of the code)
-#pragma unroll 1
+                            // columns in order; the loads of four columns are issued together
+                            // (all columns' counts and cuts first, then the rare paths)
+#pragma unroll 4
                             for (uint32_t q = 0; q < lim; q++) {
                                 const uint32_t j = c0 + q;
                                 const uint32_t tm = T.tmeta[j];
                                 const uint32_t s2 = tm & 0xFFFFu;
+                                const uint32_t sum = s1 + s2;
+                                const uint32_t cut = !fastA
+                                    ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
+                                    : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                                const uint32_t cnt = S.cstage[q][tid];
                                 if (active && s2 >= (uint32_t)kMinElem) {
-                                    const uint32_t sum = s1 + s2;
-                                    const uint32_t cut = !fastA
-                                        ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
-                                        : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
                                     counted = true;  // a counted target filter scores at least 0
-                                    const uint32_t cnt = S.cstage[q][tid];
                                     if (cnt > cut) {
                                         const uint64_t fr =
                                             candidate_fraction(aw, T.tw[j], cnt, cut, fastA, min(e1, tm >> 16));
