@@ -60,9 +60,10 @@ def parse():
     ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
     ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve"],
+    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve", "load"],
                     help="stream: bulk digest generation (headline); allpairs: batched uneven all-pairs compare; "
-                         "image: block-mode disk image + query fragments compared against it")
+                         "image: block-mode disk image + query fragments compared against it; serve: continuous-batching "
+                         "server under Poisson load; load: bulk SDBF text load into a resident set")
     ap.add_argument("--image-gib", type=int, default=16, help="image: disk image size (GiB, multiple of 128 MiB)")
     ap.add_argument("--queries", type=int, default=100000, help="image: query fragments")
     ap.add_argument("--ref-filters", type=int, default=244 * 8192, help="serve: block filters in the reference set")
@@ -785,8 +786,98 @@ def main_serve(args):
     return 0
 
 
+LD_METRIC = "SDBF text loaded GB/s"
+
+
+def main_load(args):
+    """Bulk load of a large SDBF reference set from its text form into a
+    resident set (sdbf_set(const char* fname), sdbf/sdbf_set.cc:51-74): the
+    serving workload's block-mode reference image written out with
+    to_string, then loaded K times.  value: the device decode kernel over
+    text already in HBM (k_text_decode, CUDA events); e2e: the whole
+    Context.load_text call from host text (header scan, host->device copy,
+    decode, checks); cpu_baseline: the oracle's line parser, one thread --
+    the reference's loader reads and parses one line at a time."""
+    import torch
+    import sdhash_gb300 as g
+    torch.cuda.set_device(0)
+    ctx = g.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    refs, _, _ = serve_reference_set(args, ctx, stream, 0)
+    text = "".join(d.to_string() for d in refs).encode()
+    nfilt = sum(d.bf_count for d in refs)
+    nb = len(text)
+    for _ in range(max(3, args.warmup)):
+        ctx.load_text(text).close()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ds = ctx.load_text(text)
+        ds.close()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    clocks.stop()
+    # device part: kernel time per launch (CUDA events on the launch stream)
+    ctx.profile(True)
+    launches0 = ctx.launch_count
+    for _ in range(args.steps):
+        ctx.load_text(text).close()
+    ms, n = ctx.kernel_time("k_text_decode")
+    n_launch = ctx.launch_count - launches0
+    ctx.profile(False)
+    kms = ms / max(1, n)
+    # parity at size: a sample of loaded digests equals the digests written out
+    ds = ctx.load_text(text)
+    for i in range(0, len(refs), max(1, len(refs) // 8)):
+        d = ds.digest(i)
+        assert d.to_string() == refs[i].to_string(), "loaded digest differs"
+    ds.close()
+    # CPU: the oracle's parser over a sample of lines, one thread
+    from oracle import Oracle
+    O = Oracle()
+    lines = text.splitlines(True)
+    t1 = time.perf_counter()
+    done = 0
+    k = 0
+    while time.perf_counter() - t1 < 10.0 and k < len(lines):
+        O.parse(lines[k].decode())
+        done += len(lines[k])
+        k += 1
+    t_cpu = time.perf_counter() - t1
+    hbm, src = peaks()
+    alg = nb + nfilt * (256 + 4)   # text read once, filters and (hamming, count) words written
+    achieved = alg / (kms / 1e3) / 1e9
+    line = {"metric": LD_METRIC, "value": nb / (kms / 1e3) / 1e9, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": kms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8 (base64 text)", "data": "synthetic",
+            "config": {"workload": "bulk SDBF text load: block-mode reference set (serving image)",
+                       "digests": len(refs), "filters": nfilt, "text_bytes": nb,
+                       "l2": "text larger than L2 (no flush needed)"},
+            "gpu_launches": int(n_launch // max(1, args.steps)),
+            "clocks": clocks.summary(),
+            "roofline": {"bound": "hbm", "kernel": "k_text_decode", "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_source": f"{src} hbm_gbs (MEASURED_PEAKS.json)",
+                         "algorithmic_bytes_per_launch": alg},
+            "e2e": {"value": nb / wall / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nb,
+                    "d2h_bytes_per_step": 4 * len(refs), "ms_per_step": wall * 1e3,
+                    "filters_per_s": nfilt / wall,
+                    "path": "Context.load_text(host bytes) -> resident set (sdbfg_set_load_text)"},
+            "cpu_baseline": {"value": done / t_cpu / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                             "sample": f"{k} of {len(lines)} lines parsed by the oracle, one thread",
+                             "seconds": round(t_cpu, 3)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "load":
+        return main_load(args)
     if args.workload == "serve":
         return main_serve(args)
     if args.workload == "image":

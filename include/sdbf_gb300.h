@@ -160,6 +160,27 @@ typedef struct {
  * (sdbf::compute_hamming, sdbf_class.cc:388-401). */
 int sdbfg_set_upload(sdbfg_ctx *ctx, const sdbfg_digest_desc *digests, uint32_t n, sdbfg_set **out);
 void sdbfg_set_free(sdbfg_set *set);
+/* Bulk load of SDBF v3 text (one digest per line) into a resident set:
+ * sdbf_set(const char* fname) (sdbf/sdbf_set.cc:51-74) over
+ * sdbf(const std::string&) (sdbf/sdbf_class.cc:144-215) for every line.
+ * The host reads the line headers; the base64 payloads are decoded, checked
+ * and their hamming weights computed on the device.  Loading stops at the
+ * first empty line, as the reference's does.  A malformed line returns
+ * SDBFG_ERR_FORMAT with *bad_line = its index (0-based) and *bad_code = the
+ * value the reference constructor throws for it (-1: shorter than 344
+ * characters, -2: any other format error); no set is created.  Either
+ * pointer may be NULL. */
+int sdbfg_set_load_text(sdbfg_ctx *ctx, const char *text, uint64_t len, sdbfg_set **out, int64_t *bad_line,
+                        int32_t *bad_code);
+/* Header fields of digest i (name owned by the set; filters and
+ * elem_counts are NULL): the sdbf accessors name(), input_size(),
+ * filter_count() (sdbf/sdbf_class.h:23-121). */
+int sdbfg_set_digest_info(const sdbfg_set *set, uint32_t i, sdbfg_digest_desc *out);
+/* Copies digest i's filters (bf_count*256 bytes; the folded bytes after
+ * sdbfg_set_fast) and, if elem_counts is not NULL, its per-filter element
+ * counts (sdbf::get_elem_count, sdbf_class.cc:406-415) back to the host. */
+int sdbfg_set_read_digest(sdbfg_ctx *ctx, const sdbfg_set *set, uint32_t i, uint8_t *filters,
+                          uint16_t *elem_counts);
 /* sdbf::fast (sdbf/sdbf_class.cc:425-439) on digests [first, first+count)
  * of a resident set: every filter's 256 bytes are folded into its first 64
  * (bloom_filter::fold(2), bloom_filter.cc:262-288; the other bytes are left

@@ -100,6 +100,40 @@ char *ref_compare_to_files_fast(const char *qname, const char *tname, int thresh
     return out;
 }
 
+// Loads a file of SDBF lines with sdbf_set(const char*) (sdbf_set.cc:51-74).
+// On success returns the loaded digests re-encoded with to_string, one per
+// line (malloc'd).  When a line throws, returns NULL with the thrown value in
+// *err and, in *bad_line, the index of the first line that sdbf(const
+// std::string&) rejects when the file is read line by line the same way.
+char *ref_load_file(const char *fname, int *err, int *bad_line) {
+    *err = 0;
+    *bad_line = -1;
+    try {
+        sdbf_set set(fname);
+        std::string r;
+        for (uint32_t i = 0; i < set.size(); i++) {
+            r += set.at(i)->to_string();
+            delete set.at(i);
+        }
+        char *out = (char *)malloc(r.size() + 1);
+        memcpy(out, r.c_str(), r.size() + 1);
+        return out;
+    } catch (int e) {
+        *err = e;
+    }
+    std::ifstream f(fname, std::ifstream::in | std::ios::binary);
+    std::string line;
+    for (int i = 0; std::getline(f, line) && !line.empty(); i++) {
+        try {
+            sdbf s(line);
+        } catch (int) {
+            *bad_line = i;
+            break;
+        }
+    }
+    return NULL;
+}
+
 void ref_free(void *p) { free(p); }
 
 }  // extern "C"

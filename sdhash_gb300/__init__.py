@@ -106,6 +106,10 @@ def lib() -> C.CDLL:
         L.sdbfg_set_free.argtypes = [vp]
         L.sdbfg_set_fast.argtypes = [vp, vp, C.c_uint32, C.c_uint32]
         L.sdbfg_set_size.argtypes = [vp]
+        L.sdbfg_set_load_text.argtypes = [vp, C.c_char_p, C.c_uint64, C.POINTER(vp), C.POINTER(C.c_int64),
+                                          C.POINTER(C.c_int32)]
+        L.sdbfg_set_digest_info.argtypes = [vp, C.c_uint32, C.POINTER(DigestDesc)]
+        L.sdbfg_set_read_digest.argtypes = [vp, vp, C.c_uint32, vp, vp]
         L.sdbfg_set_size.restype = C.c_uint32
         L.sdbfg_score_pairs.argtypes = [vp, vp, vp, u32p, u32p, C.c_uint64, i32p]
         L.sdbfg_compare_all.argtypes = [vp, vp, i32p]
@@ -221,11 +225,17 @@ class Digest:
 
 
 class DeviceSet:
-    """Digests resident in device memory (sdbfg_set)."""
+    """Digests resident in device memory (sdbfg_set).  ``digests`` holds the
+    host digests a set was uploaded from, or None for a set loaded from SDBF
+    text on the device (``digest(i)`` reads one back)."""
 
-    def __init__(self, ctx: "Context", digests: list[Digest]):
+    def __init__(self, ctx: "Context", digests: list[Digest] | None, _handle=None):
         self.ctx = ctx
         self.digests = digests
+        if _handle is not None:
+            self.h = _handle
+            self.n = int(lib().sdbfg_set_size(_handle))
+            return
         keep: list = []
         arr = (DigestDesc * max(1, len(digests)))()
         for i, d in enumerate(digests):
@@ -234,13 +244,38 @@ class DeviceSet:
         rc = lib().sdbfg_set_upload(ctx.h, arr, len(digests), C.byref(h))
         ctx._check(rc)
         self.h = h
+        self.n = len(digests)
 
     def __len__(self):
-        return len(self.digests)
+        return self.n
+
+    def _info(self, i: int) -> DigestDesc:
+        d = DigestDesc()
+        if lib().sdbfg_set_digest_info(self.h, i, C.byref(d)) != 0:
+            raise IndexError(i)
+        return d
+
+    def name(self, i: int) -> str:
+        if self.digests is not None:
+            return self.digests[i].name
+        return self._info(i).name.decode()
+
+    def names(self) -> list[str]:
+        return [self.name(i) for i in range(self.n)]
+
+    def digest(self, i: int) -> Digest:
+        """Digest i as held on the device (folded filters after fast())."""
+        d = self._info(i)
+        filters = np.zeros(d.bf_count * 256, dtype=np.uint8)
+        counts = np.zeros(d.bf_count, dtype=np.uint16)
+        self.ctx._check(lib().sdbfg_set_read_digest(self.ctx.h, self.h, i, filters.ctypes.data, counts.ctypes.data))
+        out = Digest(d.name.decode(), d.orig_size, d.bf_count, d.last_count, d.max_elem, d.dd_block_size, filters,
+                     counts if d.dd_block_size else None)
+        return out
 
     def fast(self, first: int = 0, count: int | None = None) -> "DeviceSet":
         """sdbf::fast on digests [first, first+count): fold to 64 bytes on the device."""
-        n = len(self.digests) - first if count is None else count
+        n = self.n - first if count is None else count
         self.ctx._check(lib().sdbfg_set_fast(self.ctx.h, self.h, first, n))
         return self
 
@@ -383,6 +418,28 @@ class Context:
         return res
 
     # ---------------------------------------------------------- compare
+    def load_text(self, text: bytes | str) -> DeviceSet:
+        """A resident set from SDBF v3 text, one digest per line, as
+        sdbf_set(const char* fname) loads a file (sdbf/sdbf_set.cc:51-74):
+        headers read on the host, base64 payloads decoded on the device.
+        A malformed line raises SdbfError with the reference constructor's
+        throw value (-1 or -2) and ``line`` = its index."""
+        b = text.encode() if isinstance(text, str) else bytes(text)
+        h = C.c_void_p()
+        bad_line, bad_code = C.c_int64(-1), C.c_int32(0)
+        rc = lib().sdbfg_set_load_text(self.h, b, len(b), C.byref(h), C.byref(bad_line), C.byref(bad_code))
+        if rc == -4:  # SDBFG_ERR_FORMAT
+            e = SdbfError(int(bad_code.value), f"line {bad_line.value}")
+            e.line = int(bad_line.value)
+            raise e
+        self._check(rc)
+        return DeviceSet(self, None, _handle=h)
+
+    def load_file(self, path: str) -> DeviceSet:
+        """load_text of a file's contents (sdbf_set(const char* fname))."""
+        with open(path, "rb") as f:
+            return self.load_text(f.read())
+
     def upload(self, digests: list[Digest]) -> DeviceSet:
         """Resident set; digests folded with Digest.fast() keep their fast mode."""
         ds = DeviceSet(self, digests)
@@ -619,13 +676,25 @@ class sdbf_set:  # noqa: N801
         self.setname = "default"
         self.sep = "|"
         self._lock = threading.Lock()
+        self._resident: DeviceSet | None = None
+        self._resident_key = None
         if fname is not None and os.path.isfile(fname):
-            with open(fname) as f:
-                for line in f:
-                    if not line.strip():
-                        break
-                    self.items.append(sdbf.from_string(line))
+            # the whole file is parsed on the device (Context.load_file); the
+            # resident set is kept for comparisons until the items change
+            ds = default_context().load_file(fname)
+            self.items = [sdbf(_digest=ds.digest(i)) for i in range(len(ds))]
+            self._resident, self._resident_key = ds, self._key()
             self.setname = fname
+
+    def _key(self):
+        return tuple((id(s), s.digest.fastmode) for s in self.items)
+
+    def _device_set(self, ctx: "Context") -> "DeviceSet":
+        """The items as a resident set: the one loaded from the file while the
+        items are unchanged, else a fresh upload."""
+        if self._resident is not None and self._resident.ctx is ctx and self._resident_key == self._key():
+            return self._resident
+        return ctx.upload([s.digest for s in self.items])
 
     def at(self, pos: int):
         return self.items[pos] if pos < len(self.items) else None
@@ -667,7 +736,7 @@ class sdbf_set:  # noqa: N801
         if n < 2:
             return ""
         ctx = default_context()
-        ds = ctx.upload([s.digest for s in self.items])
+        ds = self._device_set(ctx)
         scores = ctx.compare_all(ds)
         pairs = [(i, j) for i in range(n) for j in range(i + 1, n)]
         names = [s.name() for s in self.items]
@@ -692,8 +761,8 @@ class sdbf_set:  # noqa: N801
         if not self.items or not other.items:
             return ""
         ctx = default_context()
-        q = ctx.upload([s.digest for s in self.items])
-        t = ctx.upload([s.digest for s in other.items])
+        q = self._device_set(ctx)
+        t = other._device_set(ctx)
         scores = ctx.compare_to(q, t)
         pairs = [(i, j) for i in range(len(self.items)) for j in range(len(other.items))]
         return _result_lines([s.name() for s in self.items], [s.name() for s in other.items], pairs,

@@ -15,6 +15,8 @@
 
 static std::atomic<uint64_t> g_set_serial{1};
 
+uint64_t next_set_serial() { return g_set_serial.fetch_add(1); }
+
 // -------------------------------------------------------------- comparison
 extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint32_t n, sdbfg_set** out) {
     if (!c || !out || (n && !ds)) return SDBFG_ERR_ARG;
@@ -23,7 +25,7 @@ extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint3
     auto* s = new sdbfg_set();
     s->ctx = c;
     s->n = n;
-    s->serial = g_set_serial.fetch_add(1);
+    s->serial = next_set_serial();
     uint64_t total = 0;
     std::vector<CmpDigest> dig(n);
     for (uint32_t i = 0; i < n; i++) {
@@ -45,10 +47,20 @@ extern "C" int sdbfg_set_upload(sdbfg_ctx* c, const sdbfg_digest_desc* ds, uint3
     s->fast.assign(n, 0);
     s->bf_count.resize(n);
     s->last_elem.resize(n);
+    s->orig_size.resize(n);
+    s->max_elem.resize(n);
+    s->last_count.resize(n);
+    s->dd_block.resize(n);
+    s->first.resize(n);
     for (uint32_t i = 0; i < n; i++) {
         const sdbfg_digest_desc& d = ds[i];
         s->names[i] = d.name ? d.name : "";
         s->bf_count[i] = d.bf_count;
+        s->orig_size[i] = d.orig_size;
+        s->max_elem[i] = d.max_elem;
+        s->last_count[i] = d.elem_counts ? 0 : d.last_count;
+        s->dd_block[i] = d.elem_counts ? d.dd_block_size : 0;
+        s->first[i] = dig[i].first;
         memcpy(&filt[(uint64_t)dig[i].first * 256], d.filters, (uint64_t)d.bf_count * 256);
         for (uint32_t f = 0; f < d.bf_count; f++) {
             // get_elem_count (sdbf_class.cc:406-415)

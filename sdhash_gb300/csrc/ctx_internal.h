@@ -130,10 +130,17 @@ struct sdbfg_set {
     std::vector<uint32_t> bf_count;
     std::vector<uint32_t> last_elem;  // element count of the last filter (swap rule)
     std::vector<uint8_t> fast;         // per digest: folded by sdbfg_set_fast
+    // header fields of the SDBF text form (sdbf::to_string, sdbf_class.cc:293-334)
+    std::vector<uint64_t> orig_size;
+    std::vector<uint32_t> max_elem, last_count, dd_block;  // dd_block 0: stream digest
     uint64_t serial = 0;               // identifies the set in cached comparison plans
     uint64_t total_filters = 0;
+    std::vector<uint32_t> first;       // first filter of each digest in d_filters
     DevBuf d_filters, d_meta, d_digests;
 };
+
+// Serial number of a new set (cached comparison plans are keyed by it).
+uint64_t next_set_serial();
 
 // A comparison job prepared for the matrix engine: work units sorted by
 // size, the target list, split-pair table and slot array, and (once run) a

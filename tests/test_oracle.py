@@ -128,3 +128,20 @@ def test_oracle_fast_mode_matches_reference(oracle, golden):
     for d in dd:
         oracle.fast(oracle.fast(d))  # folding twice changes nothing
     assert oracle.compare_all(dd, -1) == g["compare_all_dd_fast_tneg1"]
+
+
+def test_text_load_fixture_lines_are_canonical(oracle):
+    """The reference loader's outputs recorded in tests/golden/text_load.json
+    (digests re-encoded by to_string) parse and re-encode unchanged in the
+    oracle, and the error cases carry the reference's throw values."""
+    import json
+    with open(os.path.join(os.path.dirname(__file__), "golden", "text_load.json")) as f:
+        cases = json.load(f)["cases"]
+    ok = [c for c in cases if "lines" in c["expect"]]
+    bad = [c for c in cases if "err" in c["expect"]]
+    assert len(ok) >= 5 and len(bad) >= 5
+    for c in ok:
+        for line in c["expect"]["lines"]:
+            assert oracle.parse(line).to_string() == line, c["name"]
+    assert {c["expect"]["err"] for c in bad} == {-1, -2}
+    assert all(c["expect"]["line"] >= 0 for c in bad)
