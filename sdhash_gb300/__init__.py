@@ -369,7 +369,10 @@ class Context:
         offsets, lens = _u64(offsets), _u64(lens)
         n = len(lens)
         cap = self.capacity(lens, dd_block_size)
-        if out_filters is None or out_filters.size < cap * 256:
+        # a buffer made here is the digests' own storage (each Digest views
+        # its slice); a caller's buffer may be reused, so its slices are copied
+        own = out_filters is None or out_filters.size < cap * 256
+        if own:
             out_filters = np.zeros(max(1, cap) * 256, dtype=np.uint8)
         counts = np.zeros(max(1, cap), dtype=np.uint16)
         res = (DigestResult * max(1, n))()
@@ -385,7 +388,9 @@ class Context:
                 continue
             o, k = int(r.filter_offset), int(r.bf_count)
             name = names[i] if names is not None else f"f{i}"
-            filt = out_filters[o * 256:(o + k) * 256].copy()
+            filt = out_filters[o * 256:(o + k) * 256]
+            if not own:
+                filt = filt.copy()
             if dd_block_size:
                 out.append(Digest(name, int(lens[i]), k, 0, BLOCK_MAX_ELEM, dd_block_size, filt,
                                   counts[o:o + k].copy()))

@@ -22,6 +22,7 @@ namespace sdbfg_host {
 
 constexpr uint32_t kMaxTilesPerLaunch = 1u << 18;  // 2 GiB of stream input per launch group
 constexpr uint64_t kMaxBytesPerLaunch = 2ull << 30;
+constexpr uint64_t kFirstHostGroupBytes = 256ull << 20;  // first group of a host-input stream batch
 constexpr uint32_t kMinFile = 512;                 // MIN_FILE_SIZE (sdbf_defines.h:56)
 constexpr uint64_t kPairsPerLaunch = 1ull << 22;
 constexpr int kSlots = 3;  // stream-mode launch groups in flight

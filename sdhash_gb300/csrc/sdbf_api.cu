@@ -202,7 +202,12 @@ struct Group {  // consecutive inputs processed by one launch sequence
 };
 
 // Splits inputs into launch groups bounded by tiles (stream) or bytes.
-std::vector<Group> make_groups(const uint64_t* lens, uint32_t n, uint32_t dd) {
+// Launch groups of consecutive inputs, each at most kMaxTilesPerLaunch tiles
+// and kMaxBytesPerLaunch bytes; the first group at most first_cap bytes
+// (host inputs: a short first copy lets the kernels start early while the
+// later groups' copies overlap them).
+std::vector<Group> make_groups(const uint64_t* lens, uint32_t n, uint32_t dd,
+                               uint64_t first_cap = kMaxBytesPerLaunch) {
     std::vector<Group> gs;
     uint32_t start = 0;
     uint64_t tiles = 0, bytes = 0;
@@ -215,7 +220,8 @@ std::vector<Group> make_groups(const uint64_t* lens, uint32_t n, uint32_t dd) {
             }
         }
         const uint64_t b = (lens[i] + 15) & ~15ull;
-        if (i > start && (tiles + t > kMaxTilesPerLaunch || bytes + b > kMaxBytesPerLaunch)) {
+        const uint64_t cap_bytes = gs.empty() ? std::min(first_cap, kMaxBytesPerLaunch) : kMaxBytesPerLaunch;
+        if (i > start && (tiles + t > kMaxTilesPerLaunch || bytes + b > cap_bytes)) {
             gs.push_back({start, i - start});
             start = i;
             tiles = 0;
@@ -371,7 +377,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
     CUDA_TRY(c, cudaMemsetAsync(c->d_binfo.p, 0, std::max<size_t>(1, n) * sizeof(FileInfoDev), c->stream));
     CUDA_TRY(c, cudaMemsetAsync(c->d_total.p, 0, 64, c->stream));
     CUDA_TRY(c, cudaEventRecord(c->ev_start, c->stream));
-    const std::vector<Group> groups = make_groups(lens, n, 0);
+    const std::vector<Group> groups = make_groups(lens, n, 0, host_data ? kFirstHostGroupBytes : kMaxBytesPerLaunch);
     cudaEvent_t prev_scan = c->ev_start;
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
