@@ -37,6 +37,7 @@ extern "C" {
 
 typedef struct sdbfg_ctx sdbfg_ctx;
 typedef struct sdbfg_set sdbfg_set;
+typedef struct sdbfg_index sdbfg_index;
 
 /* ---------------------------------------------------------------- context
  * One context = one device + one CUDA stream + reusable device buffers.
@@ -172,6 +173,40 @@ void sdbfg_set_free(sdbfg_set *set);
  * pointer may be NULL. */
 int sdbfg_set_load_text(sdbfg_ctx *ctx, const char *text, uint64_t len, sdbfg_set **out, int64_t *bad_line,
                         int32_t *bad_code);
+/* ------------------------------------------------------------ indexes
+ * An index is one large Bloom filter (bloom_filter, sdbf/bloom_filter.cc),
+ * resident on the device.  sdbfg_index_load_file reads an index file as
+ * bloom_filter(string indexfilename) does (bloom_filter.cc:87-118): the
+ * header "sdbf-idx:<bf_size>:<elem_count>:<hash_count>:<bit_mask>:<compressed
+ * size>:<set name>" and the LZ4-compressed filter.  An unreadable file
+ * returns SDBFG_ERR_ARG (the reference throws -1), a malformed one
+ * SDBFG_ERR_FORMAT (-2).  sdbfg_index_create makes one from raw filter
+ * bytes (bloom_filter(size, hash_count, 0, 0) plus its contents; size a
+ * power of two >= 64, bit mask size*8-1). */
+int sdbfg_index_load_file(sdbfg_ctx *ctx, const char *path, sdbfg_index **out);
+int sdbfg_index_create(sdbfg_ctx *ctx, const uint8_t *bits, uint64_t bf_size, uint32_t hash_count, const char *name,
+                       sdbfg_index **out);
+void sdbfg_index_free(sdbfg_index *index);
+int sdbfg_index_info(const sdbfg_index *index, uint64_t *bf_size, uint64_t *elem_count, uint32_t *hash_count,
+                     uint64_t *bit_mask, const char **name);
+/* Block-mode digests (as sdbfg_digest_batch with dd_block_size > 0) with
+ * the index search of sdhash --index-search (sdbf::gen_block_hash with an
+ * index list, sdbf/sdbf_core.cc:141-191; check_indexes :482-493): every
+ * fourth counted feature of each block is looked up in every index, and
+ * out_hits[slot * nidx + i] receives how many of them index i holds (all
+ * hash bits set) for the filter in output slot `slot`.  The reference
+ * prints "<name> [<block>] |<index set name>|<hits>" for hits > 4
+ * (print_indexes :458-472); out_hits has out_cap * nidx bytes. */
+int sdbfg_digest_batch_search(sdbfg_ctx *ctx, const uint8_t *host_data, const uint64_t *offsets,
+                              const uint64_t *lens, uint32_t n, uint32_t dd_block_size, uint8_t *out_filters,
+                              uint64_t out_cap, uint16_t *out_counts, sdbfg_digest_result *results,
+                              const sdbfg_index *const *indexes, uint32_t nidx, uint8_t *out_hits);
+/* LZ4 block decode of in_len bytes into exactly out_len bytes (the index
+ * file payload, LZ4_uncompress in bloom_filter::decompress,
+ * bloom_filter.cc:185-190); returns the input bytes used or
+ * SDBFG_ERR_FORMAT.  Host-only. */
+int64_t sdbfg_lz4_decode(const uint8_t *in, uint64_t in_len, uint8_t *out, uint64_t out_len);
+
 /* Header fields of digest i (name owned by the set; filters and
  * elem_counts are NULL): the sdbf accessors name(), input_size(),
  * filter_count() (sdbf/sdbf_class.h:23-121). */

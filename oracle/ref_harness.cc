@@ -21,6 +21,7 @@
 
 #include "sdbf_class.h"
 #include "sdbf_set.h"
+#include "index_info.h"
 #include "sdbf_defines.h"
 
 extern "C" {
@@ -132,6 +133,89 @@ char *ref_load_file(const char *fname, int *err, int *bad_line) {
         }
     }
     return NULL;
+}
+
+// sdhash --index for one group of inputs (sdhash-src/sdhash_threads.cc:
+// 376-470): a new 64 MiB index, every input hashed into a set with the index
+// attached (stream mode when dd_block_size is 0, as --index does for files
+// below 16 MiB; block mode otherwise), the set written as SDBF text to
+// sdbf_path and the index, named after sdbf_path, to idx_path.
+int ref_index_build(const char **names, const unsigned char **bufs, const unsigned long long *lens, int n,
+                    unsigned dd_block_size, const char *sdbf_path, const char *idx_path) {
+    bloom_filter *index1 = new bloom_filter(64ull << 20, 5, 0, 0.01);
+    index_info *info = (index_info *)calloc(1, sizeof(index_info));
+    info->index = index1;
+    sdbf_set *set1 = new sdbf_set(index1);
+    for (int i = 0; i < n; i++) {
+        std::vector<char> copy(bufs[i], bufs[i] + lens[i]);
+        try {
+            set1->add(new sdbf(names[i], &copy[0], dd_block_size, lens[i], info));
+        } catch (int) {
+        }
+    }
+    std::ofstream os(sdbf_path, std::ios::out | std::ios::binary);
+    os << set1->to_string();
+    os.close();
+    set1->index->set_name(sdbf_path);
+    const int rc = set1->index->write_out(idx_path);
+    for (uint32_t i = 0; i < set1->size(); i++) delete set1->at(i);
+    delete set1;
+    delete index1;
+    free(info);
+    return rc;
+}
+
+// sdhash --index-search (sdhash-src/sdhash.cc:231-266, 638-652): the index
+// files and the sets beside them loaded as the CLI loads them, every input
+// hashed in block mode with that index list, and set1->index_results()
+// returned (malloc'd).
+char *ref_index_search(const char **idx_paths, const char **set_paths, int nidx, const char **names,
+                       const unsigned char **bufs, const unsigned long long *lens, int n, unsigned dd_block_size) {
+    std::vector<bloom_filter *> indexlist;
+    std::vector<sdbf_set *> setlist;
+    index_info *info = (index_info *)calloc(1, sizeof(index_info));
+    info->indexlist = &indexlist;
+    info->setlist = &setlist;
+    for (int i = 0; i < nidx; i++) {
+        bloom_filter *b = new bloom_filter(std::string(idx_paths[i]));
+        indexlist.push_back(b);
+        sdbf_set *tmp = new sdbf_set(set_paths[i]);
+        setlist.push_back(tmp);
+        tmp->index = b;
+    }
+    sdbf_set *set1 = new sdbf_set();
+    for (int i = 0; i < n; i++) {
+        std::vector<char> copy(bufs[i], bufs[i] + lens[i]);
+        try {
+            set1->add(new sdbf(names[i], &copy[0], dd_block_size, lens[i], info));
+        } catch (int) {
+        }
+    }
+    std::string r = set1->index_results();
+    for (uint32_t i = 0; i < set1->size(); i++) delete set1->at(i);
+    delete set1;
+    for (size_t k = 0; k < setlist.size(); k++) {
+        for (uint32_t m = 0; m < setlist[k]->size(); m++) delete setlist[k]->at(m);
+        delete setlist[k];
+        delete indexlist[k];
+    }
+    free(info);
+    char *out = (char *)malloc(r.size() + 1);
+    memcpy(out, r.c_str(), r.size() + 1);
+    return out;
+}
+
+// An index file read by bloom_filter(string) (bloom_filter.cc:87-118): copies
+// its filter bytes (up to cap) and returns the filter size, or -1 / -2 as the
+// constructor throws.
+long long ref_index_bits(const char *path, unsigned char *out, unsigned long long cap) {
+    try {
+        bloom_filter b((std::string(path)));
+        memcpy(out, b.bf, b.bf_size < cap ? b.bf_size : cap);
+        return (long long)b.bf_size;
+    } catch (int e) {
+        return e;
+    }
 }
 
 void ref_free(void *p) { free(p); }

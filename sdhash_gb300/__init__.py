@@ -106,6 +106,15 @@ def lib() -> C.CDLL:
         L.sdbfg_set_free.argtypes = [vp]
         L.sdbfg_set_fast.argtypes = [vp, vp, C.c_uint32, C.c_uint32]
         L.sdbfg_set_size.argtypes = [vp]
+        L.sdbfg_index_load_file.argtypes = [vp, C.c_char_p, C.POINTER(vp)]
+        L.sdbfg_index_create.argtypes = [vp, vp, C.c_uint64, C.c_uint32, C.c_char_p, C.POINTER(vp)]
+        L.sdbfg_index_free.argtypes = [vp]
+        L.sdbfg_index_free.restype = None
+        L.sdbfg_index_info.argtypes = [vp, u64p, u64p, C.POINTER(C.c_uint32), u64p, C.POINTER(C.c_char_p)]
+        L.sdbfg_digest_batch_search.argtypes = [vp, vp, u64p, u64p, C.c_uint32, C.c_uint32, vp, C.c_uint64, vp, vp,
+                                                C.POINTER(vp), C.c_uint32, vp]
+        L.sdbfg_lz4_decode.argtypes = [vp, C.c_uint64, vp, C.c_uint64]
+        L.sdbfg_lz4_decode.restype = C.c_int64
         L.sdbfg_set_load_text.argtypes = [vp, C.c_char_p, C.c_uint64, C.POINTER(vp), C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int32)]
         L.sdbfg_set_digest_info.argtypes = [vp, C.c_uint32, C.POINTER(DigestDesc)]
@@ -222,6 +231,31 @@ class Digest:
         if self.elem_counts is not None:
             return int(self.elem_counts[i])
         return self.max_elem if i < self.bf_count - 1 else self.last_count
+
+
+class Index:
+    """An index filter resident on the device (sdbfg_index): the reference's
+    bloom_filter as read from an index file (sdbf/bloom_filter.cc:87-118)."""
+
+    def __init__(self, ctx: "Context", handle):
+        self.ctx = ctx
+        self.h = handle
+        size, elem, mask = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        hc, name = C.c_uint32(), C.c_char_p()
+        lib().sdbfg_index_info(handle, C.byref(size), C.byref(elem), C.byref(hc), C.byref(mask), C.byref(name))
+        self.bf_size, self.elem_count, self.hash_count, self.bit_mask = size.value, elem.value, hc.value, mask.value
+        self.name = (name.value or b"").decode(errors="surrogateescape")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sdbfg_index_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class DeviceSet:
@@ -397,6 +431,63 @@ class Context:
             else:
                 out.append(Digest(name, int(lens[i]), k, int(r.last_count), STREAM_MAX_ELEM, 0, filt, None))
         return out
+
+    def load_index(self, path: str) -> Index:
+        """bloom_filter(string indexfilename): an index file, resident on the device.
+        An unreadable file raises SdbfError(-1), a malformed one SdbfError(-2)."""
+        h = C.c_void_p()
+        rc = lib().sdbfg_index_load_file(self.h, os.fsencode(path), C.byref(h))
+        if rc == -1:
+            raise SdbfError(-1, path)
+        if rc == -4:
+            raise SdbfError(-2, path)
+        self._check(rc)
+        return Index(self, h)
+
+    def index_from_bits(self, bits: np.ndarray, hash_count: int = 5, name: str = "") -> Index:
+        """An index from raw filter bytes (size a power of two >= 64)."""
+        bits = np.ascontiguousarray(bits, dtype=np.uint8)
+        h = C.c_void_p()
+        self._check(lib().sdbfg_index_create(self.h, bits.ctypes.data, bits.size, hash_count, name.encode(),
+                                             C.byref(h)))
+        return Index(self, h)
+
+    def digest_search(self, buffers, names, dd_block_size: int, indexes: list[Index]):
+        """Block-mode digests with the index search of sdhash --index-search
+        (sdbf_core.cc:141-191): returns (digests, hits) where hits[k] is a
+        (bf_count, len(indexes)) uint8 array for digest k (None where the
+        input is too small): sampled features of each block found in each index."""
+        lens = np.array([len(b) for b in buffers], dtype=np.uint64)
+        offs = np.zeros(len(buffers), dtype=np.uint64)
+        tot = 0
+        for i, b in enumerate(buffers):
+            offs[i] = tot
+            tot += (len(b) + 15) & ~15
+        data = np.zeros(max(16, tot), dtype=np.uint8)
+        for i, b in enumerate(buffers):
+            data[int(offs[i]):int(offs[i]) + len(b)] = np.frombuffer(bytes(b), dtype=np.uint8)
+        n, nidx = len(lens), len(indexes)
+        cap = self.capacity(lens, dd_block_size)
+        out_filters = np.zeros(max(1, cap) * 256, dtype=np.uint8)
+        counts = np.zeros(max(1, cap), dtype=np.uint16)
+        hits = np.zeros(max(1, cap * nidx), dtype=np.uint8)
+        res = (DigestResult * max(1, n))()
+        arr = (C.c_void_p * max(1, nidx))(*[x.h for x in indexes])
+        self._check(lib().sdbfg_digest_batch_search(self.h, data.ctypes.data, _ptr(offs), _ptr(lens), n, dd_block_size,
+                                                    out_filters.ctypes.data, cap, counts.ctypes.data, res, arr, nidx,
+                                                    hits.ctypes.data))
+        digs, hit_rows = [], []
+        for i in range(n):
+            r = res[i]
+            if r.status != 0:
+                digs.append(None)
+                hit_rows.append(None)
+                continue
+            o, k = int(r.filter_offset), int(r.bf_count)
+            digs.append(Digest(names[i], int(lens[i]), k, 0, BLOCK_MAX_ELEM, dd_block_size,
+                               out_filters[o * 256:(o + k) * 256], counts[o:o + k].copy()))
+            hit_rows.append(hits[o * nidx:(o + k) * nidx].reshape(k, nidx).copy())
+        return digs, hit_rows
 
     def digest_buffers(self, buffers, names=None, dd_block_size: int = 0):
         """Digest a list of bytes-like inputs."""

@@ -24,7 +24,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = os.environ.get("SDBFG_ARCH", "-gencode=arch=compute_103a,code=sm_103a")
 CU_SOURCES = ["gen_kernels.cu", "compare_kernels.cu", "matrix_tc.cu", "sdbf_api.cu", "compare_api.cu", "serve.cu",
-              "noalloc.cu", "text_load.cu"]
+              "noalloc.cu", "text_load.cu",
+              "index_search.cu"]
 CPP_SOURCES = ["sdbf_text.cpp", "../compat/sdbf_compat.cpp"]
 HEADERS = ["gen_kernels.h", "compare_kernels.h", "compare_device.cuh", "ctx_internal.h", "matrix_plan.h", "sdbf_device.cuh", "sdbf_tables.h", "../compat/sdbf_class.h",
            "../compat/sdbf_set.h", "../compat/sdbf_conf.h"]

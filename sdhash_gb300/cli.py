@@ -12,7 +12,8 @@ pairs, `-c` compares the digests of one SDBF file (all pairs) or of two
 (every digest of the first against every digest of the second).  Result
 lines, separators, thresholds and `--fast` are the reference's.  Not
 offered: `-s` (filter sampling seeds rand() from time() in the reference),
-`--large`, `--index`, `--index-search`, `--details`.
+`--large`, `--index` (index building), `--details`.  `--index-search DIR`
+looks every block up in the directory's index files on the GPU.
 """
 from __future__ import annotations
 
@@ -64,10 +65,14 @@ def _collect(inputs, deep: bool):
     return files
 
 
-def _hash(ctx, files, block_kb: int, seg: int, name_for_stdin=None, stdin_data=None):
+def _hash(ctx, files, block_kb: int, seg: int, name_for_stdin=None, stdin_data=None, indexes=None):
+    """Digests of the inputs in the reference's set order; with indexes
+    (block mode only) also each digest's index-search hits per block."""
     import numpy as np
     import sdhash_gb300 as g
     digs = []
+    hits = []
+
     def seg_digests(data, name, dd):
         # a segment digests csize bytes read from the stream, zero-filled past
         # its end, and records the bytes actually read (sdbf_class.cc:71-88)
@@ -80,17 +85,27 @@ def _hash(ctx, files, block_kb: int, seg: int, name_for_stdin=None, stdin_data=N
             b[:len(part)] = part
             bufs.append(b)
             got.append(len(part))
-        out = ctx.digest_buffers(bufs, [nm for nm, _, _ in segs], dd)
+        names = [nm for nm, _, _ in segs]
+        if indexes is not None:
+            out, hr = ctx.digest_search(bufs, names, dd, indexes)
+        else:
+            out, hr = ctx.digest_buffers(bufs, names, dd), [None] * len(bufs)
         res = []
-        for d, n in zip(out, got):
+        for d, h, n in zip(out, hr, got):
             if d is not None and n >= 512:
                 d.orig_size = n
                 res.append(d)
+                hits.append(h)
         return res
+
+    def done():
+        items = [g.sdbf(_digest=d) for d in digs]
+        return (items, hits) if indexes is not None else items
 
     if stdin_data is not None:
         dd = (block_kb if block_kb > 0 else 16) * KB
-        return [g.sdbf(_digest=d) for d in seg_digests(stdin_data, name_for_stdin or "stdin", dd)]
+        digs += seg_digests(stdin_data, name_for_stdin or "stdin", dd)
+        return done()
     small = [f for f in files if os.path.getsize(f) < 16 * MB]
     large = [f for f in files if os.path.getsize(f) >= 16 * MB]
     for group, is_large in ((small, False), (large, True)):
@@ -106,7 +121,46 @@ def _hash(ctx, files, block_kb: int, seg: int, name_for_stdin=None, stdin_data=N
             dd = (16 if block_kb < 0 else block_kb) * KB
             for f in group:
                 digs += seg_digests(np.fromfile(f, dtype=np.uint8), f, dd)
-    return [g.sdbf(_digest=d) for d in digs]
+    return done()
+
+
+def _load_indexes(ctx, idx_dir: str):
+    """The --index-search list (sdhash-src/sdhash.cc:241-266): every regular
+    '*.idx' file of the directory in directory order, each with the name of
+    the SDBF set stored beside it (idx_dir + "/" + the file name without
+    '.idx'; sdbf_set(fname) names a set after the path only when the file
+    exists, and throws on a malformed one)."""
+    import sdhash_gb300 as g
+    out = []
+    if not os.path.isdir(idx_dir):
+        return out
+    with os.scandir(idx_dir) as it:
+        for e in it:
+            stem, ext = os.path.splitext(e.name)
+            if not (e.is_file() and ext == ".idx" and stem):
+                continue
+            index = ctx.load_index(os.path.join(idx_dir, e.name))
+            set_path = idx_dir + "/" + stem
+            name = ""
+            if os.path.isfile(set_path):
+                ctx.load_file(set_path).close()
+                name = set_path
+            out.append((index, name))
+    return out
+
+
+def _index_results(items, hits, set_names) -> str:
+    """sdbf_set::index_results (sdbf/sdbf_set.cc:161-167): per digest in set
+    order, per block, per index with more than 4 hits (_FP_THRESHOLD,
+    sdbf_defines.h:36): "<digest> [<block>] |<index set>|<hits>" (print_indexes,
+    sdbf/sdbf_core.cc:458-472)."""
+    lines = []
+    for it, h in zip(items, hits):
+        for b in range(h.shape[0]):
+            for i, nm in enumerate(set_names):
+                if h[b, i] > 4:
+                    lines.append(f"{it.name()} [{b}] |{nm}|{int(h[b, i])}\n")
+    return "".join(lines)
 
 
 def main(argv=None) -> int:
@@ -125,6 +179,8 @@ def main(argv=None) -> int:
     ap.add_argument("--hash-name", default=None, help="set name of hash on stdin")
     ap.add_argument("--fast", action="store_true", help="shrink sdbf filters for speedup")
     ap.add_argument("--validate", action="store_true", help="parse SDBF file to check if it is valid")
+    ap.add_argument("--index-search", default=None, metavar="DIR",
+                    help="search directory of reference indexes (block mode)")
     ap.add_argument("--version", action="store_true")
     ap.add_argument("files", nargs="*")
     a = ap.parse_args(argv)
@@ -184,9 +240,22 @@ def main(argv=None) -> int:
         return 0
     ctx = g.default_context()
     seg = a.segment_size * MB
+    indexes = None
+    if a.index_search is not None:
+        if block_kb == 0:
+            print("ERROR: Index searching only supported in block mode", file=sys.stderr)
+            return 0
+        if block_kb == -1:
+            block_kb = 16      # sdhash.cc:245-249
+        loaded = _load_indexes(ctx, a.index_search)
+        indexes = [x for x, _ in loaded]
+        set_names = [nm for _, nm in loaded]
+    hits = None
     if a.files == ["-"]:
         data = sys.stdin.buffer.read()
-        items = _hash(ctx, [], block_kb, seg, a.hash_name, data)
+        items = _hash(ctx, [], block_kb, seg, a.hash_name, data, indexes=indexes)
+        if indexes is not None:
+            items, hits = items
     else:
         inputs = a.files
         if a.target_list:
@@ -198,13 +267,24 @@ def main(argv=None) -> int:
         if not files:
             print(VERSION + "\n\nUsage: sdhash <options> <files>")
             return 0
-        items = _hash(ctx, files, block_kb, seg)
+        items = _hash(ctx, files, block_kb, seg, indexes=indexes)
+        if indexes is not None:
+            items, hits = items
     s = g.sdbf_set()
     s.set_separator(sep)
     for it in items:
         s.add(it)
     if a.gen_compare:
         emit(s.compare_all_quiet(a.threshold, 0, a.fast), ".compare")
+    elif indexes is not None:
+        # sdhash.cc:638-652: the hashes are not written; the results go to
+        # <output>.idx-result, or to stderr
+        text = _index_results(items, hits, set_names)
+        if a.output:
+            with open(a.output + ".idx-result", "w") as f:
+                f.write(text)
+        else:
+            sys.stderr.write(text)
     else:
         emit(s.to_string(), ".sdbf")
     return 0

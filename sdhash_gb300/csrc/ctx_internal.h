@@ -122,7 +122,25 @@ struct sdbfg_ctx {
     bool mat_graphs = true;
     std::vector<struct MatPlan*> plans;
     DevBuf d_match_counts, d_match_offs, d_matches, d_mphase;
+    // index search: per-slot probe words and counts of the group being
+    // digested (set around a block-mode batch), the device index table
+    uint32_t* probe_words = nullptr;
+    uint8_t* probe_counts = nullptr;
+    DevBuf d_probes, d_nprobes, d_hits, d_index_tab;
 };
+
+// A resident index filter (bloom_filter of an index file).
+struct sdbfg_index {
+    sdbfg_ctx* ctx = nullptr;
+    uint64_t bf_size = 0, elem_count = 0, bit_mask = 0;
+    uint32_t hash_count = 0;
+    std::string name;
+    DevBuf d_bits;
+};
+
+// Hits of every probe slot against every index (k_index_query).
+int index_query(sdbfg_ctx* c, const uint32_t* d_probes, const uint8_t* d_nprobes, uint64_t nslots,
+                const sdbfg_index* const* indexes, uint32_t nidx, uint8_t* d_hits, cudaStream_t st);
 
 struct sdbfg_set {
     sdbfg_ctx* ctx = nullptr;

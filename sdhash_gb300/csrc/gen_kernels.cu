@@ -990,6 +990,11 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
                         filt[idx >> 5] |= bit;
                     }
                     if (!added) continue;
+                    if (P.probes && (hashed & 3) == 0) {  // index search sample (sdbf_core.cc:168-175)
+                        uint32_t* pr = P.probes + (size_t)C.filter * kProbeWords + (hashed >> 2) * 5;
+#pragma unroll
+                        for (int z = 0; z < 5; z++) pr[z] = hsh[q][z];
+                    }
                     hashed++;
                     if (v == k) allowed--;
                 }
@@ -1001,6 +1006,7 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
         }
         if (threadIdx.x < 64) P.out_filters[(size_t)C.filter * 64 + threadIdx.x] = filt[threadIdx.x];
         if (threadIdx.x == 0) P.out_counts[C.filter] = (uint16_t)state[2];
+        if (threadIdx.x == 0 && P.nprobes) P.nprobes[C.filter] = (uint8_t)((state[2] + 3) >> 2);
         __syncthreads();
     }
 }

@@ -81,7 +81,16 @@ struct GenParams {
     uint32_t lead;               // speculative lead-in steps (<= kLead)
     unsigned long long* phase;   // optional phase cycle counters (kPhase*), null = off
     uint32_t* chunk_redo;        // per chunk: first tile whose link failed (stream)
+    // block mode with index search: SHA-1 words of every fourth counted
+    // feature of each block ([slot][kProbeWords]) and their number per slot;
+    // null = no search
+    uint32_t* probes;
+    uint8_t* nprobes;
 };
+
+// Index search samples counted features 0, 4, 8, ... of a block
+// (sdbf_core.cc:168-175): at most 192 / 4 = 48, five words each.
+constexpr uint32_t kProbeWords = 48 * 5;
 
 // Phase counters (cycles summed over CTAs / warps) when GenParams::phase is set.
 enum : int {

@@ -276,6 +276,8 @@ static int digest_group_device(sdbfg_ctx* c, const uint8_t* dev_base, const std:
         P.nchunks = (uint32_t)chunks.size();
         P.out_filters = dev_out;
         P.out_counts = dev_counts;
+        P.probes = c->probe_words;
+        P.nprobes = c->probe_counts;
         P.block_lmax = (lmax + 63) / 64 * 64;
         const uint32_t grid = (uint32_t)std::min<size_t>(chunks.size(), (size_t)c->sms * 2 * 8);
         TIMED_LAUNCH(c, "k_block_digest", launch_block(P, grid, st));
@@ -592,34 +594,13 @@ extern "C" int sdbfg_digest_batch_device(sdbfg_ctx* c, const uint8_t* dev_data, 
     return SDBFG_OK;
 }
 
-extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets,
-                                  const uint64_t* lens, uint32_t n, uint32_t dd, uint8_t* out_filters,
-                                  uint64_t out_cap, uint16_t* out_counts, sdbfg_digest_result* res) {
-    int rc = validate_batch(c, offsets, lens, n, dd, res);
-    if (rc) return rc;
-    if (n && !host_data) return SDBFG_ERR_ARG;
-    CUDA_TRY(c, cudaSetDevice(c->device));
+// Block-mode batch from host memory, launch group by launch group; with
+// indexes, also the index-search hits of every filter slot.
+static int digest_block_host(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets, const uint64_t* lens,
+                             uint32_t n, uint32_t dd, uint8_t* out_filters, uint16_t* out_counts,
+                             sdbfg_digest_result* res, const sdbfg_index* const* indexes, uint32_t nidx,
+                             uint8_t* out_hits) {
     cudaStream_t st = c->stream;
-    uint64_t total_slots = 0;
-    if (dd) {
-        total_slots = assign_block_slots(lens, n, dd, res);
-        if (total_slots > out_cap)
-            return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)total_slots);
-        if (total_slots && !out_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
-    }
-    if (!dd) {
-        uint64_t cap_needed = 0;
-        for (uint32_t i = 0; i < n; i++)
-            if (lens[i] >= kMinFile) cap_needed += stream_cap(lens[i]);
-        CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, cap_needed) * 256));
-        uint64_t total = 0;
-        rc = digest_stream_pipelined(c, host_data, nullptr, offsets, lens, n, c->d_out_filters.as<uint32_t>(),
-                                     std::min(cap_needed, out_cap), res, &total);
-        if (rc) return rc;
-        if (total) CUDA_TRY(c, cudaMemcpyAsync(out_filters, c->d_out_filters.p, total * 256, cudaMemcpyDeviceToHost, st));
-        CUDA_TRY(c, cudaStreamSynchronize(st));
-        return SDBFG_OK;
-    }
     cudaPointerAttributes attr{};
     const bool pinned = cudaPointerGetAttributes(&attr, host_data) == cudaSuccess &&
                         (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
@@ -648,40 +629,101 @@ extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const 
                 CUDA_TRY(c, cudaMemcpyAsync(d + off[k], host_data + offsets[i], lens[i], cudaMemcpyHostToDevice, st));
             }
         }
+        // block mode writes its slots directly; copy back this group's range
         uint64_t group_slots = 0, group_first_slot = 0;
-        if (dd) {
-            // block mode writes its slots directly; copy back this group's range
-            bool first = true;
-            for (uint32_t k = 0; k < g.count; k++) {
-                const uint32_t i = g.first + k;
-                if (lens[i] < kMinFile) continue;
-                if (first) {
-                    group_first_slot = res[i].filter_offset;
-                    first = false;
-                }
-                group_slots = res[i].filter_offset + res[i].bf_count - group_first_slot;
+        bool first = true;
+        for (uint32_t k = 0; k < g.count; k++) {
+            const uint32_t i = g.first + k;
+            if (lens[i] < kMinFile) continue;
+            if (first) {
+                group_first_slot = res[i].filter_offset;
+                first = false;
             }
-            CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, group_slots) * 256));
-            CUDA_TRY(c, c->d_out_counts.ensure(std::max<uint64_t>(1, group_slots) * 2));
-            // shift slots into the group-local output buffer
-            std::vector<uint64_t> saved(g.count);
-            for (uint32_t k = 0; k < g.count; k++) {
-                saved[k] = res[g.first + k].filter_offset;
-                res[g.first + k].filter_offset -= group_first_slot;
-            }
-            rc = digest_group_device(c, d, off, lens, g, dd, c->d_out_filters.as<uint32_t>(),
-                                     c->d_out_counts.as<uint16_t>(), res, &next, out_cap);
-            for (uint32_t k = 0; k < g.count; k++) res[g.first + k].filter_offset = saved[k];
+            group_slots = res[i].filter_offset + res[i].bf_count - group_first_slot;
+        }
+        CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, group_slots) * 256));
+        CUDA_TRY(c, c->d_out_counts.ensure(std::max<uint64_t>(1, group_slots) * 2));
+        if (nidx) {
+            CUDA_TRY(c, c->d_probes.ensure(std::max<uint64_t>(1, group_slots) * kProbeWords * 4));
+            CUDA_TRY(c, c->d_nprobes.ensure(std::max<uint64_t>(1, group_slots)));
+            CUDA_TRY(c, c->d_hits.ensure(std::max<uint64_t>(1, group_slots) * nidx));
+            c->probe_words = c->d_probes.as<uint32_t>();
+            c->probe_counts = c->d_nprobes.as<uint8_t>();
+        }
+        // shift slots into the group-local output buffer
+        std::vector<uint64_t> saved(g.count);
+        for (uint32_t k = 0; k < g.count; k++) {
+            saved[k] = res[g.first + k].filter_offset;
+            res[g.first + k].filter_offset -= group_first_slot;
+        }
+        int rc = digest_group_device(c, d, off, lens, g, dd, c->d_out_filters.as<uint32_t>(),
+                                     c->d_out_counts.as<uint16_t>(), res, &next, UINT64_MAX);
+        c->probe_words = nullptr;
+        c->probe_counts = nullptr;
+        for (uint32_t k = 0; k < g.count; k++) res[g.first + k].filter_offset = saved[k];
+        if (rc) return rc;
+        if (nidx && group_slots) {
+            rc = index_query(c, c->d_probes.as<uint32_t>(), c->d_nprobes.as<uint8_t>(), group_slots, indexes, nidx,
+                             c->d_hits.as<uint8_t>(), st);
             if (rc) return rc;
-            if (group_slots) {
-                CUDA_TRY(c, cudaMemcpyAsync(out_filters + group_first_slot * 256, c->d_out_filters.p,
-                                            group_slots * 256, cudaMemcpyDeviceToHost, st));
-                CUDA_TRY(c, cudaMemcpyAsync(out_counts + group_first_slot, c->d_out_counts.p, group_slots * 2,
-                                            cudaMemcpyDeviceToHost, st));
-            }
+            CUDA_TRY(c, cudaMemcpyAsync(out_hits + group_first_slot * nidx, c->d_hits.p, group_slots * nidx,
+                                        cudaMemcpyDeviceToHost, st));
+        }
+        if (group_slots) {
+            CUDA_TRY(c, cudaMemcpyAsync(out_filters + group_first_slot * 256, c->d_out_filters.p, group_slots * 256,
+                                        cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(c, cudaMemcpyAsync(out_counts + group_first_slot, c->d_out_counts.p, group_slots * 2,
+                                        cudaMemcpyDeviceToHost, st));
         }
         CUDA_TRY(c, cudaStreamSynchronize(st));
     }
     return SDBFG_OK;
+}
+
+extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets,
+                                  const uint64_t* lens, uint32_t n, uint32_t dd, uint8_t* out_filters,
+                                  uint64_t out_cap, uint16_t* out_counts, sdbfg_digest_result* res) {
+    int rc = validate_batch(c, offsets, lens, n, dd, res);
+    if (rc) return rc;
+    if (n && !host_data) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    if (!dd) {
+        uint64_t cap_needed = 0;
+        for (uint32_t i = 0; i < n; i++)
+            if (lens[i] >= kMinFile) cap_needed += stream_cap(lens[i]);
+        CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, cap_needed) * 256));
+        uint64_t total = 0;
+        rc = digest_stream_pipelined(c, host_data, nullptr, offsets, lens, n, c->d_out_filters.as<uint32_t>(),
+                                     std::min(cap_needed, out_cap), res, &total);
+        if (rc) return rc;
+        if (total) CUDA_TRY(c, cudaMemcpyAsync(out_filters, c->d_out_filters.p, total * 256, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(c, cudaStreamSynchronize(st));
+        return SDBFG_OK;
+    }
+    const uint64_t total_slots = assign_block_slots(lens, n, dd, res);
+    if (total_slots > out_cap)
+        return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)total_slots);
+    if (total_slots && !out_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
+    return digest_block_host(c, host_data, offsets, lens, n, dd, out_filters, out_counts, res, nullptr, 0, nullptr);
+}
+
+extern "C" int sdbfg_digest_batch_search(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets,
+                                         const uint64_t* lens, uint32_t n, uint32_t dd, uint8_t* out_filters,
+                                         uint64_t out_cap, uint16_t* out_counts, sdbfg_digest_result* res,
+                                         const sdbfg_index* const* indexes, uint32_t nidx, uint8_t* out_hits) {
+    if (!dd) return fail(c, SDBFG_ERR_ARG, "index search needs block mode");  // sdhash.cc:241-244
+    if (nidx && (!indexes || !out_hits)) return SDBFG_ERR_ARG;
+    for (uint32_t i = 0; i < nidx; i++)
+        if (!indexes[i] || indexes[i]->ctx != c) return fail(c, SDBFG_ERR_ARG, "index %u belongs to no/another context", i);
+    int rc = validate_batch(c, offsets, lens, n, dd, res);
+    if (rc) return rc;
+    if (n && !host_data) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    const uint64_t total_slots = assign_block_slots(lens, n, dd, res);
+    if (total_slots > out_cap)
+        return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)total_slots);
+    if (total_slots && !out_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
+    return digest_block_host(c, host_data, offsets, lens, n, dd, out_filters, out_counts, res, indexes, nidx, out_hits);
 }
 

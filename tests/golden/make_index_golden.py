@@ -1,0 +1,118 @@
+"""Generate the index-search fixtures (tests/golden/index/) from the REFERENCE
+sdhash.
+
+Builds two indexes as sdhash --index does (sdhash-src/sdhash_threads.cc:
+376-470; one group each): A from two stream-mode digests (the --index path
+of files below 16 MiB), B from one block-mode digest (the path of larger
+files).  Each is written as the reference writes it: the set as SDBF text
+(idx/A.sdbf) and the index file (idx/A.sdbf.idx, LZ4-compressed 64 MiB
+filter), stored here gzip-compressed.  Then runs the reference's index
+search (sdhash --index-search idx, sdhash.cc:231-266 and 638-652) on five
+seeded query inputs in 16 KiB block mode and records index_results(), and
+records the sha256 of each index filter as the reference decompresses it.
+
+Inputs are seeded synthetic mixture content (sdhash_gb300/synth.py), so the
+GPU tests regenerate them on any machine.
+
+Needs the reference tree (only in the build container):
+    python tests/golden/make_index_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import gzip
+import hashlib
+import json
+import os
+import shutil
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oracle import Reference, build_reference  # noqa: E402
+from sdhash_gb300 import synth  # noqa: E402
+
+OUT = os.path.join(HERE, "index")
+
+
+def index_inputs():
+    """(name, bytes) of the indexed files: group A (stream) and B (block)."""
+    a = [(f"a{i}.bin", synth.mixture_bytes(91, i, n).tobytes()) for i, n in enumerate((40_000, 56_000))]
+    b = [("b0.bin", synth.mixture_bytes(92, 0, 256 << 10).tobytes())]
+    return a, b
+
+
+def queries():
+    """(name, bytes) of the searched inputs."""
+    a, b = index_inputs()
+    return [("q0.bin", a[1][1][5_000:35_000]),
+            ("q1.bin", b[0][1][10_000:110_000]),
+            ("q2.bin", synth.random_bytes(93, 0, 50_000).tobytes()),
+            ("q3.bin", a[0][1][:20_000] + b[0][1][130_000:170_000]),
+            ("q4.bin", synth.random_bytes(93, 1, 700).tobytes())]
+
+
+def _arr(items):
+    names = (C.c_char_p * len(items))(*[n.encode() for n, _ in items])
+    bufs = (C.c_char_p * len(items))(*[d for _, d in items])
+    lens = (C.c_ulonglong * len(items))(*[len(d) for _, d in items])
+    return names, bufs, lens
+
+
+def main():
+    build_reference()
+    R = Reference()
+    L = R.L
+    L.ref_index_build.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_uint, C.c_char_p, C.c_char_p]
+    L.ref_index_search.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                   C.c_uint]
+    L.ref_index_search.restype = C.c_void_p
+    L.ref_index_bits.argtypes = [C.c_char_p, C.c_void_p, C.c_ulonglong]
+    L.ref_index_bits.restype = C.c_longlong
+    a, b = index_inputs()
+    cwd = os.getcwd()
+    tmp = tempfile.mkdtemp()
+    try:
+        os.chdir(tmp)
+        os.mkdir("idx")
+        for items, dd, stem in ((a, 0, "A"), (b, 16384, "B")):
+            names, bufs, lens = _arr(items)
+            rc = L.ref_index_build(names, bufs, lens, len(items), dd, f"idx/{stem}.sdbf".encode(),
+                                   f"idx/{stem}.sdbf.idx".encode())
+            assert rc == 0, rc
+        qs = queries()
+        names, bufs, lens = _arr(qs)
+        order = ["A", "B"]
+        idx = (C.c_char_p * 2)(*[f"idx/{s}.sdbf.idx".encode() for s in order])
+        sets = (C.c_char_p * 2)(*[f"idx/{s}.sdbf".encode() for s in order])
+        text = R._take(L.ref_index_search(idx, sets, 2, names, bufs, lens, len(qs), 16384))
+        rec = {"generator": "tests/golden/make_index_golden.py",
+               "reference": "sdhash 4.0 --index / --index-search through its library API",
+               "index_order": order, "dd_block_size": 16384, "results": text, "indexes": {}}
+        os.makedirs(OUT, exist_ok=True)
+        for s in order:
+            raw = open(f"idx/{s}.sdbf.idx", "rb").read()
+            buf = (C.c_ubyte * (64 << 20))()
+            size = L.ref_index_bits(f"idx/{s}.sdbf.idx".encode(), buf, 64 << 20)
+            assert size == 64 << 20, size
+            head = raw[:raw.index(b"\n")].decode()
+            rec["indexes"][s] = {"header": head, "filter_sha256": hashlib.sha256(bytes(buf)).hexdigest(),
+                                 "filter_popcount": int(sum(bin(x).count("1") for x in bytes(buf) if x))}
+            with gzip.open(os.path.join(OUT, f"{s}.sdbf.idx.gz"), "wb", compresslevel=9) as f:
+                f.write(raw)
+            shutil.copy(f"idx/{s}.sdbf", os.path.join(OUT, f"{s}.sdbf"))
+        with open(os.path.join(OUT, "index_search.json"), "w") as f:
+            json.dump(rec, f, indent=1)
+        print(text)
+        for s in order:
+            print(s, rec["indexes"][s]["header"], os.path.getsize(os.path.join(OUT, f"{s}.sdbf.idx.gz")))
+    finally:
+        os.chdir(cwd)
+        shutil.rmtree(tmp)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,93 @@
+"""Index search on the GPU (sdbfg_digest_batch_search, --index-search)
+against the reference: its index files and index_results() text for seeded
+queries (tests/golden/index/, made by tests/golden/make_index_golden.py)."""
+import gzip
+import json
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "index")
+
+
+def _fixture():
+    with open(os.path.join(GOLD, "index_search.json")) as f:
+        return json.load(f)
+
+
+def _queries():
+    # the same seeded inputs as the fixture generator
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mkidx", os.path.join(os.path.dirname(__file__), "golden",
+                                                                        "make_index_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m.queries()
+
+
+@pytest.fixture()
+def idx_dir(tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    os.mkdir("idx")
+    for s in ("A", "B"):
+        with gzip.open(os.path.join(GOLD, f"{s}.sdbf.idx.gz")) as f, open(f"idx/{s}.sdbf.idx", "wb") as o:
+            o.write(f.read())
+        shutil.copy(os.path.join(GOLD, f"{s}.sdbf"), f"idx/{s}.sdbf")
+    return tmp_path
+
+
+def test_search_matches_reference(ctx, idx_dir):
+    from sdhash_gb300 import cli
+    rec = _fixture()
+    indexes = [ctx.load_index(f"idx/{s}.sdbf.idx") for s in rec["index_order"]]
+    for s, x in zip(rec["index_order"], indexes):
+        assert x.name == f"idx/{s}.sdbf" and x.hash_count == 5 and x.bf_size == 64 << 20
+    qs = _queries()
+    digs, hits = ctx.digest_search([d for _, d in qs], [n for n, _ in qs], rec["dd_block_size"], indexes)
+    import sdhash_gb300 as g
+    items = [g.sdbf(_digest=d) for d in digs if d is not None]
+    rows = [h for h in hits if h is not None]
+    text = cli._index_results(items, rows, [f"idx/{s}.sdbf" for s in rec["index_order"]])
+    assert text == rec["results"]
+    # the digests themselves are the plain block-mode digests
+    plain = ctx.digest_buffers([d for _, d in qs], [n for n, _ in qs], rec["dd_block_size"])
+    for a, b in zip(digs, plain):
+        assert (a is None) == (b is None)
+        if a is not None:
+            assert a.to_string() == b.to_string()
+
+
+def test_cli_index_search(ctx, idx_dir, capsys):
+    from sdhash_gb300 import cli
+    rec = _fixture()
+    for n, d in _queries():
+        with open(n, "wb") as f:
+            f.write(d)
+    names = [n for n, _ in _queries()]
+    assert cli.main(["--index-search", "idx", "-o", "res"] + names) == 0
+    got = open("res.idx-result").read()
+    # lines within a block follow the directory's order of the index files
+    assert sorted(got.splitlines()) == sorted(rec["results"].splitlines())
+    assert cli.main(["--index-search", "idx"] + names) == 0
+    assert sorted(capsys.readouterr().err.splitlines()) == sorted(rec["results"].splitlines())
+    assert cli.main(["--index-search", "idx", "-b", "0"] + names) == 0
+    assert "only supported in block mode" in capsys.readouterr().err
+
+
+def test_empty_index_has_no_hits(ctx):
+    qs = _queries()
+    x = ctx.index_from_bits(np.zeros(1 << 20, dtype=np.uint8))
+    full = ctx.index_from_bits(np.full(1 << 10, 0xFF, dtype=np.uint8))
+    digs, hits = ctx.digest_search([d for _, d in qs], [n for n, _ in qs], 16384, [x, full])
+    for d, h in zip(digs, hits):
+        if d is None:
+            continue
+        assert h.shape == (d.bf_count, 2)
+        assert (h[:, 0] == 0).all()
+        # every bit set: every sampled feature hits (counted features 0, 4, 8, ...)
+        want = (d.elem_counts.astype(np.int64) + 3) // 4
+        assert np.array_equal(h[:, 1], want)
