@@ -13,7 +13,9 @@ One step = digest every file of the rank's shard once.
            (sdbfg_digest_batch_device), CUDA events on the launch stream.
   e2e   -- through the public C ABI with HOST buffers (sdbfg_digest_batch):
            host->device copy of the inputs from pinned memory, generation,
-           device->host copy of the packed filters, every step.
+           device->host copy of the packed filters and per-file results into
+           the caller's host buffers, every step (python_api_value: the same
+           batch once through Context.digest_packed, Digest objects built).
 
 --impl reference times the reference's CPU implementation of the path (the
 oracle port of sdhash's generation, all host threads) on the same workload.
@@ -60,15 +62,18 @@ def parse():
     ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
     ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve", "load"],
+    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve", "load", "index"],
                     help="stream: bulk digest generation (headline); allpairs: batched uneven all-pairs compare; "
                          "image: block-mode disk image + query fragments compared against it; serve: continuous-batching "
-                         "server under Poisson load; load: bulk SDBF text load into a resident set")
+                         "server under Poisson load; load: bulk SDBF text load into a resident set; index: "
+                         "block-mode index search")
     ap.add_argument("--image-gib", type=int, default=16, help="image: disk image size (GiB, multiple of 128 MiB)")
     ap.add_argument("--queries", type=int, default=100000, help="image: query fragments")
     ap.add_argument("--ref-filters", type=int, default=244 * 8192, help="serve: block filters in the reference set")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: offered Poisson load (queries/s)")
     ap.add_argument("--serve-queries", type=int, default=1500, help="serve: queries per load run")
+    ap.add_argument("--search-gib", type=float, default=4.0, help="index: input size (GiB, 128 MiB segments)")
+    ap.add_argument("--indexes", type=int, default=8, help="index: 64 MiB index filters searched")
     ap.add_argument("--digests", type=int, default=20000, help="allpairs: digests in the set")
     ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
     ap.add_argument("--plain-pairs", type=int, default=400, help="allpairs: pairs timed one call each")
@@ -786,6 +791,128 @@ def main_serve(args):
     return 0
 
 
+IX_METRIC = "index-searched input GB/s (block mode)"
+
+
+def main_index(args):
+    """sdhash --index-search on the GPU (sdbfg_digest_batch_search): an image
+    of 128 MiB segments (mixture content) digested in 16 KiB block mode with
+    every fourth counted feature of each block looked up in `--indexes`
+    64 MiB index filters.  The index filters are seeded random bits at
+    12.5 % density, near the ~10 % of a 64 MiB index built from the 640 MB
+    group sdhash --index writes (about 17 features per KiB x 5 bits).  value: device time of the two kernels (block digest
+    with feature sampling + k_index_query, CUDA events); e2e: the whole call
+    from pinned host memory (copies, digests and hit counts back);
+    cpu_baseline: the oracle's restatement of the same search on a sample,
+    all host threads."""
+    import ctypes as C
+    import torch
+    import sdhash_gb300 as g
+    from sdhash_gb300 import DigestResult, lib, synth, _ptr
+    torch.cuda.set_device(0)
+    ctx = g.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    dd = 16384
+    nseg = max(1, int(args.search_gib * 1024) // 128)
+    sizes = np.full(nseg, SEG, dtype=np.uint64)
+    offs, total = synth.packed_layout(sizes)
+    pinned = torch.empty(max(16, total), dtype=torch.uint8, pin_memory=True)
+    data = pinned.numpy()
+    synth.fill_many(args.seed + 5000, "mixture", sizes, out=data)
+    bits = []
+    for x in range(args.indexes):  # AND of three random bit strings: 12.5 % of the bits set
+        r = [synth.random_bytes(args.seed + 5001, 3 * x + j, 64 << 20) for j in range(3)]
+        bits.append(r[0] & r[1] & r[2])
+    idx = [ctx.index_from_bits(b) for b in bits]
+    n, nidx = nseg, len(idx)
+    lens = np.ascontiguousarray(sizes, dtype=np.uint64)
+    offs = np.ascontiguousarray(offs, dtype=np.uint64)
+    cap = ctx.capacity(lens, dd)
+    out_f = torch.empty(cap * 256, dtype=torch.uint8, pin_memory=True).numpy()
+    out_c = np.zeros(cap, dtype=np.uint16)
+    hits = np.zeros(cap * nidx, dtype=np.uint8)
+    arr = (C.c_void_p * nidx)(*[x.h for x in idx])
+    res = (DigestResult * n)()
+
+    def call(with_index=True):
+        if with_index:
+            rc = lib().sdbfg_digest_batch_search(ctx.h, data.ctypes.data, _ptr(offs), _ptr(lens), n, dd,
+                                                 out_f.ctypes.data, cap, out_c.ctypes.data, res, arr, nidx,
+                                                 hits.ctypes.data)
+        else:
+            rc = lib().sdbfg_digest_batch(ctx.h, data.ctypes.data, _ptr(offs), _ptr(lens), n, dd, out_f.ctypes.data,
+                                          cap, out_c.ctypes.data, res)
+        ctx._check(rc)
+
+    for _ in range(max(3, args.warmup)):
+        call()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        call()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    clocks.stop()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        call(False)
+    wall_plain = (time.perf_counter() - t0) / args.steps
+    ctx.profile(True)
+    l0 = ctx.launch_count
+    for _ in range(args.steps):
+        call()
+    kd_ms, kd_n = ctx.kernel_time("k_block_digest")
+    kq_ms, kq_n = ctx.kernel_time("k_index_query")
+    launches = (ctx.launch_count - l0) // args.steps
+    ctx.profile(False)
+    dev_ms = (kd_ms + kq_ms) / args.steps
+    nprobe_hits = int((hits > 4).sum())
+    # parity and CPU baseline: the oracle on a sample of segments
+    from oracle import Oracle
+    O = Oracle()
+    ncpu = os.cpu_count() or 1
+    ks = list(range(0, n, max(1, n // 4)))[:4]
+    sample = [data[int(offs[k]):int(offs[k]) + int(lens[k])] for k in ks]
+    t1 = time.perf_counter()
+    want = O.index_search(sample, dd, bits, ncpu)
+    t_cpu = time.perf_counter() - t1
+    for k, w in zip(ks, want):
+        o = int(res[k].filter_offset)
+        got = hits[o * nidx:(o + int(res[k].bf_count)) * nidx].reshape(-1, nidx)
+        assert np.array_equal(got, w), "index-search hits differ from the oracle"
+    hbm, src = peaks()
+    alg = total  # each input byte read once by the block kernel
+    line = {"metric": IX_METRIC, "value": total / (dev_ms / 1e3) / 1e9, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": dev_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": "block-mode index search (sdhash --index-search)", "input_bytes": int(total),
+                       "segments": n, "block": dd, "indexes": nidx, "index_bytes": 64 << 20,
+                       "index_content": "seeded random bits at 12.5% density", "blocks": int(cap),
+                       "l2": "inputs and indexes larger than L2 (no flush needed)"},
+            "gpu_launches": int(launches), "clocks": clocks.summary(),
+            "kernel_ms_per_step": {"k_block_digest": kd_ms / args.steps, "k_index_query": kq_ms / args.steps},
+            "lookups_per_step": int(cap) * 48 * nidx,
+            "blocks_with_hits_gt4": nprobe_hits,
+            "roofline": {"bound": "hbm", "kernel": "k_block_digest", "achieved": alg / (kd_ms / args.steps / 1e3) / 1e9,
+                         "peak": hbm, "unit": "GB/s", "frac": alg / (kd_ms / args.steps / 1e3) / 1e9 / hbm,
+                         "traffic": None,
+                         "peak_source": f"{src} hbm_gbs (MEASURED_PEAKS.json)", "algorithmic_bytes_per_step": alg},
+            "plain_block_digest_e2e": {"value": total / wall_plain / 1e9, "unit": "GB/s",
+                                       "path": "sdbfg_digest_batch, same input, no index"},
+            "e2e": {"value": total / wall / 1e9, "unit": "GB/s", "h2d_bytes_per_step": int(total),
+                    "d2h_bytes_per_step": int(cap) * (256 + 2 + nidx), "ms_per_step": wall * 1e3,
+                    "path": "sdbfg_digest_batch_search from pinned host memory"},
+            "cpu_baseline": {"value": sum(int(lens[k]) for k in ks) / t_cpu / 1e9, "unit": "GB/s", "cores": ncpu,
+                             "kind": "port", "sample": f"{len(ks)} of {n} segments searched by the oracle",
+                             "seconds": round(t_cpu, 3)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 LD_METRIC = "SDBF text loaded GB/s"
 
 
@@ -878,6 +1005,8 @@ def main():
     args = parse()
     if args.workload == "load":
         return main_load(args)
+    if args.workload == "index":
+        return main_index(args)
     if args.workload == "serve":
         return main_serve(args)
     if args.workload == "image":
@@ -946,21 +1075,41 @@ def main():
     value = bytes_all / (ms_per_step / 1e3) / 1e9
     out_filters = sum(int(r.bf_count) for r in res[: len(sizes)]) if len(sizes) else 0
 
-    # e2e through the host-buffer entry point
+    # e2e through the C ABI's host-buffer entry point (sdbfg_digest_batch):
+    # the caller's pinned input in, the packed filters and per-file results
+    # out into the caller's host buffers, every step
     e2e = None
     if not args.no_e2e:
-        ctx.digest_packed(data, offs, sizes, 0)  # warm host staging
+        import ctypes as C
+        from sdhash_gb300 import DigestResult, lib, _ptr, _u64
+        o64, l64 = _u64(offs), _u64(sizes)
+        nf = len(sizes)
+        cap_f = ctx.capacity(l64, 0)
+        out_host = torch.empty(max(1, cap_f) * 256, dtype=torch.uint8, pin_memory=True).numpy()
+        res_c = (DigestResult * max(1, nf))()
+
+        def abi_call():
+            ctx._check(lib().sdbfg_digest_batch(ctx.h, data.ctypes.data, _ptr(o64), _ptr(l64), nf, 0,
+                                                out_host.ctypes.data, cap_f, None, res_c))
+
+        abi_call()  # warm host staging
         barrier(world)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            ds = ctx.digest_packed(data, offs, sizes, 0)
+            abi_call()
         torch.cuda.synchronize()
         e2e_s = allmax(world, (time.perf_counter() - t0) / args.steps)
-        d2h = sum(d.bf_count for d in ds if d is not None) * 256 + 24 * len(sizes)
-        e2e = {"value": bytes_all / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(total_bytes),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+        d2h = sum(int(res_c[i].bf_count) for i in range(nf) if res_c[i].status == 0) * 256 + C.sizeof(res_c)
+        # the Python object API on the same batch, once (Digest objects built on the host)
+        t1 = time.perf_counter()
+        ds = ctx.digest_packed(data, offs, sizes, 0)
+        py_s = allmax(world, time.perf_counter() - t1)
         del ds
+        e2e = {"value": bytes_all / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(total_bytes),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+               "path": "C ABI sdbfg_digest_batch: pinned host input -> packed filters + results in host buffers",
+               "python_api_value": bytes_all / py_s / 1e9}
 
     peak, peak_kind = peaks()
     ngroups = max(1, tiles_n)

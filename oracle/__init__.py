@@ -127,6 +127,9 @@ class Oracle:
                                       C.c_uint64, i32p, C.c_int]
         L.orc_digest_many.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.POINTER(C.c_char_p),
                                       C.c_uint32, C.c_uint32, C.c_int, C.POINTER(_Digest), C.POINTER(C.c_int)]
+        L.orc_index_search_many.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_uint32, C.c_uint32,
+                                            C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                            C.c_uint32, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int)]
         L.orc_b64_encode.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p]
         L.orc_b64_encode.restype = C.c_size_t
 
@@ -228,6 +231,41 @@ class Oracle:
                                pj.ctypes.data_as(C.POINTER(C.c_uint32)), len(pi),
                                out.ctypes.data_as(C.POINTER(C.c_int32)), nthreads)
         return out[: len(pi)]
+
+    def index_search(self, bufs, dd_block_size: int, index_bits, nthreads: int = 0, hash_count: int = 5):
+        """Index search of block-mode hashing (gen_block_hash with an index
+        list): per input, a (bf_count, nidx) uint8 array of sampled features
+        found in each index (None for inputs below 512 bytes).  index_bits:
+        uint8 arrays, power-of-two sizes (mask = 8 * size - 1)."""
+        import numpy as np
+        n, nidx = len(bufs), len(index_bits)
+        ptrs = (C.c_void_p * max(1, n))()
+        lens = (C.c_uint64 * max(1, n))()
+        keep = []
+        for i, b in enumerate(bufs):
+            arr = np.ascontiguousarray(np.frombuffer(bytes(b), dtype=np.uint8) if isinstance(b, (bytes, bytearray))
+                                       else b, dtype=np.uint8)
+            keep.append(arr)
+            ptrs[i] = arr.ctypes.data
+            lens[i] = arr.size
+        bits = (C.c_void_p * max(1, nidx))(*[np.ascontiguousarray(x, dtype=np.uint8).ctypes.data for x in index_bits])
+        masks = (C.c_uint32 * max(1, nidx))(*[min(0xFFFFFFFF, 8 * len(x) - 1) for x in index_bits])
+        hcs = (C.c_uint32 * max(1, nidx))(*([hash_count] * nidx))
+        rows = []
+        for i in range(n):
+            nb = int(lens[i]) // dd_block_size + (1 if int(lens[i]) % dd_block_size >= 512 else 0)
+            rows.append(np.zeros((max(1, nb), max(1, nidx)), dtype=np.uint8))
+        hp = (C.c_void_p * max(1, n))(*[r.ctypes.data for r in rows])
+        status = (C.c_int * max(1, n))()
+        self.L.orc_index_search_many(ptrs, lens, n, dd_block_size, bits, masks, hcs, nidx, nthreads, hp, status)
+        out = []
+        for i in range(n):
+            if status[i] != 0:
+                out.append(None)
+            else:
+                nb = int(lens[i]) // dd_block_size + (1 if int(lens[i]) % dd_block_size >= 512 else 0)
+                out.append(rows[i][:nb, :nidx])
+        return out
 
     def digest_many(self, bufs, dd_block_size: int = 0, nthreads: int = 0, names=None):
         """Digest a list of bytes-like buffers on nthreads threads (file-parallel)."""

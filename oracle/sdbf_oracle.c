@@ -283,15 +283,36 @@ int orc_digest_stream(const char *name, const uint8_t *x, uint64_t len, orc_dige
 }
 
 /* ------------------------------------------------------------ block mode */
+/* The index list of an index search (index_info::setlist, sdbf/index_info.h). */
+typedef struct {
+    const uint8_t *const *bits;
+    const uint32_t *masks;
+    const uint32_t *hash_counts;
+    uint32_t n;
+} orc_index_list;
+
 static void block_hash(const uint8_t *data, uint64_t n, const uint16_t *scores, uint32_t k,
-                       int32_t allowed, uint8_t *bf, uint16_t *count) {
-    /* gen_block_hash, sdbf_core.cc:141-191 (no index, so only the insert) */
+                       int32_t allowed, uint8_t *bf, uint16_t *count, const orc_index_list *idx,
+                       uint8_t *hits) {
+    /* gen_block_hash, sdbf_core.cc:141-191; with an index list, counted
+     * features 0, 4, 8, ... are looked up in every index (check_indexes,
+     * :482-493; bloom_filter::query_sha1 = all hash bits set) */
     uint32_t hashed = 0;
     for (uint64_t i = 0; i < n - ORC_WIN && hashed < ORC_MAX_ELEM_DD; i++) {
         if (scores[i] > k || (scores[i] == k && allowed > 0)) {
             uint32_t h[5];
             sha1_words(data + i, h);
             if (bf_insert5(bf, h) == 0) continue;
+            if (idx && hashed % 4 == 0) {
+                for (uint32_t x = 0; x < idx->n; x++) {
+                    uint32_t all = 1;
+                    for (uint32_t z = 0; z < idx->hash_counts[x] && all; z++) {
+                        const uint32_t pos = h[z] & idx->masks[x];
+                        all = (idx->bits[x][pos >> 3] >> (pos & 7)) & 1u;
+                    }
+                    hits[x] += (uint8_t)all;
+                }
+            }
             hashed++;
             if (scores[i] == k) allowed--;
         }
@@ -299,8 +320,23 @@ static void block_hash(const uint8_t *data, uint64_t n, const uint16_t *scores, 
     *count = (uint16_t)hashed;
 }
 
+static int digest_block_idx(const char *name, const uint8_t *x, uint64_t len, uint32_t B, orc_digest *d,
+                            const orc_index_list *idx, uint8_t *hits);
+
 int orc_digest_block(const char *name, const uint8_t *x, uint64_t len, uint32_t B,
                      orc_digest *d) {
+    return digest_block_idx(name, x, len, B, d, NULL, NULL);
+}
+
+int orc_index_search_block(const char *name, const uint8_t *x, uint64_t len, uint32_t B,
+                           const uint8_t *const *bits, const uint32_t *masks, const uint32_t *hash_counts,
+                           uint32_t nidx, orc_digest *d, uint8_t *hits) {
+    const orc_index_list idx = {bits, masks, hash_counts, nidx};
+    return digest_block_idx(name, x, len, B, d, &idx, hits);
+}
+
+static int digest_block_idx(const char *name, const uint8_t *x, uint64_t len, uint32_t B, orc_digest *d,
+                            const orc_index_list *idx, uint8_t *hits) {
     memset(d, 0, sizeof *d);
     if (len < ORC_MIN_FILE) return -3;
     d->name = dup_name(name);
@@ -325,14 +361,14 @@ int orc_digest_block(const char *name, const uint8_t *x, uint64_t len, uint32_t 
             sum += (uint32_t)histo[k];
         }
         block_hash(x + b * B, B, scores, k, (int32_t)(ORC_MAX_ELEM_DD - sum),
-                   d->filters + 256 * b, &d->elem_counts[b]);
+                   d->filters + 256 * b, &d->elem_counts[b], idx, idx ? hits + b * idx->n : NULL);
     }
     if (rem >= ORC_MIN_FILE) {
         /* tail block, sdbf_core.cc:309-319: threshold 16, allowed 192 */
         orc_ranks(x + qt * B, rem, ranks);
         orc_scores(ranks, rem, scores, NULL);
         block_hash(x + qt * B, rem, scores, ORC_THRESHOLD, ORC_MAX_ELEM_DD,
-                   d->filters + 256 * qt, &d->elem_counts[qt]);
+                   d->filters + 256 * qt, &d->elem_counts[qt], idx, idx ? hits + qt * idx->n : NULL);
     }
     free(ranks);
     free(scores);
@@ -738,6 +774,42 @@ static void *digest_worker(void *arg) {
                              : orc_digest_stream(nm, t->bufs[i], t->lens[i], &t->outs[i]);
     }
     return NULL;
+}
+
+typedef struct {
+    int id, nt;
+    const uint8_t *const *bufs;
+    const uint64_t *lens;
+    uint32_t n, dd;
+    orc_index_list idx;
+    uint8_t *const *hits;
+    int *status;
+} search_task;
+
+static void *search_worker(void *arg) {
+    search_task *t = (search_task *)arg;
+    for (uint32_t i = (uint32_t)t->id; i < t->n; i += (uint32_t)t->nt) {
+        orc_digest d;
+        t->status[i] = digest_block_idx("", t->bufs[i], t->lens[i], t->dd, &d, &t->idx, t->hits[i]);
+        if (t->status[i] == 0) orc_digest_free(&d);
+    }
+    return NULL;
+}
+
+void orc_index_search_many(const uint8_t *const *bufs, const uint64_t *lens, uint32_t n, uint32_t dd,
+                           const uint8_t *const *bits, const uint32_t *masks, const uint32_t *hash_counts,
+                           uint32_t nidx, int nthreads, uint8_t *const *hits, int *status) {
+    int nt = resolve_threads(nthreads);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nt);
+    search_task *ts = (search_task *)malloc(sizeof(search_task) * (size_t)nt);
+    for (int i = 0; i < nt; i++) {
+        search_task d = {i, nt, bufs, lens, n, dd, {bits, masks, hash_counts, nidx}, hits, status};
+        ts[i] = d;
+        pthread_create(&th[i], NULL, search_worker, &ts[i]);
+    }
+    for (int i = 0; i < nt; i++) pthread_join(th[i], NULL);
+    free(th);
+    free(ts);
 }
 
 void orc_digest_many(const uint8_t *const *bufs, const uint64_t *lens, const char *const *names, uint32_t n,

@@ -98,6 +98,17 @@ void orc_score_pairs(const orc_digest *set, const uint32_t *pi, const uint32_t *
 
 /* Digest many buffers on nthreads host threads (file-parallel, as
  * sdhash-src/sdhash_threads.cc:152-186 assigns files round-robin). */
+/* Block-mode digest with an index search (gen_block_hash with an index list,
+ * sdbf/sdbf_core.cc:141-191): hits[b * nidx + x] = sampled features (counted
+ * features 0, 4, 8, ...) of block b that index x holds.  hits must hold
+ * bf_count * nidx zeroed bytes.  orc_index_search_many runs it over n inputs
+ * on nthreads threads (hits[i] per input, digests discarded). */
+int orc_index_search_block(const char *name, const uint8_t *x, uint64_t len, uint32_t B,
+                           const uint8_t *const *bits, const uint32_t *masks, const uint32_t *hash_counts,
+                           uint32_t nidx, orc_digest *d, uint8_t *hits);
+void orc_index_search_many(const uint8_t *const *bufs, const uint64_t *lens, uint32_t n, uint32_t dd,
+                           const uint8_t *const *bits, const uint32_t *masks, const uint32_t *hash_counts,
+                           uint32_t nidx, int nthreads, uint8_t *const *hits, int *status);
 void orc_digest_many(const uint8_t *const *bufs, const uint64_t *lens, const char *const *names, uint32_t n,
                      uint32_t dd_block_size, int nthreads, orc_digest *outs, int *status);
 

@@ -91,3 +91,21 @@ def test_empty_index_has_no_hits(ctx):
         # every bit set: every sampled feature hits (counted features 0, 4, 8, ...)
         want = (d.elem_counts.astype(np.int64) + 3) // 4
         assert np.array_equal(h[:, 1], want)
+
+
+def test_hits_match_oracle_dense_indexes(ctx, oracle):
+    """Every hit count, for indexes dense enough that most blocks hit, on
+    ragged inputs (tails, sub-block inputs, a too-small input)."""
+    from sdhash_gb300 import synth
+    rng = np.random.default_rng(5)
+    bits = [np.packbits(rng.random(8 << 20) < d).astype(np.uint8) for d in (0.5, 0.8, 0.97)]
+    sizes = [int(s) for s in synth.log_uniform_sizes(95, 40, 400, 3 << 20)]
+    bufs = [synth.mixture_bytes(95, i, s).tobytes() for i, s in enumerate(sizes)]
+    idx = [ctx.index_from_bits(b) for b in bits]
+    digs, hits = ctx.digest_search(bufs, [f"x{i}" for i in range(len(bufs))], 16384, idx)
+    want = oracle.index_search(bufs, 16384, bits)
+    for d, h, w in zip(digs, hits, want):
+        assert (d is None) == (w is None)
+        if d is not None:
+            assert np.array_equal(h, w)
+    assert sum(int((h > 4).sum()) for h in hits if h is not None) > 100

@@ -56,3 +56,33 @@ def test_lz4_decode_rejects_malformed(native):
     assert _decode(native, b"\x24ab\x05\x00\x10z", 11)[0] < 0   # offset before the output start
     assert _decode(native, b"\x50hel", 5)[0] < 0                # truncated literals
     assert _decode(native, b"\x50hello", 4)[0] < 0              # output too small
+
+
+def test_oracle_index_search_matches_reference(native, oracle):
+    """The oracle's restatement of the index search reproduces the
+    reference's result text on the fixture's indexes and queries."""
+    import importlib.util
+    rec = _fixture()
+    bits = []
+    for s in rec["index_order"]:
+        raw = gzip.open(os.path.join(GOLD, f"{s}.sdbf.idx.gz")).read()
+        nl = raw.index(b"\n")
+        f = raw[:nl].decode().split(":")
+        r, out = _decode(native, raw[nl + 1:nl + 1 + int(f[5])], int(f[1]))
+        assert r == int(f[5])
+        bits.append(out)
+    spec = importlib.util.spec_from_file_location("mkidx", os.path.join(os.path.dirname(GOLD),
+                                                                        "make_index_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    qs = m.queries()
+    hits = oracle.index_search([d for _, d in qs], rec["dd_block_size"], bits)
+    lines = []
+    for (n, _), h in zip(qs, hits):
+        if h is None:
+            continue
+        for b in range(h.shape[0]):
+            for i, s in enumerate(rec["index_order"]):
+                if h[b, i] > 4:
+                    lines.append(f"{n} [{b}] |idx/{s}.sdbf|{int(h[b, i])}\n")
+    assert "".join(lines) == rec["results"]
