@@ -60,7 +60,10 @@ uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx *ctx);
  * cycles per phase; the names "k_stream_tiles.{load,ranks,fres,walk,link,
  * compact,sha1}" and "k_stream_commit.{wait,busy,max_file}" report those
  * cycles in *total_ms (and the tile count in *launches); ".count",
- * ".groups", ".loops" report counts.
+ * ".groups", ".loops" report counts.  The tensor-core comparison kernel
+ * reports "k_matrix_tc.{compose,fill,fetch_wait,stage_wait,widen,issue,
+ * producer_step,acc_wait,score,mark,walk,fold,consumer_step,step_barrier,
+ * tmem_ld}" in SM cycles and ".tiles" as a count.
  * Instrumentation without a counterpart in the reference. */
 int sdbfg_ctx_profile(sdbfg_ctx *ctx, int enable);
 int sdbfg_ctx_kernel_time(sdbfg_ctx *ctx, const char *kernel, double *total_ms, uint64_t *launches);

@@ -108,7 +108,8 @@ struct MatParams {
 // phase counters of the tensor-core kernel (one producer and one consumer thread per CTA)
 enum : int {
     kTcPhCompose = 0, kTcPhFill, kTcPhFetchWait, kTcPhStageWait, kTcPhWiden, kTcPhIssue, kTcPhProdStep,
-    kTcPhAccWait, kTcPhScore, kTcPhFold, kTcPhConsStep, kTcPhStepBarrier, kTcPhTiles, kTcPhLd, kTcPhCount
+    kTcPhAccWait, kTcPhScore, kTcPhFold, kTcPhConsStep, kTcPhStepBarrier, kTcPhTiles, kTcPhLd, kTcPhMark,
+    kTcPhWalk, kTcPhCount
 };
 
 // Kernel variants (rows per CTA x target filters per tile), chosen by the

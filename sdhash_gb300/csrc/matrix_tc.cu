@@ -14,8 +14,11 @@
 // score it exactly as the CUDA-core kernel does (compare_kernels.cu
 // k_matrix): a pair can score above 0 only if its full count exceeds the
 // cut, and for those rare pairs the reference's staged exits
-// (bf_utils.cc:114-206) are rechecked from the filters in memory.  Maxima of
-// completed targets collect in a 32-column ring and are summed in filter
+// (bf_utils.cc:114-206) are rechecked from the filters in memory.  Each
+// 32-column slice is scored in two passes: a branch-free pass marks the
+// row's counted columns and those above the cut, then the slice's segments
+// are walked in column order, re-checking only the marked columns.  Maxima
+// of completed targets collect in a ring of eight and are summed in filter
 // order as it fills.  Work units, group units, running sums and split pairs
 // are those of k_matrix.
 //
@@ -157,28 +160,16 @@ struct RowHead {
 // Returns (num << 32) | den of the pair's score (0 / 1 when it scores 0).
 __device__ __forceinline__ uint64_t candidate_fraction(const RowHead& aw, const uint4* tw, uint32_t cnt,
                                                       uint32_t cut, bool fast, uint32_t max_est) {
-    uint32_t c = 0;
-    bool exit = false;
+    // all eight loads first, then the three stage counts (an exit at any
+    // stage is an exit: the stages only end the count early)
+    uint32_t p[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
         const uint4 y = tw[q];
-        c += __popc(aw.w[q].x & y.x) + __popc(aw.w[q].y & y.y) + __popc(aw.w[q].z & y.z) + __popc(aw.w[q].w & y.w);
-        if (q == 1) {
-            if (fast) {
-                exit = 2 * c + 48 < cut;
-                break;
-            }
-            if (8 * c + 48 < cut) {
-                exit = true;
-                break;
-            }
-        }
-        if (q == 3 && 4 * c + 48 < cut) {
-            exit = true;
-            break;
-        }
-        if (q == 7) exit = 2 * c + 48 < cut;
+        p[q] = __popc(aw.w[q].x & y.x) + __popc(aw.w[q].y & y.y) + __popc(aw.w[q].z & y.z) + __popc(aw.w[q].w & y.w);
     }
+    const uint32_t c1 = p[0] + p[1], c2 = c1 + p[2] + p[3], c3 = c2 + p[4] + p[5] + p[6] + p[7];
+    const bool exit = fast ? 2 * c1 + 48 < cut : (8 * c1 + 48 < cut || 4 * c2 + 48 < cut || 2 * c3 + 48 < cut);
     if (exit || cnt <= cut) return 1;
     return ((uint64_t)(cnt - cut) << 32) | (uint32_t)(max_est - cut);
 }
@@ -567,32 +558,57 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             for (int q = 0; q < 32; q++) S.cstage[q][tid] = (uint16_t)__uint_as_float(v[q]);
                             if (tid == 0) TC_ADD(kTcPhLd, t_ld);
                             const uint32_t lim = min(32u, nt - c0);
-                            const uint32_t lm = T.lastmask[c0 >> 5];
-                            // columns in order; the loads of four columns are issued together
-                            // (all columns' counts and cuts first, then the rare paths)
-#pragma unroll 4
-                            for (uint32_t q = 0; q < lim; q++) {
-                                const uint32_t j = c0 + q;
-                                const uint32_t tm = T.tmeta[j];
-                                const uint32_t s2 = tm & 0xFFFFu;
-                                const uint32_t sum = s1 + s2;
-                                const uint32_t cut = !fastA
-                                    ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
-                                    : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
-                                const uint32_t cnt = S.cstage[q][tid];
-                                if (active && s2 >= (uint32_t)kMinElem) {
-                                    counted = true;  // a counted target filter scores at least 0
-                                    if (cnt > cut) {
-                                        const uint64_t fr =
-                                            candidate_fraction(aw, T.tw[j], cnt, cut, fastA, min(e1, tm >> 16));
-                                        const uint32_t num = (uint32_t)(fr >> 32), den = (uint32_t)fr;
-                                        if ((uint64_t)num * bden > (uint64_t)bnum * den) {
-                                            bnum = num;
-                                            bden = den;
-                                        }
+                            const uint32_t valid = lim == 32 ? 0xFFFFFFFFu : (1u << lim) - 1u;
+                            // pass 1, no branches: which columns count for this row
+                            // (kmask) and which are above the cut (cmask)
+                            uint32_t kmask = 0, cmask = 0;
+                            TC_STAMP(t_mk);
+#pragma unroll 8
+                            for (uint32_t q = 0; q < 32; q++) {
+                                if (q < lim) {
+                                    const uint32_t s2 = T.tmeta[c0 + q] & 0xFFFFu;
+                                    const uint32_t sum = s1 + s2;
+                                    const uint32_t cut = !fastA
+                                        ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
+                                        : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                                    const bool ct = active && s2 >= (uint32_t)kMinElem;
+                                    kmask |= (uint32_t)ct << q;
+                                    cmask |= (uint32_t)(ct && S.cstage[q][tid] > cut) << q;
+                                }
+                            }
+                            // pass 2: the slice's segments in column order (the same for
+                            // every thread, so the ring fold's barrier stays uniform); in
+                            // each, this row's columns above the cut, then the segment end
+                            if (tid == 0) TC_ADD(kTcPhMark, t_mk);
+                            TC_STAMP(t_wk);
+                            uint32_t lmq = T.lastmask[c0 >> 5] & valid;
+                            uint32_t q0 = 0;
+                            for (;;) {
+                                const uint32_t qe = lmq ? (uint32_t)(__ffs(lmq) - 1) : lim;  // end column (incl.) or slice end
+                                const uint32_t upto = lmq ? qe + 1 : lim;
+                                const uint32_t range = (upto == 32 ? 0xFFFFFFFFu : (1u << upto) - 1u) & ~(q0 >= 32 ? 0xFFFFFFFFu : (1u << q0) - 1u);
+                                if (kmask & range) counted = true;  // a counted target filter scores at least 0
+                                for (uint32_t cm = cmask & range; cm; cm &= cm - 1u) {
+                                    const uint32_t q = __ffs(cm) - 1;
+                                    const uint32_t j = c0 + q;
+                                    const uint32_t tm = T.tmeta[j];
+                                    const uint32_t sum = s1 + (tm & 0xFFFFu);
+                                    const uint32_t cut = !fastA
+                                        ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
+                                        : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
+                                    const uint64_t fr = candidate_fraction(aw, T.tw[j], S.cstage[q][tid], cut, fastA,
+                                                                           min(e1, tm >> 16));
+                                    const uint32_t num = (uint32_t)(fr >> 32), den = (uint32_t)fr;
+                                    if ((uint64_t)num * bden > (uint64_t)bnum * den) {
+                                        bnum = num;
+                                        bden = den;
                                     }
                                 }
-                                if ((lm >> q) & 1u) {
+                                if (!lmq) break;  // the open segment goes on in the next slice
+                                lmq &= lmq - 1u;
+                                q0 = qe + 1;
+                                const uint32_t j = c0 + qe;
+                                {
                                     const double m = row_maximum(active, bnum, bden, counted);
                                     if (split) {
                                         if (have) P.slots[P.split[U.split].slot_base + row] = m;
@@ -611,6 +627,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                     }
                                 }
                             }
+                            if (tid == 0) TC_ADD(kTcPhWalk, t_wk);
                         }
                         if (pend) {  // the tile's last completed targets
                             TC_STAMP(t_fo);

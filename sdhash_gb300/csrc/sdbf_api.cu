@@ -133,7 +133,7 @@ extern "C" int sdbfg_ctx_kernel_time(sdbfg_ctx* c, const char* name, double* tot
         "k_matrix_tc.compose", "k_matrix_tc.fill", "k_matrix_tc.fetch_wait", "k_matrix_tc.stage_wait",
         "k_matrix_tc.widen", "k_matrix_tc.issue", "k_matrix_tc.producer_step", "k_matrix_tc.acc_wait",
         "k_matrix_tc.score", "k_matrix_tc.fold", "k_matrix_tc.consumer_step", "k_matrix_tc.step_barrier",
-        "k_matrix_tc.tiles", "k_matrix_tc.tmem_ld"};
+        "k_matrix_tc.tiles", "k_matrix_tc.tmem_ld", "k_matrix_tc.mark", "k_matrix_tc.walk"};
     for (int k = 0; k < kTcPhCount; k++)
         if (!strcmp(name, kTcNames[k]) && c->d_mphase.p) {
             unsigned long long v[kTcPhCount];
