@@ -563,19 +563,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             // (kmask) and which are above the cut (cmask)
                             uint32_t kmask = 0, cmask = 0;
                             TC_STAMP(t_mk);
-#pragma unroll 8
+                            // a table lookup only: element sums of 1024 and more (beyond
+                            // the reference's limits, never produced by its generator) are
+                            // marked and get their exact cut in pass 2
+                            const uint16_t* ctab = fastA ? S.cut64_sum : S.cut_sum;
+                            // (all 32 columns from the registers; c0 + 31 < 256, so the
+                            // columns past the tile read stale entries and are masked off)
+#pragma unroll
                             for (uint32_t q = 0; q < 32; q++) {
-                                if (q < lim) {
-                                    const uint32_t s2 = T.tmeta[c0 + q] & 0xFFFFu;
-                                    const uint32_t sum = s1 + s2;
-                                    const uint32_t cut = !fastA
-                                        ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
-                                        : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
-                                    const bool ct = active && s2 >= (uint32_t)kMinElem;
-                                    kmask |= (uint32_t)ct << q;
-                                    cmask |= (uint32_t)(ct && S.cstage[q][tid] > cut) << q;
-                                }
+                                const uint32_t s2 = T.tmeta[c0 + q] & 0xFFFFu;
+                                const uint32_t sum = s1 + s2;
+                                const uint32_t cut = sum < 1024 ? ctab[sum] : 0u;
+                                const bool ct = s2 >= (uint32_t)kMinElem;
+                                kmask |= (uint32_t)ct << q;
+                                cmask |= (uint32_t)(ct && (uint32_t)__uint_as_float(v[q]) > cut) << q;
                             }
+                            kmask = active ? kmask & valid : 0u;
+                            cmask = active ? cmask & valid : 0u;
                             // pass 2: the slice's segments in column order (the same for
                             // every thread, so the ring fold's barrier stays uniform); in
                             // each, this row's columns above the cut, then the segment end
