@@ -1,9 +1,10 @@
 // matrix_tc.cu -- the filter-matrix comparison counted on the tensor cores.
 //
 // popcount(a & b) of two 2048-bit filters is the dot product of their bit
-// vectors.  With each bit widened to an e4m3 byte (1.0 = 0x38 or 0) and fp32
-// accumulation, tcgen05.mma computes it exactly (every partial sum is an
-// integer <= 2048).  One CTA multiplies 128 reference filters (TMEM lanes)
+// vectors.  With each bit widened to an e4m3 byte (0x08 = 2^-6, or 0) and
+// fp32 accumulation, tcgen05.mma computes it exactly: every product is
+// 2^-12, every partial sum a multiple of 2^-12 no larger than 2048 * 2^-12,
+// well inside fp32's 24-bit significand; the count is the sum times 4096.  One CTA multiplies 128 reference filters (TMEM lanes)
 // by tiles of up to 256 target filters (TMEM columns) over K = 2048 in 16
 // chunks of 128.  The CTA is a two-stage software pipeline: warps 4-7
 // compose tile g, fetch its filter bits with cp.async, widen each chunk into
@@ -24,8 +25,8 @@
 //
 // The widening permutes K inside each 32-bit word (output word k of a word
 // w holds bits k, k+8, k+16, k+24 of w), identically for both operands, so
-// the dot product is unchanged; one shift and one mask per output word, the
-// x0x38 on the FMA pipe.  --fast digests count only chunks 0-3 (their first
+// the dot product is unchanged; bit k of each byte moves to bit 3 (the
+// single set bit of 0x08), one shift and one mask per output word.  --fast digests count only chunks 0-3 (their first
 // 64 bytes).
 //
 // Every mbarrier wait is bounded; a wait that gives up sets P.error, all
@@ -112,6 +113,11 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     return d;
 }
 
+// bit k of every byte of w, as 0x08 or 0x00 in that byte
+__device__ __forceinline__ uint32_t bit_to_08(uint32_t w, int k) {
+    return (k <= 3 ? w << (3 - k) : w >> (k - 3)) & 0x08080808u;
+}
+
 // row r's 128 e4m3 bytes of one chunk from its 128 filter bits (4 words):
 // 8 granules of 16 bytes at their swizzled places
 __device__ __forceinline__ void widen_row(uint8_t* stage, uint32_t r, uint4 bits) {
@@ -122,10 +128,10 @@ __device__ __forceinline__ void widen_row(uint8_t* stage, uint32_t r, uint4 bits
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             uint4 g;
-            g.x = ((w[m] >> (4 * h + 0)) & 0x01010101u) * 0x38u;
-            g.y = ((w[m] >> (4 * h + 1)) & 0x01010101u) * 0x38u;
-            g.z = ((w[m] >> (4 * h + 2)) & 0x01010101u) * 0x38u;
-            g.w = ((w[m] >> (4 * h + 3)) & 0x01010101u) * 0x38u;
+            g.x = bit_to_08(w[m], 4 * h + 0);
+            g.y = bit_to_08(w[m], 4 * h + 1);
+            g.z = bit_to_08(w[m], 4 * h + 2);
+            g.w = bit_to_08(w[m], 4 * h + 3);
             const uint32_t gi = 2 * m + h;
             *reinterpret_cast<uint4*>(row + ((gi ^ (r & 7)) << 4)) = g;
         }
@@ -555,7 +561,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                 : "r"(taddr));
                             asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-                            for (int q = 0; q < 32; q++) S.cstage[q][tid] = (uint16_t)__uint_as_float(v[q]);
+                            for (int q = 0; q < 32; q++) S.cstage[q][tid] = (uint16_t)(__uint_as_float(v[q]) * 4096.0f);
                             if (tid == 0) TC_ADD(kTcPhLd, t_ld);
                             const uint32_t lim = min(32u, nt - c0);
                             const uint32_t valid = lim == 32 ? 0xFFFFFFFFu : (1u << lim) - 1u;
@@ -576,7 +582,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                 const uint32_t cut = sum < 1024 ? ctab[sum] : 0u;
                                 const bool ct = s2 >= (uint32_t)kMinElem;
                                 kmask |= (uint32_t)ct << q;
-                                cmask |= (uint32_t)(ct && (uint32_t)__uint_as_float(v[q]) > cut) << q;
+                                cmask |= (uint32_t)(ct && (uint32_t)(__uint_as_float(v[q]) * 4096.0f) > cut) << q;
                             }
                             kmask = active ? kmask & valid : 0u;
                             cmask = active ? cmask & valid : 0u;
