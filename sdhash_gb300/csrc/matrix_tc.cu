@@ -58,7 +58,7 @@ constexpr int kTcBitSlots = 3;     // chunks of filter bits in flight (cp.async 
 // one tile's composition (double-buffered: warps 4-7 compose and count tile
 // k while warps 0-3 score tile k-1)
 struct TcTile {
-    uint4 tw[kTcCols][8];  // first 128 bytes of each target filter (staged re-check of candidates)
+    uint4 tw[8][kTcCols];  // first 128 bytes of each target filter, chunk-major (staged re-check)
     uint32_t gidx[kTcCols], tmeta[kTcCols], tinfo[kTcCols], comp[kTcCols];
     uint32_t seg_first[kTcCols], seg_start[kTcCols + 1], seg_te[kTcCols];  // one segment per target
     uint32_t lastmask[kTcCols / 32];
@@ -162,7 +162,8 @@ struct RowHead {
 
 // A pair whose full count is above the cut (rare): the reference's staged
 // exits (normal mode: after 8, 16, 32 words) or its 32-byte stage (fast
-// mode), from the row's first 128 bytes and the target's (shared memory).
+// mode), from the row's first 128 bytes and the target's (shared memory,
+// 16 bytes every kTcCols uint4s).
 // Returns (num << 32) | den of the pair's score (0 / 1 when it scores 0).
 __device__ __forceinline__ uint64_t candidate_fraction(const RowHead& aw, const uint4* tw, uint32_t cnt,
                                                       uint32_t cut, bool fast, uint32_t max_est) {
@@ -171,7 +172,7 @@ __device__ __forceinline__ uint64_t candidate_fraction(const RowHead& aw, const 
     uint32_t p[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-        const uint4 y = tw[q];
+        const uint4 y = tw[q * kTcCols];
         p[q] = __popc(aw.w[q].x & y.x) + __popc(aw.w[q].y & y.y) + __popc(aw.w[q].z & y.z) + __popc(aw.w[q].w & y.w);
     }
     const uint32_t c1 = p[0] + p[1], c2 = c1 + p[2] + p[3], c3 = c2 + p[4] + p[5] + p[6] + p[7];
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                 } else {
                                     if (i - kTcRows < nt) {
                                         bits = slot[i];
-                                        if (c < 8) T.tw[i - kTcRows][c] = bits;
+                                        if (c < 8) T.tw[c][i - kTcRows] = bits;
                                     }
                                     widen_row(sb, i - kTcRows, bits);
                                 }
@@ -606,7 +607,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                                     const uint32_t cut = !fastA
                                         ? (sum < 1024 ? S.cut_sum[sum] : S.cut256[4096u / sum])
                                         : (sum < 1024 ? S.cut64_sum[sum] : S.cut64[1024u / sum]);
-                                    const uint64_t fr = candidate_fraction(aw, T.tw[j], S.cstage[q][tid], cut, fastA,
+                                    const uint64_t fr = candidate_fraction(aw, &T.tw[0][j], S.cstage[q][tid], cut, fastA,
                                                                            min(e1, tm >> 16));
                                     const uint32_t num = (uint32_t)(fr >> 32), den = (uint32_t)fr;
                                     if ((uint64_t)num * bden > (uint64_t)bnum * den) {
