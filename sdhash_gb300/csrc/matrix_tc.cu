@@ -79,6 +79,8 @@ struct TcSmem {
     alignas(8) uint64_t mbar[5];      // stage 0, stage 1 emptied; accumulator 0, 1 full; drain
 };
 
+static_assert(kTcRows == 128 && kTcCols == 256 && kTcThreads == 256,
+              "producer threads widen one reference row and two target columns each");
 constexpr size_t kTcSmemBytes = 1024 /* alignment */ + 2 * kTcStage + sizeof(TcSmem);
 static_assert(kTcSmemBytes <= 227 * 1024, "tensor-core kernel exceeds the shared memory of one CTA");
 
@@ -494,18 +496,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_matrix_tc(MatParams P) {
                             uint8_t* sa = stages + s * kTcStage;
                             uint8_t* sb = sa + kTcAStage;
                             const uint4* slot = S.bits[c % kTcBitSlots];
-                            for (uint32_t i = ptid; i < kTcRows + ncols; i += 128) {
-                                uint4 bits = make_uint4(0, 0, 0, 0);
-                                if (i < kTcRows) {
-                                    if (S.rowf[i] != 0xFFFFFFFFu) bits = slot[i];
-                                    widen_row(sa, i, bits);
-                                } else {
-                                    if (i - kTcRows < nt) {
-                                        bits = slot[i];
-                                        if (c < 8) T.tw[c][i - kTcRows] = bits;
-                                    }
-                                    widen_row(sb, i - kTcRows, bits);
+                            {
+                                // each producer thread: reference row ptid and target
+                                // columns ptid, ptid + 128 (zero bits past the tile);
+                                // the three loads first, then the three widenings
+                                const uint32_t c1 = ptid, c2 = ptid + 128;
+                                const uint4 z = make_uint4(0, 0, 0, 0);
+                                const uint4 ba = S.rowf[ptid] != 0xFFFFFFFFu ? slot[ptid] : z;
+                                const uint4 b1 = c1 < nt ? slot[kTcRows + c1] : z;
+                                const uint4 b2 = c2 < nt ? slot[kTcRows + c2] : z;
+                                if (c < 8) {
+                                    if (c1 < nt) T.tw[c][c1] = b1;
+                                    if (c2 < nt) T.tw[c][c2] = b2;
                                 }
+                                widen_row(sa, ptid, ba);
+                                if (c1 < ncols) widen_row(sb, c1, b1);
+                                if (c2 < ncols) widen_row(sb, c2, b2);
                             }
                             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                             group_sync<2>();
