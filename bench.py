@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
     ap.add_argument("--plain-pairs", type=int, default=400, help="allpairs: pairs timed one call each")
     ap.add_argument("--cpu-pairs", type=int, default=256, help="allpairs: pairs timed on the host (oracle)")
+    ap.add_argument("--phases", action="store_true",
+                    help="allpairs: one more run with the tensor-core kernel's per-phase cycle counters")
     ap.add_argument("--variant", type=int, default=-1,
                     help="comparison kernel variant (0-4 CUDA cores, 5 tensor cores); -1: autotune")
     return ap.parse_args()
@@ -299,6 +301,24 @@ def allpairs_digests(args, ctx):
     return digs, counts, int(sizes.sum())
 
 
+TC_PHASES = ("compose", "fill", "fetch_wait", "stage_wait", "widen", "issue", "producer_step", "acc_wait", "score",
+             "mark", "walk", "fold", "consumer_step", "step_barrier", "tmem_ld")
+
+
+def tc_phases(ctx, run):
+    """SM cycles per tile of each phase of the tensor-core kernel (one CTA's
+    clock, summed over CTAs, divided by the tiles counted) for one more run."""
+    import torch
+    ctx.profile(True)
+    run()
+    torch.cuda.synchronize()
+    tiles = ctx.kernel_time("k_matrix_tc.tiles")[0] or 1.0
+    out = {k: round(ctx.kernel_time("k_matrix_tc." + k)[0] / tiles) for k in TC_PHASES}
+    out["tiles"] = int(tiles)
+    ctx.profile(False)
+    return out
+
+
 def main_allpairs(args):
     import torch
     import sdhash_gb300 as g
@@ -405,6 +425,8 @@ def main_allpairs(args):
                              "sample": f"{len(ci)} random pairs ({cpu_work} filter pairs)",
                              "seconds": round(t_cpu, 3)},
             "scores_ge_1": int((scores >= 1).sum())}
+    if args.phases and variant == 5:
+        line["tc_phase_cycles_per_tile"] = tc_phases(ctx, lambda: ctx.compare_all_device(dev, out.data_ptr()))
     print(json.dumps(line), flush=True)
     return 0
 
