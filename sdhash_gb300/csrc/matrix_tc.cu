@@ -183,8 +183,14 @@ __device__ __forceinline__ uint64_t candidate_fraction(const RowHead& aw, const 
     return ((uint64_t)(cnt - cut) << 32) | (uint32_t)(max_est - cut);
 }
 
-__device__ __noinline__ double row_maximum(bool active, uint32_t bnum, uint32_t bden, bool counted) {
-    return max_value(active, bnum, bden, counted);
+// A row's maximum over a completed target (max_value), with the division
+// of the rare positive score out of line.
+__device__ __noinline__ double score_ratio(uint32_t bnum, uint32_t bden) { return __ddiv_rn((double)bnum, (double)bden); }
+
+__device__ __forceinline__ double row_maximum(bool active, uint32_t bnum, uint32_t bden, bool counted) {
+    if (!active) return 0.0;
+    if (!counted) return -1.0;
+    return bnum == 0 ? 0.0 : score_ratio(bnum, bden);
 }
 
 // Sums the maxima of `done` completed targets (completion indices from
