@@ -86,9 +86,24 @@ def build_synth(force: bool = False) -> str:
     return SYNTH
 
 
+CLI_SRC = os.path.join(HERE, "cli", "sdhash_main.cpp")
+CLI = os.path.join(HERE, "sdhash-gb300")
+
+
+def build_cli(force: bool = False) -> str:
+    """The native command line (sdhash's options) linked against the library."""
+    lib = build_gb300()
+    if force or _stale(CLI, [CLI_SRC, lib, os.path.join(INCLUDE, "sdbf_gb300.h")]):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-O2", "-std=c++17", "-Wall", "-o", CLI, CLI_SRC, "-L", HERE, "-lsdbf_gb300",
+              "-Wl,-rpath,$ORIGIN", "-lpthread"])
+    return CLI
+
+
 def build_all(force: bool = False, verbose: bool = False) -> None:
     build_synth(force)
     build_gb300(force, verbose)
+    build_cli(force)
 
 
 if __name__ == "__main__":

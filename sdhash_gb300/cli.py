@@ -55,7 +55,8 @@ def _collect(inputs, deep: bool):
     files = []
     for p in inputs:
         if deep and os.path.isdir(p):
-            for root, _dirs, names in os.walk(p):
+            for root, dirs, names in os.walk(p):
+                dirs.sort()  # each directory's files in name order, then its subdirectories in name order
                 for n in sorted(names):
                     q = os.path.join(root, n)
                     if os.path.isfile(q):

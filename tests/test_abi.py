@@ -121,3 +121,17 @@ def test_cli_segments_follow_reference_rule():
         assert [o for _, o, _ in got] == [j * 128 * M for j in range(len(got))]
     names = [nm for nm, _, _ in _segments("img", 300 * M, 128 * M)]
     assert names == ["img.0000M", "img.0128M", "img.0256M"]
+
+
+def test_native_cli_builds_and_answers_without_a_gpu(native):
+    """The native command line links against the library; --version and
+    --help need no device, and a command that needs one fails cleanly."""
+    import subprocess
+    from sdhash_gb300 import build
+    exe = build.build_cli()
+    r = subprocess.run([exe, "--version"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "SDBF v3" in r.stdout
+    r = subprocess.run([exe, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "--index-search" in r.stdout and "--gen-compare" in r.stdout
+    r = subprocess.run([exe, "-s", "4", "x"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 255 and "not offered" in r.stderr
