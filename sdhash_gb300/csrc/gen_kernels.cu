@@ -58,7 +58,7 @@ struct TileGeom {
 // Shared-memory carve-up for a tile of at most Lmax owned positions.
 struct TileSmem {
     uint32_t* bytes32;     // chunk bytes [Q0, BE) (+pad)
-    uint16_t* ranks;       // ranks [Q0, RE)
+    uint16_t* ranks;       // ranks [Q0, RE); from the full-rescan phase on, bits 10-15 hold run lengths
     uint8_t* hist;         // per-thread byte histograms (phase 2 only)
     uint16_t* fres;        // full-rescan result per step [Q0, SE)
     uint32_t* eqw;         // run bits: bit o = rank[o]==rank[o+1]
@@ -233,6 +233,18 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
     }
     if (threadIdx.x < 4) s.eqw[nw + threadIdx.x] = 0;
     __syncthreads();
+    // run lengths: bits 10-15 of each rank entry (ranks are <= 990) hold how
+    // many of the following ranks equal it, capped at 63 (a run that long
+    // reaches the end of any window that starts at or before it)
+    for (uint32_t o = threadIdx.x; o < np; o += blockDim.x) {
+        const uint32_t w = o >> 5, sh = o & 31;
+        const uint32_t lo32 = __funnelshift_r(s.eqw[w], s.eqw[w + 1], sh);
+        const uint32_t hi32 = __funnelshift_r(s.eqw[w + 1], s.eqw[w + 2], sh);
+        const uint64_t bits = ((uint64_t)hi32 << 32) | lo32;
+        const uint32_t len = (~bits == 0ull) ? 63u : min(63u, (uint32_t)__ffsll((long long)~bits) - 1);
+        s.ranks[pidx(o)] = (uint16_t)(s.ranks[pidx(o)] | (len << 10));
+    }
+    __syncthreads();
     const uint32_t nsteps = g.SE - g.Q0;
     const uint32_t nblk = (nsteps + 63) / 64;
     for (uint32_t j = threadIdx.x; j < nblk; j += blockDim.x) {
@@ -244,17 +256,16 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 #pragma unroll
         for (int u = 0; u < 64; u++) {
             const uint32_t o = base + 64 + u;
-            uint32_t r = (o < np) ? s.ranks[pidx(o)] : 0;
+            uint32_t r = (o < np) ? s.ranks[pidx(o)] & 1023u : 0;
             const uint32_t key = ((r == 0 ? 1023u : r) << 6) | (uint32_t)u;
             run = min(run, key);
             pre[u] = (uint16_t)run;
         }
         uint32_t suf = 0xFFFFu;
-        uint32_t last_f = 0xFFFFFFFFu, last_end = 0;
 #pragma unroll
         for (int u = 63; u >= 0; u--) {
             const uint32_t k = base + u;
-            const uint32_t rk = (k < np) ? s.ranks[pidx(k)] : 0;
+            const uint32_t rk = (k < np) ? s.ranks[pidx(k)] & 1023u : 0;
             suf = min(suf, ((rk == 0 ? 1023u : rk) << 6) | (uint32_t)u);
             if (k < nsteps) {
                 uint16_t out = 0;
@@ -273,18 +284,9 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
                             m = pk >> 6;
                         }
                     }
-                    // end of the run of equal ranks starting at f (the run bits
-                    // are only re-read when f changes)
-                    if (f != last_f) {
-                        const uint32_t w = f >> 5, sh = f & 31;
-                        const uint32_t b0 = s.eqw[w], b1 = s.eqw[w + 1], b2 = s.eqw[w + 2];
-                        const uint32_t lo32 = __funnelshift_r(b0, b1, sh);
-                        const uint32_t hi32 = __funnelshift_r(b1, b2, sh);
-                        const uint64_t bits = ((uint64_t)hi32 << 32) | lo32;
-                        last_end = f + ((~bits == 0ull) ? 64u : (uint32_t)__ffsll((long long)~bits) - 1);
-                        last_f = f;
-                    }
-                    uint32_t p = last_end;
+                    // end of the run of equal ranks starting at f (f >= k, so a
+                    // run length capped at 63 gives the same cap at k + 63)
+                    uint32_t p = f + (s.ranks[pidx(f)] >> 10);
                     if (p > k + 63) p = k + 63;
                     out = (uint16_t)((m << 6) | (p - k));
                 }
@@ -331,9 +333,10 @@ __device__ __forceinline__ ChainState walk(const TileGeom& g, const TileSmem& s,
     if (a >= b) return st;
     const uint16_t* __restrict__ R = s.ranks;
     const uint16_t* __restrict__ Fr = s.fres;
-    uint32_t r64 = R[pidx(a + 64 - g.Q0)], f = Fr[pidx(a - g.Q0)];
+    // (rank entries carry a run length in bits 10-15: masked off here)
+    uint32_t r64 = R[pidx(a + 64 - g.Q0)] & 1023u, f = Fr[pidx(a - g.Q0)];
     for (uint32_t i = a; i < b; i++) {
-        const uint32_t r64n = R[pidx(i + 65 - g.Q0)], fn = Fr[pidx(i + 1 - g.Q0)];
+        const uint32_t r64n = R[pidx(i + 65 - g.Q0)] & 1023u, fn = Fr[pidx(i + 1 - g.Q0)];
         const bool cheap = (st.M != 0) & (r64 >= st.M) & (i < st.P);
         const uint32_t cheapP = (r64 == st.M) ? i + 64 : st.P;
         st.P = cheap ? cheapP : i + (f & 63);
