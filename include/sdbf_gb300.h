@@ -68,7 +68,7 @@ uint64_t sdbfg_ctx_launch_count(const sdbfg_ctx *ctx);
 int sdbfg_ctx_profile(sdbfg_ctx *ctx, int enable);
 int sdbfg_ctx_kernel_time(sdbfg_ctx *ctx, const char *kernel, double *total_ms, uint64_t *launches);
 /* Speculative lead-in of the parallel popularity-score walk, in window steps
- * (default 48, maximum 128).  Results are exact for every value -- shorter
+ * (default 64, maximum 128).  Results are exact for every value -- shorter
  * lead-ins only make the re-walk path run more often; tests use this to
  * exercise it.  No counterpart in the reference (its walk is sequential). */
 int sdbfg_ctx_set_lead(sdbfg_ctx *ctx, uint32_t steps);

@@ -348,10 +348,10 @@ __device__ __forceinline__ ChainState walk(const TileGeom& g, const TileSmem& s,
     return st;
 }
 
-// Lead-in of a tile's first segment: the maximum under the default lead (a
-// failed link between tiles recomputes a whole tile), the configured lead
-// otherwise (so tests can drive the cross-tile path).
-__host__ __device__ inline uint32_t tile_lead(uint32_t lead) { return lead >= kDefaultLead ? kLead : lead; }
+// Lead-in of a tile's first segment: the maximum for leads from
+// kFullTileLead on (a failed link between tiles recomputes a whole tile),
+// the configured lead below it (so tests can drive the cross-tile path).
+__host__ __device__ inline uint32_t tile_lead(uint32_t lead) { return lead >= kFullTileLead ? kLead : lead; }
 
 // Re-walk segment [St, Et) from its true entry state `nw` next to the chain
 // it was credited with (`old`, from its speculative entry).  Both walks run

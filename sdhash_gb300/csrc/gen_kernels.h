@@ -12,8 +12,10 @@ constexpr int kRankThreads = 96;     // threads computing ranks: 3 full warps, e
                                      // a 256-byte histogram in its own bank
 constexpr int kSegs = 128;           // popularity-chain segments per tile (one per thread)
 constexpr uint32_t kLead = 128;      // maximum speculative lead-in steps per segment
-constexpr uint32_t kDefaultLead = 48; // default lead-in; mis-speculated segments are re-walked only
-                                     // until their chain meets the speculative one
+constexpr uint32_t kDefaultLead = 64; // default lead-in (measured best of 16..128 on the bulk stream
+                                     // workload); mis-speculated segments are re-walked only until
+                                     // their chain meets the speculative one
+constexpr uint32_t kFullTileLead = 48;  // leads from here on give a tile's first segment kLead
 // window steps owned by a stream tile: with the 64-step credit halo and the
 // 128-step maximum lead-in a tile simulates 8128 steps (127 aligned 64-step
 // blocks, one per thread of the full-rescan table)

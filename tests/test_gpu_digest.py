@@ -39,10 +39,10 @@ def test_small_cases_one_batch(ctx, golden, dd):
     assert not bad, f"dd={dd}: {bad}"
 
 
-@pytest.mark.parametrize("lead", [0, 3, 17, 64])
+@pytest.mark.parametrize("lead", [0, 3, 17, 48, 128])
 def test_short_lead_in_exercises_relink(ctx, golden, lead):
-    """Lead-ins shorter than the default make speculation fail often; the
-    in-tile and cross-tile re-walks must keep the digests exact."""
+    """Lead-ins from none to the maximum (short ones make speculation fail
+    often); the in-tile and cross-tile re-walks keep the digests exact."""
     recs = [r for r in _golden_by_mode(golden)[0] if r["status"] == 0]
     big = [r for r in golden["large"] if r["dd"] == 0 and r["spec"]["n"] <= (8 << 20)]
     datas = [cases.make(r["spec"]) for r in recs + big]
@@ -51,7 +51,7 @@ def test_short_lead_in_exercises_relink(ctx, golden, lead):
     try:
         out = ctx.digest_buffers([d.tobytes() for d in datas], [r["name"] for r in recs + big], 0)
     finally:
-        ctx.set_lead(48)
+        ctx.set_lead(64)  # the default
     bad = [r["name"] for r, d in zip(recs + big, out) if sha(d.to_string()) != r["sha256"]]
     assert not bad, bad
     if lead <= 17:
@@ -142,6 +142,6 @@ def test_short_lead_in_block_mode(ctx, golden, lead):
     try:
         out = ctx.digest_buffers([d.tobytes() for d in datas], [r["name"] for r in recs], 16384)
     finally:
-        ctx.set_lead(48)
+        ctx.set_lead(64)  # the default
     bad = [r["name"] for r, d in zip(recs, out) if sha(d.to_string()) != r["sha256"]]
     assert not bad, bad
