@@ -766,7 +766,7 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                     const bool act = have && lane >= start;
                     if (!__any_sync(0xffffffffu, act)) break;
                     n_loops++;
-                    // round 1: state before the group, publish holders
+                    // pass 1: state before the group, publish holders
                     uint32_t fpre = 0, gpre = 0;
                     if (act) {
 #pragma unroll
@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                         }
                     }
                     __syncwarp();
-                    // round 2: holders of each index
+                    // pass 2: holders of each index
                     uint32_t m[5];
 #pragma unroll
                     for (int k = 0; k < 5; k++) m[k] = act ? S.own[a[k]] : 0u;
