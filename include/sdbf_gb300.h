@@ -204,6 +204,31 @@ int sdbfg_digest_batch_search(sdbfg_ctx *ctx, const uint8_t *host_data, const ui
                               const uint64_t *lens, uint32_t n, uint32_t dd_block_size, uint8_t *out_filters,
                               uint64_t out_cap, uint16_t *out_counts, sdbfg_digest_result *results,
                               const sdbfg_index *const *indexes, uint32_t nidx, uint8_t *out_hits);
+/* Digests (as sdbfg_digest_batch) with an index being built, as sdhash
+ * --index builds one per group of files (sdhash-src/sdhash_threads.cc:
+ * 376-470).  index_bits (index_bytes, a power of two, host memory) is the
+ * index before the batch and receives it after; *elem_count is increased by
+ * the inserts that set a new bit (bloom_filter::insert_sha1,
+ * bloom_filter.cc:333-359).  Stream mode (dd_block_size 0): every feature
+ * whose filter insert set a new bit is inserted into the index and is
+ * skipped unless that set a new index bit (sdbf_core.cc:108-114), so each
+ * digest depends on the inputs before it: inputs are taken in order, as
+ * sdhash -p 1 does.  Block mode: every counted feature is inserted
+ * (sdbf_core.cc:164-167) and the digests are those of sdbfg_digest_batch. */
+int sdbfg_digest_batch_index(sdbfg_ctx *ctx, const uint8_t *host_data, const uint64_t *offsets, const uint64_t *lens,
+                             uint32_t n, uint32_t dd_block_size, uint8_t *out_filters, uint64_t out_cap,
+                             uint16_t *out_elem_counts, sdbfg_digest_result *results, uint8_t *index_bits,
+                             uint64_t index_bytes, uint64_t *elem_count);
+/* bloom_filter::write_out (bloom_filter.cc:190-216): the index file header
+ * and the filter as one LZ4 block (this library's own encoder: any LZ4
+ * decoder, the reference's included, reads it; the bytes differ from the
+ * reference's compressor's).  Host-only; SDBFG_ERR_ARG when the file cannot
+ * be written. */
+int sdbfg_index_write_file(const char *path, const uint8_t *bits, uint64_t bf_size, uint64_t elem_count,
+                           uint32_t hash_count, const char *set_name);
+/* LZ4 block encode (the encoder of sdbfg_index_write_file): returns the
+ * encoded size; writes it to out when it fits out_cap.  Host-only. */
+int64_t sdbfg_lz4_encode(const uint8_t *in, uint64_t in_len, uint8_t *out, uint64_t out_cap);
 /* LZ4 block decode of in_len bytes into exactly out_len bytes (the index
  * file payload, LZ4_uncompress in bloom_filter::decompress,
  * bloom_filter.cc:185-190); returns the input bytes used or

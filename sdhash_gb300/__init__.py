@@ -113,6 +113,11 @@ def lib() -> C.CDLL:
         L.sdbfg_index_info.argtypes = [vp, u64p, u64p, C.POINTER(C.c_uint32), u64p, C.POINTER(C.c_char_p)]
         L.sdbfg_digest_batch_search.argtypes = [vp, vp, u64p, u64p, C.c_uint32, C.c_uint32, vp, C.c_uint64, vp, vp,
                                                 C.POINTER(vp), C.c_uint32, vp]
+        L.sdbfg_digest_batch_index.argtypes = [vp, vp, u64p, u64p, C.c_uint32, C.c_uint32, vp, C.c_uint64, vp, vp,
+                                               vp, C.c_uint64, u64p]
+        L.sdbfg_index_write_file.argtypes = [C.c_char_p, vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_char_p]
+        L.sdbfg_lz4_encode.argtypes = [vp, C.c_uint64, vp, C.c_uint64]
+        L.sdbfg_lz4_encode.restype = C.c_int64
         L.sdbfg_lz4_decode.argtypes = [vp, C.c_uint64, vp, C.c_uint64]
         L.sdbfg_lz4_decode.restype = C.c_int64
         L.sdbfg_set_load_text.argtypes = [vp, C.c_char_p, C.c_uint64, C.POINTER(vp), C.POINTER(C.c_int64),
@@ -488,6 +493,54 @@ class Context:
                                out_filters[o * 256:(o + k) * 256], counts[o:o + k].copy()))
             hit_rows.append(hits[o * nidx:(o + k) * nidx].reshape(k, nidx).copy())
         return digs, hit_rows
+
+    def digest_index(self, buffers, names, dd_block_size: int, index_bits: np.ndarray, elem_count: int = 0):
+        """Digests with an index being built (sdhash --index for one group of
+        files): stream mode takes the inputs in order and drops features the
+        index already holds, block mode inserts every counted feature.
+        index_bits (uint8, power-of-two size) is updated in place; returns
+        (digests, elem_count after the batch)."""
+        lens = np.array([len(b) for b in buffers], dtype=np.uint64)
+        offs = np.zeros(len(buffers), dtype=np.uint64)
+        tot = 0
+        for i, b in enumerate(buffers):
+            offs[i] = tot
+            tot += (len(b) + 15) & ~15
+        data = np.zeros(max(16, tot), dtype=np.uint8)
+        for i, b in enumerate(buffers):
+            data[int(offs[i]):int(offs[i]) + len(b)] = np.frombuffer(bytes(b), dtype=np.uint8)
+        n = len(lens)
+        cap = self.capacity(lens, dd_block_size)
+        out_filters = np.zeros(max(1, cap) * 256, dtype=np.uint8)
+        counts = np.zeros(max(1, cap), dtype=np.uint16)
+        res = (DigestResult * max(1, n))()
+        assert index_bits.dtype == np.uint8 and index_bits.flags.c_contiguous
+        ec = np.array([elem_count], dtype=np.uint64)
+        self._check(lib().sdbfg_digest_batch_index(self.h, data.ctypes.data, _ptr(offs), _ptr(lens), n, dd_block_size,
+                                                   out_filters.ctypes.data, cap, counts.ctypes.data, res,
+                                                   index_bits.ctypes.data, index_bits.size, _ptr(ec)))
+        digs = []
+        for i in range(n):
+            r = res[i]
+            if r.status != 0:
+                digs.append(None)
+                continue
+            o, k = int(r.filter_offset), int(r.bf_count)
+            f = out_filters[o * 256:(o + k) * 256]
+            if dd_block_size:
+                digs.append(Digest(names[i], int(lens[i]), k, 0, BLOCK_MAX_ELEM, dd_block_size, f, counts[o:o + k].copy()))
+            else:
+                digs.append(Digest(names[i], int(lens[i]), k, int(r.last_count), STREAM_MAX_ELEM, 0, f, None))
+        return digs, int(ec[0])
+
+    @staticmethod
+    def write_index(path: str, bits: np.ndarray, elem_count: int, set_name: str, hash_count: int = 5):
+        """bloom_filter::write_out: an index file the reference can read."""
+        bits = np.ascontiguousarray(bits, dtype=np.uint8)
+        rc = lib().sdbfg_index_write_file(os.fsencode(path), bits.ctypes.data, bits.size, elem_count, hash_count,
+                                          set_name.encode())
+        if rc != 0:
+            raise SdbfError(-2, f"cannot write {path}")
 
     def digest_buffers(self, buffers, names=None, dd_block_size: int = 0):
         """Digest a list of bytes-like inputs."""

@@ -12,8 +12,9 @@ pairs, `-c` compares the digests of one SDBF file (all pairs) or of two
 (every digest of the first against every digest of the second).  Result
 lines, separators, thresholds and `--fast` are the reference's.  Not
 offered: `-s` (filter sampling seeds rand() from time() in the reference),
-`--large`, `--index` (index building), `--details`.  `--index-search DIR`
-looks every block up in the directory's index files on the GPU.
+`--large`, `--details`.  `--index` builds an index per group of files as
+the reference does with one thread; `--index-search DIR` looks every block
+up in the directory's index files on the GPU.
 """
 from __future__ import annotations
 
@@ -125,6 +126,70 @@ def _hash(ctx, files, block_kb: int, seg: int, name_for_stdin=None, stdin_data=N
     return done()
 
 
+INDEX_BYTES = 64 << 20   # bloom_filter(64*MB, 5, 0, 0.01), sdhash_threads.cc:414,460
+INDEX_GROUP = 640 * MB   # a group ends once its files exceed this (sdhash_threads.cc:409,455)
+
+
+def _index_files(ctx, files, output: str, seg: int):
+    """hash_index_stringlist (sdhash-src/sdhash_threads.cc:376-470) for one of
+    the small / large file lists: files in groups of just over 640 MB, each
+    hashed with a fresh 64 MiB index (files below 16 MiB in stream mode, the
+    others in 16 KiB block mode with 128 MiB segments), written as
+    <output><k>.sdbf and its index <output><k>.sdbf.idx, k counting from 0.
+    The reference's file-list array is reproduced as it behaves: after a
+    group its count restarts at 1, so each later group also hashes the file
+    left in slot 0."""
+    import numpy as np
+    for count, gi in enumerate(_index_groups([os.path.getsize(f) for f in files])):
+        group = [files[i] for i in gi]
+        bits = np.zeros(INDEX_BYTES, dtype=np.uint8)
+        if os.path.getsize(group[0]) < 16 * MB and all(os.path.getsize(x) < 16 * MB for x in group):
+            bufs = [open(x, "rb").read() for x in group]
+            digs, ec = ctx.digest_index(bufs, group, 0, bits)
+        else:
+            names, bufs, got = [], [], []
+            for x in group:
+                data = np.fromfile(x, dtype=np.uint8)
+                for nm, o, n in _segments(x, len(data), seg):
+                    b = np.zeros(n, dtype=np.uint8)
+                    part = data[o:o + n]
+                    b[:len(part)] = part
+                    names.append(nm)
+                    bufs.append(b)
+                    got.append(len(part))
+            digs, ec = ctx.digest_index(bufs, names, 16 * KB, bits)
+            for d, n in zip(digs, got):
+                if d is not None:
+                    d.orig_size = n
+            digs = [d for d, n in zip(digs, got) if d is not None and n >= 512]
+        name = f"{output}{count}.sdbf"
+        with open(name, "w") as fh:
+            fh.write("".join(d.to_string() for d in digs if d is not None))
+        ctx.write_index(name + ".idx", bits, ec, name)
+    return 0
+
+
+def _index_groups(sizes):
+    """The groups hash_index_stringlist hashes (sdhash-src/
+    sdhash_threads.cc:402-411,446-455), as lists of positions in the file
+    list: a group closes once the running size passes 640 MB or at the last
+    file.  Its file array keeps the entry in slot 0 after a group (the
+    count restarts at 1), and the running size is a C int, which wraps
+    modulo 2^32 (a file of 2 GiB or more makes it negative)."""
+    groups, slots, filect, total = [], [], 0, 0
+    for i, n in enumerate(sizes):
+        if filect < len(slots):
+            slots[filect] = i
+        else:
+            slots.append(i)
+        total = ((total + n + (1 << 31)) & 0xFFFFFFFF) - (1 << 31)
+        if total > INDEX_GROUP or i == len(sizes) - 1:
+            groups.append(slots[:filect + 1])
+            total, filect = 0, 0
+        filect += 1
+    return groups
+
+
 def _load_indexes(ctx, idx_dir: str):
     """The --index-search list (sdhash-src/sdhash.cc:241-266): every regular
     '*.idx' file of the directory in directory order, each with the name of
@@ -180,6 +245,7 @@ def main(argv=None) -> int:
     ap.add_argument("--hash-name", default=None, help="set name of hash on stdin")
     ap.add_argument("--fast", action="store_true", help="shrink sdbf filters for speedup")
     ap.add_argument("--validate", action="store_true", help="parse SDBF file to check if it is valid")
+    ap.add_argument("--index", action="store_true", help="generate indexes while hashing (needs -o)")
     ap.add_argument("--index-search", default=None, metavar="DIR",
                     help="search directory of reference indexes (block mode)")
     ap.add_argument("--version", action="store_true")
@@ -239,8 +305,23 @@ def main(argv=None) -> int:
             print(f"contains {sum(x.filter_count() for x in s.items)} bloom filters.")
             print(f"{s.input_size()} total data size. ")
         return 0
+    if a.index and not a.output:
+        print("sdhash:  ERROR: indexing requires output base filename ", file=sys.stderr)
+        return -1
     ctx = g.default_context()
     seg = a.segment_size * MB
+    if a.index:
+        inputs = a.files
+        if a.target_list:
+            inputs = []
+            for lst in a.files:
+                with open(lst) as f:
+                    inputs += [ln.rstrip("\n") for ln in f if ln.strip()]
+        files = _collect(inputs, a.deep)
+        # sdhash.cc:556-561: the small list, then the large one, each from k = 0
+        _index_files(ctx, [f for f in files if os.path.getsize(f) < 16 * MB], a.output, seg)
+        _index_files(ctx, [f for f in files if os.path.getsize(f) >= 16 * MB], a.output, 128 * MB)
+        return 0
     indexes = None
     if a.index_search is not None:
         if block_kb == 0:

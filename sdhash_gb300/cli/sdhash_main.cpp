@@ -12,8 +12,11 @@
 //             against every digest of the second;
 //   --index-search DIR   block-mode hashing looked up in DIR's index files.
 //
+//   --index   an index per group of files, as the reference builds them
+//             with one thread.
+//
 // Not offered: -s (filter sampling seeds rand() from time() in the
-// reference), --large, --index, --details.
+// reference), --large, --details.
 #include <dirent.h>
 #include <sys/stat.h>
 
@@ -42,7 +45,7 @@ struct Options {
     bool validate = false, version = false, help = false;
     int threshold = 1, block_kb = -1, sample = 0, segment_mb = 128;
     std::string output, separator = "pipe", hash_name, index_search;
-    bool have_index_search = false;
+    bool have_index_search = false, index = false;
     std::vector<std::string> files;
 };
 
@@ -67,6 +70,7 @@ void usage(std::ostream& os) {
        << "  --hash-name arg            set name of hash on stdin\n"
        << "  --fast                     shrink sdbf filters for speedup\n"
        << "  --validate                 parse SDBF file to check if it is valid\n"
+       << "  --index                    generate indexes while hashing (needs -o)\n"
        << "  --index-search arg         search directory of reference indexes\n"
        << "  --version                  show version info\n"
        << "  -h [ --help ]              produce help message\n";
@@ -97,6 +101,7 @@ Options parse_args(int argc, char** argv) {
         else if (a == "-g" || a == "--gen-compare") o.gen_compare = true;
         else if (a == "--fast") o.fast = true;
         else if (a == "--validate") o.validate = true;
+        else if (a == "--index") o.index = true;
         else if (a == "--version") o.version = true;
         else if (a == "-h" || a == "--help") o.help = true;
         else if (a == "-t" || key == "--threshold") o.threshold = to_int(value(i, "threshold"), "threshold");
@@ -475,6 +480,85 @@ std::string index_results(const std::vector<Digest>& ds, const std::vector<std::
     return out;
 }
 
+// hash_index_stringlist (sdhash-src/sdhash_threads.cc:376-470) for one of
+// the small / large file lists: groups of just over 640 MiB, each hashed
+// with a fresh 64 MiB index (small files in stream mode, large ones in
+// 16 KiB block mode with 128 MiB segments) and written as <out><k>.sdbf
+// and <out><k>.sdbf.idx, k from 0.  The reference's file-list array is
+// reproduced as it behaves: after a group its count restarts at 1, so every
+// later group also hashes the file left in slot 0; its running size is a C
+// int, which wraps modulo 2^32 (a file of 2 GiB or more makes it negative).
+void index_files(sdbfg_ctx* c, const std::vector<std::string>& files, const std::string& out, bool large) {
+    std::vector<std::string> slots;
+    size_t filect = 0;
+    int32_t total = 0;
+    int count = 0;
+    for (size_t i = 0; i < files.size(); i++) {
+        if (filect < slots.size()) slots[filect] = files[i];
+        else slots.push_back(files[i]);
+        total = (int32_t)((uint32_t)total + (uint32_t)file_size(files[i]));
+        if (total > (int32_t)(640 * kMB) || i + 1 == files.size()) {
+            std::vector<Input> in;
+            for (size_t k = 0; k <= filect; k++) {
+                std::vector<uint8_t> b = read_file(slots[k]);
+                if (large) {
+                    segment_inputs(slots[k], b, 128 * kMB, in);
+                } else {
+                    Input x{slots[k], std::move(b), 0};
+                    x.read = x.data.size();
+                    in.push_back(std::move(x));
+                }
+            }
+            const uint32_t dd = large ? 16 * (uint32_t)kKB : 0u;
+            const uint32_t n = (uint32_t)in.size();
+            std::vector<uint64_t> offs(n), lens(n);
+            uint64_t tot = 0;
+            for (uint32_t j = 0; j < n; j++) {
+                offs[j] = tot;
+                lens[j] = in[j].data.size();
+                tot += (lens[j] + 15) & ~15ull;
+            }
+            std::vector<uint8_t> data(std::max<uint64_t>(16, tot), 0);
+            for (uint32_t j = 0; j < n; j++) std::copy(in[j].data.begin(), in[j].data.end(), data.begin() + offs[j]);
+            const uint64_t cap = sdbfg_digest_capacity(lens.data(), n, dd);
+            std::vector<uint8_t> filters(std::max<uint64_t>(1, cap) * 256), bits(64 * kMB, 0);
+            std::vector<uint16_t> counts(std::max<uint64_t>(1, cap));
+            std::vector<sdbfg_digest_result> res(n);
+            uint64_t elem = 0;
+            check(c, sdbfg_digest_batch_index(c, data.data(), offs.data(), lens.data(), n, dd, filters.data(), cap,
+                                              counts.data(), res.data(), bits.data(), bits.size(), &elem),
+                  "index");
+            std::string text;
+            for (uint32_t j = 0; j < n; j++) {
+                if (res[j].status != SDBFG_DIGEST_OK || in[j].read < kMinFile) continue;
+                Digest d;
+                d.name = in[j].name;
+                d.bf_count = res[j].bf_count;
+                d.orig_size = in[j].read;
+                d.dd_block = dd;
+                d.max_elem = dd ? 192 : 160;
+                d.last_count = dd ? 0 : res[j].last_count;
+                const uint64_t o = res[j].filter_offset;
+                d.filters.assign(filters.begin() + o * 256, filters.begin() + (o + d.bf_count) * 256);
+                if (dd) d.elem_counts.assign(counts.begin() + o, counts.begin() + o + d.bf_count);
+                text += to_text(d);
+            }
+            const std::string name = out + std::to_string(count) + ".sdbf";
+            std::ofstream f(name, std::ios::binary);
+            if (!f) die("cannot write to file " + name);
+            f << text;
+            f.close();
+            if (sdbfg_index_write_file((name + ".idx").c_str(), bits.data(), bits.size(), elem, 5, name.c_str()) !=
+                SDBFG_OK)
+                die("cannot write to file " + name + ".idx");
+            count++;
+            total = 0;
+            filect = 0;
+        }
+        filect++;
+    }
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -558,6 +642,28 @@ int main(int argc, char** argv) {
             std::cout << bytes << " total data size. " << std::endl;
             sdbfg_set_free(s);
         }
+        sdbfg_ctx_destroy(c);
+        return 0;
+    }
+    if (o.index) {
+        if (o.output.empty()) {
+            std::cerr << "sdhash:  ERROR: indexing requires output base filename " << std::endl;
+            return -1;
+        }
+        std::vector<std::string> inputs = o.files;
+        if (o.target_list) {
+            inputs.clear();
+            for (const auto& lst : o.files) {
+                std::ifstream f(lst);
+                std::string ln;
+                while (std::getline(f, ln))
+                    if (ln.find_first_not_of(" \t\r\n") != std::string::npos) inputs.push_back(ln);
+            }
+        }
+        std::vector<std::string> small, large;
+        for (const auto& f : collect(inputs, o.deep)) (file_size(f) < 16 * kMB ? small : large).push_back(f);
+        index_files(c, small, o.output, false);  // sdhash.cc:556-561: small, then large, each from k = 0
+        index_files(c, large, o.output, true);
         sdbfg_ctx_destroy(c);
         return 0;
     }

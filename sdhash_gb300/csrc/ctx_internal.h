@@ -127,6 +127,10 @@ struct sdbfg_ctx {
     uint32_t* probe_words = nullptr;
     uint8_t* probe_counts = nullptr;
     DevBuf d_probes, d_nprobes, d_hits, d_index_tab;
+    // index build: counted features of the group being digested (block
+    // mode), the index bits, the first setter of every bit, the new-insert count
+    uint32_t* feat_words = nullptr;
+    DevBuf d_feats, d_idx_bits, d_idx_first, d_idx_count;
 };
 
 // A resident index filter (bloom_filter of an index file).
@@ -137,6 +141,16 @@ struct sdbfg_index {
     std::string name;
     DevBuf d_bits;
 };
+
+// Block-mode index build over one launch group's slots [0, nslots) (global
+// slots from slot0): each bit's first setter in input order, then the bits
+// and the count of features that set a new one (bloom_filter::insert_sha1
+// in that order, bloom_filter.cc:333-359).
+int index_build_group(sdbfg_ctx* c, const uint32_t* d_feats, const uint16_t* d_counts, uint64_t nslots,
+                      uint64_t slot0, uint32_t mask, uint32_t* d_first, uint32_t* d_bits,
+                      unsigned long long* d_count, cudaStream_t st);
+// first[p] = 0 for bits already set, ~0 otherwise.
+int index_first_init(sdbfg_ctx* c, const uint32_t* d_bits, uint32_t* d_first, uint64_t nbits, cudaStream_t st);
 
 // Hits of every probe slot against every index (k_index_query).
 int index_query(sdbfg_ctx* c, const uint32_t* d_probes, const uint8_t* d_nprobes, uint64_t nslots,

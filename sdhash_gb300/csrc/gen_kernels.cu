@@ -706,12 +706,21 @@ __device__ __forceinline__ void stage_tile(uint32_t (*buf)[kTileCap], const uint
 // whose 17-bit values need an exact comparison (register shuffles).  Bits
 // are written only for lanes up to the first roll-over, which is found
 // before anything is written; later lanes are re-run against the new state.
-__global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P) {
-    extern __shared__ __align__(16) uint8_t smem[];
+//
+// With an index being built (kIdx, sdhash --index: sdbf_core.cc:108-114),
+// a feature whose filter insert set a new bit is inserted into the index
+// and is skipped unless that set a new index bit -- so each file depends on
+// every earlier file's features.  One warp then commits all files in input
+// order, one feature at a time (lane 0), the index in global memory.
+template <bool kIdx>
+__device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) {
     const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (kIdx && (blockIdx.x != 0 || wid != 0)) return;
     CommitSmem& S = reinterpret_cast<CommitSmem*>(smem)[wid];
     for (uint32_t i = lane; i < 2048; i += 32) S.own[i] = 0;
-    for (uint32_t fi = blockIdx.x * kCommitWarps + wid; fi < P.nfiles; fi += gridDim.x * kCommitWarps) {
+    const uint32_t fstep = kIdx ? 1u : gridDim.x * kCommitWarps;
+    constexpr uint32_t kGroup = kIdx ? 1u : 32u;
+    for (uint32_t fi = kIdx ? 0u : blockIdx.x * kCommitWarps + wid; fi < P.nfiles; fi += fstep) {
         const uint32_t file = P.file_order[fi];
         const GenFile Fd = P.files[file];
         if (Fd.nchunks == 0) continue;
@@ -750,13 +759,14 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                 stage_tile(S.feat[cur ^ 1u], P.features + (size_t)(t + 1) * 5 * kTileCap, nf_next, lane);
             nf_cur = nf_next;
             nf_next = t + 2 < t_end ? P.tile_out[t + 2].count : 0;
-            for (uint32_t g0 = 0; g0 < nf; g0 += 32) {
-                const uint32_t gi = g0 + lane;
-                const bool have = gi < nf;
-                uint32_t a[5], b[5];
+            for (uint32_t g0 = 0; g0 < nf; g0 += kGroup) {
+                const uint32_t gi = g0 + (kIdx ? 0u : lane);
+                const bool have = gi < nf && (!kIdx || lane == 0);
+                uint32_t a[5], b[5], hw[5];
 #pragma unroll
                 for (int k = 0; k < 5; k++) {
                     const uint32_t h = have ? S.feat[cur][k][gi] : 0u;
+                    hw[k] = h;
                     a[k] = h & kBfMask;
                     b[k] = h & kBigMask;
                 }
@@ -793,6 +803,20 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                     for (int k = 0; k < 5; k++)
                         if (act && !((fpre >> k) & 1u) && (uint32_t)(__ffs(m[k]) - 1) == lane) fpass = true;
                     const uint32_t fmask = __ballot_sync(0xffffffffu, fpass);
+                    // index (kIdx): insert_sha1 of the filter-passing feature; it
+                    // goes on only if that set a new index bit
+                    bool inew = true;
+                    if (kIdx) {
+                        inew = false;
+                        if (fpass) {
+#pragma unroll
+                            for (int k = 0; k < 5; k++) {
+                                const uint32_t pos = hw[k] & P.index_mask, bit = 1u << (pos & 31);
+                                if (!(atomicOr(P.index_bits + (pos >> 5), bit) & bit)) inew = true;
+                            }
+                            if (inew) atomicAdd(P.index_new, 1ull);
+                        }
+                    }
                     // big filter: new iff unset before the group and no earlier
                     // filter-passing lane holds the same 17-bit value
                     uint32_t gnew = 0, pend = 0;
@@ -800,7 +824,7 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
 #pragma unroll
                     for (int k = 0; k < 5; k++) {
                         cand[k] = m[k] & fmask & lanemask_lt();
-                        if (fpass && !((gpre >> k) & 1u)) {
+                        if (fpass && inew && !((gpre >> k) & 1u)) {
                             if (cand[k]) pend |= 1u << k;
                             else gnew |= 1u << k;
                         }
@@ -831,7 +855,7 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
                             }
                         }
                     }
-                    const bool counted = fpass && gnew != 0;
+                    const bool counted = fpass && inew && gnew != 0;
                     const uint32_t cm = __ballot_sync(0xffffffffu, counted);
                     const uint32_t before = __popc(cm & lanemask_le());
                     const bool hit_small = counted && (last_count + before == (uint32_t)kMaxElem);
@@ -843,7 +867,7 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
 #pragma unroll
                         for (int k = 0; k < 5; k++) {
                             atomicOr(&S.F[a[k] >> 5], 1u << (a[k] & 31));
-                            if (fpass) atomicOr(&S.G[b[k] >> 5], 1u << (b[k] & 31));
+                            if (fpass && inew) atomicOr(&S.G[b[k] >> 5], 1u << (b[k] & 31));
                         }
                     }
                     __syncwarp();
@@ -902,6 +926,16 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P
         }
         __syncwarp();
     }
+}
+
+__global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    commit_files<false>(P, smem);
+}
+
+__global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit_index(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    commit_files<true>(P, smem);
 }
 
 // ------------------------------------------------------------ block mode
@@ -993,6 +1027,11 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
                         filt[idx >> 5] |= bit;
                     }
                     if (!added) continue;
+                    if (P.feats) {  // index build: every counted feature (sdbf_core.cc:164-167)
+                        uint32_t* fw = P.feats + (size_t)C.filter * kFeatWords + hashed * 5;
+#pragma unroll
+                        for (int z = 0; z < 5; z++) fw[z] = hsh[q][z];
+                    }
                     if (P.probes && (hashed & 3) == 0) {  // index search sample (sdbf_core.cc:168-175)
                         uint32_t* pr = P.probes + (size_t)C.filter * kProbeWords + (hashed >> 2) * 5;
 #pragma unroll
@@ -1043,6 +1082,13 @@ cudaError_t launch_stream_check(const GenParams& P, uint32_t grid, cudaStream_t 
 cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st) {
     set_stream_attrs();
     k_stream_fix<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_commit_index(const GenParams& P, cudaStream_t st) {
+    cudaFuncSetAttribute(k_stream_commit_index, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(CommitSmem) * kCommitWarps));
+    k_stream_commit_index<<<1, kCommitWarps * 32, sizeof(CommitSmem) * kCommitWarps, st>>>(P);
     return cudaGetLastError();
 }
 

@@ -88,11 +88,20 @@ struct GenParams {
     // null = no search
     uint32_t* probes;
     uint8_t* nprobes;
+    // index build: stream mode inserts into index_bits (mask index_mask) and
+    // counts the inserts that set a new bit in *index_new; block mode
+    // records every counted feature's SHA-1 words in feats ([slot][kFeatWords])
+    uint32_t* index_bits;
+    uint32_t index_mask;
+    unsigned long long* index_new;
+    uint32_t* feats;
 };
 
 // Index search samples counted features 0, 4, 8, ... of a block
 // (sdbf_core.cc:168-175): at most 192 / 4 = 48, five words each.
 constexpr uint32_t kProbeWords = 48 * 5;
+// Index build in block mode: up to 192 counted features per block, five words each.
+constexpr uint32_t kFeatWords = 192 * 5;
 
 // Phase counters (cycles summed over CTAs / warps) when GenParams::phase is set.
 enum : int {
@@ -106,6 +115,8 @@ cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t 
 cudaError_t launch_stream_check(const GenParams& P, uint32_t grid, cudaStream_t st);  // 4 chunks per CTA
 cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st);
 cudaError_t launch_stream_commit(const GenParams& P, uint32_t grid, cudaStream_t st);
+// One warp, files in file_order, index inserts (GenParams::index_bits).
+cudaError_t launch_stream_commit_index(const GenParams& P, cudaStream_t st);
 cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st);
 
 }  // namespace sdbfg

@@ -40,7 +40,7 @@ long lz4_decode_block(const uint8_t* in, size_t in_len, uint8_t* out, size_t out
     const uint8_t* const iend = in + in_len;
     uint8_t* op = out;
     uint8_t* const oend = out + out_len;
-    if (out_len == 0) return 0;
+    if (out_len == 0 && in_len == 0) return 0;
     while (ip < iend) {
         const uint32_t token = *ip++;
         size_t lit = token >> 4;
@@ -77,6 +77,62 @@ long lz4_decode_block(const uint8_t* in, size_t in_len, uint8_t* out, size_t out
         op += mlen;
     }
     return -1;
+}
+
+// LZ4 block encode (the published block format): greedy matches of at
+// least 4 bytes found through a hash table of 4-byte sequences, offsets up
+// to 65,535; the format's end rules are kept (the last 5 bytes are
+// literals, no match starts in the last 12).  Any LZ4 decoder reads it.
+void lz4_put_len(std::vector<uint8_t>& out, size_t v) {
+    while (v >= 255) {
+        out.push_back(255);
+        v -= 255;
+    }
+    out.push_back((uint8_t)v);
+}
+
+void lz4_encode_block(const uint8_t* in, size_t n, std::vector<uint8_t>& out) {
+    out.clear();
+    auto read32 = [&](size_t i) {
+        uint32_t v;
+        memcpy(&v, in + i, 4);
+        return v;
+    };
+    auto emit = [&](size_t anchor, size_t lit_end, size_t off, size_t mlen) {
+        const size_t lit = lit_end - anchor;
+        const size_t ml = mlen ? mlen - 4 : 0;
+        uint8_t token = (uint8_t)((lit >= 15 ? 15 : lit) << 4);
+        if (mlen) token |= (uint8_t)(ml >= 15 ? 15 : ml);
+        out.push_back(token);
+        if (lit >= 15) lz4_put_len(out, lit - 15);
+        out.insert(out.end(), in + anchor, in + lit_end);
+        if (!mlen) return;
+        out.push_back((uint8_t)(off & 0xFF));
+        out.push_back((uint8_t)(off >> 8));
+        if (ml >= 15) lz4_put_len(out, ml - 15);
+    };
+    size_t anchor = 0;
+    if (n >= 13) {
+        std::vector<uint32_t> table(1u << 16, 0xFFFFFFFFu);
+        const size_t mflimit = n - 12, matchlimit = n - 5;
+        size_t ip = 0;
+        while (ip < mflimit) {
+            const uint32_t seq = read32(ip);
+            const uint32_t h = (seq * 2654435761u) >> 16;
+            const uint32_t ref = table[h];
+            table[h] = (uint32_t)ip;
+            if (ref != 0xFFFFFFFFu && ip - ref <= 65535 && read32(ref) == seq) {
+                size_t len = 4;
+                while (ip + len < matchlimit && in[ref + len] == in[ip + len]) len++;
+                emit(anchor, ip, ip - ref, len);
+                ip += len;
+                anchor = ip;
+            } else {
+                ip++;
+            }
+        }
+    }
+    emit(anchor, n, 0, 0);  // the last literals
 }
 
 bool parse_u64(const std::string& s, uint64_t* v) {
@@ -176,6 +232,77 @@ int index_query(sdbfg_ctx* c, const uint32_t* d_probes, const uint8_t* d_nprobes
     return SDBFG_OK;
 }
 
+// ------------------------------------------------------ block-mode build
+// Exact in input order without a sequential pass: a feature set a new bit
+// iff it is the first setter (smallest ordinal) of one of its bits.
+// Ordinal = (global slot + 1) << 8 | feature index (bits set before the
+// batch have first setter 0).
+
+__global__ void k_index_first_init(const uint32_t* __restrict__ bits, uint32_t* __restrict__ first, uint64_t nbits) {
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nbits; p += (uint64_t)gridDim.x * blockDim.x)
+        first[p] = ((bits[p >> 5] >> (p & 31)) & 1u) ? 0u : 0xFFFFFFFFu;
+}
+
+__global__ void k_index_first(const uint32_t* __restrict__ feats, const uint16_t* __restrict__ counts, uint64_t nslots,
+                              uint64_t slot0, uint32_t mask, uint32_t* __restrict__ first) {
+    const uint64_t n = nslots * 192;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = i / 192;
+        const uint32_t k = (uint32_t)(i % 192);
+        if (k >= counts[s]) continue;
+        const uint32_t ord = (uint32_t)((slot0 + s + 1) << 8) | k;
+        const uint32_t* w = feats + s * kFeatWords + k * 5;
+#pragma unroll
+        for (int z = 0; z < 5; z++) atomicMin(first + (w[z] & mask), ord);
+    }
+}
+
+__global__ void k_index_mark(const uint32_t* __restrict__ feats, const uint16_t* __restrict__ counts, uint64_t nslots,
+                             uint64_t slot0, uint32_t mask, const uint32_t* __restrict__ first,
+                             uint32_t* __restrict__ bits, unsigned long long* __restrict__ count) {
+    const uint64_t n = nslots * 192;
+    uint32_t mine = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = i / 192;
+        const uint32_t k = (uint32_t)(i % 192);
+        if (k >= counts[s]) continue;
+        const uint32_t ord = (uint32_t)((slot0 + s + 1) << 8) | k;
+        const uint32_t* w = feats + s * kFeatWords + k * 5;
+        bool fresh = false;
+#pragma unroll
+        for (int z = 0; z < 5; z++) {
+            const uint32_t pos = w[z] & mask;
+            fresh |= first[pos] == ord;
+            atomicOr(bits + (pos >> 5), 1u << (pos & 31));
+        }
+        mine += fresh;
+    }
+    for (int d = 16; d > 0; d >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, d);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(count, (unsigned long long)mine);
+}
+
+int index_first_init(sdbfg_ctx* c, const uint32_t* d_bits, uint32_t* d_first, uint64_t nbits, cudaStream_t st) {
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nbits + 255) / 256, (uint64_t)c->sms * 32);
+    TIMED_LAUNCH_ON(c, "k_index_first_init", st,
+                    (k_index_first_init<<<grid, 256, 0, st>>>(d_bits, d_first, nbits), cudaGetLastError()));
+    return SDBFG_OK;
+}
+
+int index_build_group(sdbfg_ctx* c, const uint32_t* d_feats, const uint16_t* d_counts, uint64_t nslots,
+                      uint64_t slot0, uint32_t mask, uint32_t* d_first, uint32_t* d_bits,
+                      unsigned long long* d_count, cudaStream_t st) {
+    if (!nslots) return SDBFG_OK;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nslots * 192 + 255) / 256, (uint64_t)c->sms * 32);
+    TIMED_LAUNCH_ON(c, "k_index_first", st,
+                    (k_index_first<<<grid, 256, 0, st>>>(d_feats, d_counts, nslots, slot0, mask, d_first),
+                     cudaGetLastError()));
+    TIMED_LAUNCH_ON(c, "k_index_mark", st,
+                    (k_index_mark<<<grid, 256, 0, st>>>(d_feats, d_counts, nslots, slot0, mask, d_first, d_bits,
+                                                        d_count),
+                     cudaGetLastError()));
+    return SDBFG_OK;
+}
+
 // ------------------------------------------------------------------ C ABI
 
 extern "C" int sdbfg_index_create(sdbfg_ctx* c, const uint8_t* bits, uint64_t bf_size, uint32_t hash_count,
@@ -255,4 +382,26 @@ extern "C" int64_t sdbfg_lz4_decode(const uint8_t* in, uint64_t in_len, uint8_t*
     if ((!in && in_len) || (!out && out_len)) return SDBFG_ERR_ARG;
     const long r = lz4_decode_block(in, in_len, out, out_len);
     return r < 0 ? SDBFG_ERR_FORMAT : r;
+}
+
+extern "C" int64_t sdbfg_lz4_encode(const uint8_t* in, uint64_t in_len, uint8_t* out, uint64_t out_cap) {
+    if (!in && in_len) return SDBFG_ERR_ARG;
+    std::vector<uint8_t> enc;
+    lz4_encode_block(in, in_len, enc);
+    if (out && enc.size() <= out_cap) memcpy(out, enc.data(), enc.size());
+    return (int64_t)enc.size();
+}
+
+extern "C" int sdbfg_index_write_file(const char* path, const uint8_t* bits, uint64_t bf_size, uint64_t elem_count,
+                                      uint32_t hash_count, const char* set_name) {
+    if (!path || !bits || bf_size < 64 || (bf_size & (bf_size - 1))) return SDBFG_ERR_ARG;
+    std::vector<uint8_t> enc;
+    lz4_encode_block(bits, bf_size, enc);
+    FILE* f = fopen(path, "wb");
+    if (!f) return SDBFG_ERR_ARG;  // bloom_filter::write_out returns -2
+    const int ok = fprintf(f, "sdbf-idx:%llu:%llu:%u:%llu:%llu:%s\n", (unsigned long long)bf_size,
+                           (unsigned long long)elem_count, hash_count, (unsigned long long)mask_for_size(bf_size),
+                           (unsigned long long)enc.size(), set_name ? set_name : "") > 0 &&
+                   fwrite(enc.data(), 1, enc.size(), f) == enc.size();
+    return (fclose(f) == 0 && ok) ? SDBFG_OK : SDBFG_ERR_ARG;
 }

@@ -278,6 +278,7 @@ static int digest_group_device(sdbfg_ctx* c, const uint8_t* dev_base, const std:
         P.out_counts = dev_counts;
         P.probes = c->probe_words;
         P.nprobes = c->probe_counts;
+        P.feats = c->feat_words;
         P.block_lmax = (lmax + 63) / 64 * 64;
         const uint32_t grid = (uint32_t)std::min<size_t>(chunks.size(), (size_t)c->sms * 2 * 8);
         TIMED_LAUNCH(c, "k_block_digest", launch_block(P, grid, st));
@@ -354,18 +355,30 @@ static int ensure_pipeline(sdbfg_ctx* c) {
 // groups alternate between two streams with their own workspaces, so the
 // commit of one group overlaps the tiles (and the input copy) of the next;
 // the host synchronises once, at the end.
+// An index being built alongside (sdhash --index): device bits, bit mask,
+// counter of inserts that set a new bit.
+struct IndexBuild {
+    uint32_t* bits;
+    uint32_t mask;
+    unsigned long long* count;
+};
+
 static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const uint8_t* dev_data,
                                    const uint64_t* offsets_in, const uint64_t* lens_in, uint32_t n, uint32_t* dev_out,
-                                   uint64_t out_cap, sdbfg_digest_result* res, uint64_t* total_out) {
+                                   uint64_t out_cap, sdbfg_digest_result* res, uint64_t* total_out,
+                                   const IndexBuild* ib = nullptr) {
     int rc = ensure_pipeline(c);
     if (rc) return rc;
     // Launch groups are formed over the inputs sorted by size (largest first),
     // so the long ordered commits of the largest inputs start early and
     // overlap the rest of the batch; the packed output follows this order and
     // results[] records where each input's filters are.
+    // (an index build keeps input order: every file's digest depends on the
+    // index inserts of the files before it)
     std::vector<uint32_t> perm(n);
     std::iota(perm.begin(), perm.end(), 0u);
-    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) { return lens_in[a] > lens_in[b]; });
+    if (!ib)
+        std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) { return lens_in[a] > lens_in[b]; });
     std::vector<uint64_t> lens_v(n), offs_v(n);
     for (uint32_t i = 0; i < n; i++) {
         lens_v[i] = lens_in[perm[i]];
@@ -383,7 +396,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
     cudaEvent_t prev_scan = c->ev_start;
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
-        const int depth = std::max(1, std::min(c->depth, kSlots));
+        const int depth = ib ? 1 : std::max(1, std::min(c->depth, kSlots));
         sdbfg_ctx::Slot& S = c->slot[gi % depth];
         cudaStream_t st = S.stream;
         if (S.used) CUDA_TRY(c, cudaEventSynchronize(S.done));  // its pinned tables may be reused now
@@ -456,7 +469,9 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             hf[k] = f;
             ho[k] = k;
         }
-        std::stable_sort(ho, ho + g.count, [&](uint32_t a, uint32_t b) { return lens[g.first + a] > lens[g.first + b]; });
+        if (!ib)
+            std::stable_sort(ho, ho + g.count,
+                             [&](uint32_t a, uint32_t b) { return lens[g.first + a] > lens[g.first + b]; });
         CUDA_TRY(c, S.chunks.ensure(std::max<size_t>(1, tb_chunks)));
         CUDA_TRY(c, S.tiles.ensure(std::max<size_t>(1, tb_tiles)));
         CUDA_TRY(c, S.files.ensure(std::max<size_t>(1, tb_files)));
@@ -496,9 +511,16 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             TIMED_LAUNCH_ON(c, "k_stream_fix", st,
                             launch_stream_fix(P, std::min<uint32_t>(P.nchunks, cap_grid), st));
         }
-        TIMED_LAUNCH_ON(c, "k_stream_commit", st,
-                        launch_stream_commit(P, std::min<uint32_t>((g.count + kCommitWarps - 1) / kCommitWarps,
-                                                                   cap_grid), st));
+        if (ib) {
+            P.index_bits = ib->bits;
+            P.index_mask = ib->mask;
+            P.index_new = ib->count;
+            TIMED_LAUNCH_ON(c, "k_stream_commit_index", st, launch_stream_commit_index(P, st));
+        } else {
+            TIMED_LAUNCH_ON(c, "k_stream_commit", st,
+                            launch_stream_commit(P, std::min<uint32_t>((g.count + kCommitWarps - 1) / kCommitWarps,
+                                                                       cap_grid), st));
+        }
         // output slots follow input order: scan after the previous group's scan
         CUDA_TRY(c, cudaStreamWaitEvent(st, prev_scan, 0));
         TIMED_LAUNCH_ON(c, "k_scan_offsets", st,
@@ -599,7 +621,7 @@ extern "C" int sdbfg_digest_batch_device(sdbfg_ctx* c, const uint8_t* dev_data, 
 static int digest_block_host(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets, const uint64_t* lens,
                              uint32_t n, uint32_t dd, uint8_t* out_filters, uint16_t* out_counts,
                              sdbfg_digest_result* res, const sdbfg_index* const* indexes, uint32_t nidx,
-                             uint8_t* out_hits) {
+                             uint8_t* out_hits, const IndexBuild* ib = nullptr, uint32_t* d_first = nullptr) {
     cudaStream_t st = c->stream;
     cudaPointerAttributes attr{};
     const bool pinned = cudaPointerGetAttributes(&attr, host_data) == cudaSuccess &&
@@ -650,6 +672,10 @@ static int digest_block_host(sdbfg_ctx* c, const uint8_t* host_data, const uint6
             c->probe_words = c->d_probes.as<uint32_t>();
             c->probe_counts = c->d_nprobes.as<uint8_t>();
         }
+        if (ib) {
+            CUDA_TRY(c, c->d_feats.ensure(std::max<uint64_t>(1, group_slots) * kFeatWords * 4));
+            c->feat_words = c->d_feats.as<uint32_t>();
+        }
         // shift slots into the group-local output buffer
         std::vector<uint64_t> saved(g.count);
         for (uint32_t k = 0; k < g.count; k++) {
@@ -660,8 +686,14 @@ static int digest_block_host(sdbfg_ctx* c, const uint8_t* host_data, const uint6
                                      c->d_out_counts.as<uint16_t>(), res, &next, UINT64_MAX);
         c->probe_words = nullptr;
         c->probe_counts = nullptr;
+        c->feat_words = nullptr;
         for (uint32_t k = 0; k < g.count; k++) res[g.first + k].filter_offset = saved[k];
         if (rc) return rc;
+        if (ib && group_slots) {
+            rc = index_build_group(c, c->d_feats.as<uint32_t>(), c->d_out_counts.as<uint16_t>(), group_slots,
+                                   group_first_slot, ib->mask, d_first, ib->bits, ib->count, st);
+            if (rc) return rc;
+        }
         if (nidx && group_slots) {
             rc = index_query(c, c->d_probes.as<uint32_t>(), c->d_nprobes.as<uint8_t>(), group_slots, indexes, nidx,
                              c->d_hits.as<uint8_t>(), st);
@@ -706,6 +738,56 @@ extern "C" int sdbfg_digest_batch(sdbfg_ctx* c, const uint8_t* host_data, const 
         return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)total_slots);
     if (total_slots && !out_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
     return digest_block_host(c, host_data, offsets, lens, n, dd, out_filters, out_counts, res, nullptr, 0, nullptr);
+}
+
+extern "C" int sdbfg_digest_batch_index(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets,
+                                        const uint64_t* lens, uint32_t n, uint32_t dd, uint8_t* out_filters,
+                                        uint64_t out_cap, uint16_t* out_counts, sdbfg_digest_result* res,
+                                        uint8_t* index_bits, uint64_t index_bytes, uint64_t* elem_count) {
+    if (!index_bits || !elem_count) return SDBFG_ERR_ARG;
+    // a power-of-two filter of 64 bytes .. 512 MiB (bit positions fit 32 bits)
+    if (index_bytes < 64 || (index_bytes & (index_bytes - 1)) || index_bytes > (512ull << 20))
+        return fail(c, SDBFG_ERR_ARG, "index size must be a power of two from 64 bytes to 512 MiB");
+    int rc = validate_batch(c, offsets, lens, n, dd, res);
+    if (rc) return rc;
+    if (n && !host_data) return SDBFG_ERR_ARG;
+    CUDA_TRY(c, cudaSetDevice(c->device));
+    cudaStream_t st = c->stream;
+    const uint64_t nbits = index_bytes * 8;
+    CUDA_TRY(c, c->d_idx_bits.ensure(index_bytes));
+    CUDA_TRY(c, c->d_idx_count.ensure(8));
+    CUDA_TRY(c, cudaMemcpyAsync(c->d_idx_bits.p, index_bits, index_bytes, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(c, cudaMemsetAsync(c->d_idx_count.p, 0, 8, st));
+    const IndexBuild ib{c->d_idx_bits.as<uint32_t>(), (uint32_t)(nbits - 1), c->d_idx_count.as<unsigned long long>()};
+    if (!dd) {
+        uint64_t cap_needed = 0;
+        for (uint32_t i = 0; i < n; i++)
+            if (lens[i] >= kMinFile) cap_needed += stream_cap(lens[i]);
+        CUDA_TRY(c, c->d_out_filters.ensure(std::max<uint64_t>(1, cap_needed) * 256));
+        uint64_t total = 0;
+        rc = digest_stream_pipelined(c, host_data, nullptr, offsets, lens, n, c->d_out_filters.as<uint32_t>(),
+                                     std::min(cap_needed, out_cap), res, &total, &ib);
+        if (rc) return rc;
+        if (total) CUDA_TRY(c, cudaMemcpyAsync(out_filters, c->d_out_filters.p, total * 256, cudaMemcpyDeviceToHost, st));
+    } else {
+        const uint64_t total_slots = assign_block_slots(lens, n, dd, res);
+        if (total_slots > out_cap)
+            return fail(c, SDBFG_ERR_CAPACITY, "need %llu filter slots", (unsigned long long)total_slots);
+        if (total_slots && !out_counts) return fail(c, SDBFG_ERR_ARG, "block mode needs element-count output");
+        if ((total_slots + 1) >> 24) return fail(c, SDBFG_ERR_ARG, "index build: more than 2^24 blocks in one batch");
+        CUDA_TRY(c, c->d_idx_first.ensure(nbits * 4));
+        rc = index_first_init(c, ib.bits, c->d_idx_first.as<uint32_t>(), nbits, st);
+        if (rc) return rc;
+        rc = digest_block_host(c, host_data, offsets, lens, n, dd, out_filters, out_counts, res, nullptr, 0, nullptr,
+                               &ib, c->d_idx_first.as<uint32_t>());
+        if (rc) return rc;
+    }
+    unsigned long long added = 0;
+    CUDA_TRY(c, cudaMemcpyAsync(index_bits, c->d_idx_bits.p, index_bytes, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaMemcpyAsync(&added, c->d_idx_count.p, 8, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(c, cudaStreamSynchronize(st));
+    *elem_count += added;
+    return SDBFG_OK;
 }
 
 extern "C" int sdbfg_digest_batch_search(sdbfg_ctx* c, const uint8_t* host_data, const uint64_t* offsets,

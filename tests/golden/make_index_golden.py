@@ -10,6 +10,9 @@ filter), stored here gzip-compressed.  Then runs the reference's index
 search (sdhash --index-search idx, sdhash.cc:231-266 and 638-652) on five
 seeded query inputs in 16 KiB block mode and records index_results(), and
 records the sha256 of each index filter as the reference decompresses it.
+Also builds two more indexes from fresh (a stream-mode group whose later
+files repeat earlier ones, and a block-mode group) and records the set
+text, the index header and the filter's sha256 of each.
 
 Inputs are seeded synthetic mixture content (sdhash_gb300/synth.py), so the
 GPU tests regenerate them on any machine.
@@ -53,6 +56,19 @@ def queries():
             ("q2.bin", synth.random_bytes(93, 0, 50_000).tobytes()),
             ("q3.bin", a[0][1][:20_000] + b[0][1][130_000:170_000]),
             ("q4.bin", synth.random_bytes(93, 1, 700).tobytes())]
+
+
+def build_inputs():
+    """(name, bytes) groups indexed with sdhash --index's two paths: stream
+    mode (later files repeat parts of earlier ones, so the index drops their
+    features from their digests) and 16 KiB block mode."""
+    s0 = synth.mixture_bytes(94, 0, 120_000).tobytes()
+    s2 = synth.mixture_bytes(94, 2, 60_000).tobytes()
+    stream = [("s0.bin", s0), ("s1.bin", s0[20_000:100_000] + synth.random_bytes(94, 1, 30_000).tobytes()),
+              ("s2.bin", s2), ("s3.bin", s0), ("s4.bin", s2[:30_000] + s0[:30_000])]
+    b0 = synth.mixture_bytes(95, 0, 300_000).tobytes()
+    block = [("b0.bin", b0), ("b1.bin", b0[50_000:250_000] + synth.mixture_bytes(95, 1, 100_000).tobytes())]
+    return stream, block
 
 
 def _arr(items):
@@ -101,9 +117,24 @@ def main():
             head = raw[:raw.index(b"\n")].decode()
             rec["indexes"][s] = {"header": head, "filter_sha256": hashlib.sha256(bytes(buf)).hexdigest(),
                                  "filter_popcount": int(sum(bin(x).count("1") for x in bytes(buf) if x))}
-            with gzip.open(os.path.join(OUT, f"{s}.sdbf.idx.gz"), "wb", compresslevel=9) as f:
-                f.write(raw)
+            with open(os.path.join(OUT, f"{s}.sdbf.idx.gz"), "wb") as fo:
+                with gzip.GzipFile(fileobj=fo, mode="wb", compresslevel=9, mtime=0) as f:
+                    f.write(raw)
             shutil.copy(f"idx/{s}.sdbf", os.path.join(OUT, f"{s}.sdbf"))
+        # index builds (stream and block groups) from fresh indexes
+        rec["builds"] = []
+        for items, dd, stem in zip(build_inputs(), (0, 16384), ("S", "K")):
+            names, bufs, lens = _arr(items)
+            rc = L.ref_index_build(names, bufs, lens, len(items), dd, f"idx/{stem}.sdbf".encode(),
+                                   f"idx/{stem}.sdbf.idx".encode())
+            assert rc == 0, rc
+            raw = open(f"idx/{stem}.sdbf.idx", "rb").read()
+            buf = (C.c_ubyte * (64 << 20))()
+            assert L.ref_index_bits(f"idx/{stem}.sdbf.idx".encode(), buf, 64 << 20) == 64 << 20
+            rec["builds"].append({"stem": stem, "dd": dd, "names": [n for n, _ in items],
+                                  "header": raw[:raw.index(b"\n")].decode(),
+                                  "filter_sha256": hashlib.sha256(bytes(buf)).hexdigest(),
+                                  "sdbf_text": open(f"idx/{stem}.sdbf").read()})
         with open(os.path.join(OUT, "index_search.json"), "w") as f:
             json.dump(rec, f, indent=1)
         print(text)

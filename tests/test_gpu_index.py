@@ -109,3 +109,64 @@ def test_hits_match_oracle_dense_indexes(ctx, oracle):
         if d is not None:
             assert np.array_equal(h, w)
     assert sum(int((h > 4).sum()) for h in hits if h is not None) > 100
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["stream group", "block group"])
+def test_index_build_matches_reference(ctx, tmp_path, case):
+    """sdhash --index for one group: the digests (stream mode: features the
+    index already holds are dropped), the index bits and its element count
+    are the reference's; the index file written here decodes to the same
+    filter and carries the reference's header fields."""
+    import ctypes as C
+    import hashlib
+    import importlib.util
+    rec = _fixture()["builds"][case]
+    spec = importlib.util.spec_from_file_location("mkidx", os.path.join(os.path.dirname(GOLD), "make_index_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    items = m.build_inputs()[case]
+    bits = np.zeros(64 << 20, dtype=np.uint8)
+    digs, ec = ctx.digest_index([d for _, d in items], [n for n, _ in items], rec["dd"], bits)
+    assert "".join(d.to_string() for d in digs) == rec["sdbf_text"]
+    assert hashlib.sha256(bits.tobytes()).hexdigest() == rec["filter_sha256"]
+    head = rec["header"].split(":")
+    assert ec == int(head[2])
+    path = str(tmp_path / "x.sdbf.idx")
+    ctx.write_index(path, bits, ec, head[6])
+    raw = open(path, "rb").read()
+    nl = raw.index(b"\n")
+    mine = raw[:nl].decode().split(":")
+    assert mine[:5] == head[:5] and mine[6] == head[6]
+    x = ctx.load_index(path)
+    assert (x.bf_size, x.elem_count, x.hash_count, x.bit_mask) == (64 << 20, ec, 5, int(head[4]))
+    from sdhash_gb300 import lib
+    out = np.zeros(64 << 20, dtype=np.uint8)
+    assert lib().sdbfg_lz4_decode(raw[nl + 1:], len(raw) - nl - 1, out.ctypes.data, out.size) == int(mine[5])
+    assert np.array_equal(out, bits)
+
+
+def test_cli_index_matches_reference_group(ctx, tmp_path, monkeypatch):
+    """sdhash --index -o out <files>: the group's set file and index (bits,
+    element count, set name) as the reference builds them."""
+    import hashlib
+    import importlib.util
+    from sdhash_gb300 import cli, lib
+    rec = _fixture()["builds"][0]
+    spec = importlib.util.spec_from_file_location("mkidx", os.path.join(os.path.dirname(GOLD), "make_index_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    monkeypatch.chdir(tmp_path)
+    items = m.build_inputs()[0]
+    for n, d in items:
+        (tmp_path / n).write_bytes(d)
+    assert cli.main(["--index"] + [n for n, _ in items]) == -1      # needs -o
+    assert cli.main(["--index", "-o", "out"] + [n for n, _ in items]) == 0
+    assert (tmp_path / "out0.sdbf").read_text() == rec["sdbf_text"]
+    raw = (tmp_path / "out0.sdbf.idx").read_bytes()
+    nl = raw.index(b"\n")
+    head = raw[:nl].decode().split(":")
+    want = rec["header"].split(":")
+    assert head[:5] == want[:5] and head[6] == "out0.sdbf"
+    out = np.zeros(64 << 20, dtype=np.uint8)
+    assert lib().sdbfg_lz4_decode(raw[nl + 1:], len(raw) - nl - 1, out.ctypes.data, out.size) == int(head[5])
+    assert hashlib.sha256(out.tobytes()).hexdigest() == rec["filter_sha256"]

@@ -2,7 +2,7 @@
 sdhash_main.cpp) against the oracle and the reference's fixtures: digests
 (stream, block mode with segments and the zero-filled last segment, the
 16 MiB automatic block mode), -g, -c with one and two SDBF files, --fast,
--o, --validate and --index-search."""
+-o, --validate, --index-search and --index."""
 import gzip
 import json
 import os
@@ -105,3 +105,31 @@ def test_native_index_search(exe, tmp_path):
     rc, _, _ = run(exe, "--index-search", "idx", "-o", "res", *names, cwd=tmp_path)
     assert rc == 0
     assert sorted((tmp_path / "res.idx-result").read_text().splitlines()) == sorted(rec["results"].splitlines())
+
+
+def test_native_index_build(exe, tmp_path):
+    """--index -o out: the group's set file and index as the reference
+    builds them (the index file's compressed bytes are this library's)."""
+    import ctypes as C
+    import hashlib
+    import importlib.util
+    from sdhash_gb300 import lib
+    rec = json.load(open(os.path.join(GOLD, "index", "index_search.json")))["builds"][0]
+    spec = importlib.util.spec_from_file_location("mkidx", os.path.join(GOLD, "make_index_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    items = m.build_inputs()[0]
+    for n, d in items:
+        (tmp_path / n).write_bytes(d)
+    rc, _, err = run(exe, "--index", *[n for n, _ in items], cwd=tmp_path)
+    assert rc == 255 and "requires output base filename" in err
+    rc, _, _ = run(exe, "--index", "-o", "out", *[n for n, _ in items], cwd=tmp_path)
+    assert rc == 0 and (tmp_path / "out0.sdbf").read_text() == rec["sdbf_text"]
+    raw = (tmp_path / "out0.sdbf.idx").read_bytes()
+    nl = raw.index(b"\n")
+    head = raw[:nl].decode().split(":")
+    assert head[:5] == rec["header"].split(":")[:5] and head[6] == "out0.sdbf"
+    out = np.zeros(64 << 20, dtype=np.uint8)
+    L = lib()
+    assert L.sdbfg_lz4_decode(raw[nl + 1:], len(raw) - nl - 1, out.ctypes.data, out.size) == int(head[5])
+    assert hashlib.sha256(out.tobytes()).hexdigest() == rec["filter_sha256"]

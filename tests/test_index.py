@@ -86,3 +86,63 @@ def test_oracle_index_search_matches_reference(native, oracle):
                 if h[b, i] > 4:
                     lines.append(f"{n} [{b}] |idx/{s}.sdbf|{int(h[b, i])}\n")
     assert "".join(lines) == rec["results"]
+
+
+def test_lz4_encoder_round_trip(native):
+    """The index writer's LZ4 encoder against the decoder, on the reference's
+    index filters and on edge inputs (empty, short, runs, random)."""
+    native.sdbfg_lz4_encode.argtypes = [C.c_char_p, C.c_uint64, C.c_void_p, C.c_uint64]
+    native.sdbfg_lz4_encode.restype = C.c_int64
+    rng = np.random.default_rng(3)
+    samples = [b"", b"a", b"abcdefghijkl", b"x" * 13, bytes(100000), rng.bytes(70000),
+               bytes(rng.integers(0, 3, 50000, dtype=np.uint8))]
+    raw = gzip.open(os.path.join(GOLD, "A.sdbf.idx.gz")).read()
+    nl = raw.index(b"\n")
+    r, bits = _decode(native, raw[nl + 1:], 64 << 20)
+    samples.append(bits.tobytes())
+    for smp in samples:
+        n = native.sdbfg_lz4_encode(smp, len(smp), None, 0)
+        enc = np.zeros(max(1, n), dtype=np.uint8)
+        assert native.sdbfg_lz4_encode(smp, len(smp), enc.ctypes.data, n) == n
+        r, out = _decode(native, enc[:n].tobytes(), len(smp))
+        assert r == n and out.tobytes() == smp
+    assert n < len(samples[-1]) // 100   # a sparse 64 MiB filter compresses well
+
+
+def test_reference_reads_written_index(native, tmp_path):
+    """An index file written here is read by the reference's own
+    bloom_filter(string) to the same filter (needs the reference library
+    built from its sources; skipped where it is absent)."""
+    import hashlib
+    from oracle import REF_SO
+    if not os.path.exists(REF_SO):
+        pytest.skip("reference library not built here")
+    L = C.CDLL(REF_SO)
+    L.ref_index_bits.argtypes = [C.c_char_p, C.c_void_p, C.c_ulonglong]
+    L.ref_index_bits.restype = C.c_longlong
+    rec = _fixture()["indexes"]["B"]
+    raw = gzip.open(os.path.join(GOLD, "B.sdbf.idx.gz")).read()
+    nl = raw.index(b"\n")
+    r, bits = _decode(native, raw[nl + 1:], 64 << 20)
+    head = raw[:nl].decode().split(":")
+    native.sdbfg_index_write_file.argtypes = [C.c_char_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint32, C.c_char_p]
+    path = str(tmp_path / "mine.idx")
+    assert native.sdbfg_index_write_file(path.encode(), bits.ctypes.data, bits.size, int(head[2]), 5,
+                                         head[6].encode()) == 0
+    back = np.zeros(64 << 20, dtype=np.uint8)
+    assert L.ref_index_bits(path.encode(), back.ctypes.data, back.size) == 64 << 20
+    assert hashlib.sha256(back.tobytes()).hexdigest() == rec["filter_sha256"]
+
+
+def test_index_groups():
+    """--index groups (hash_index_stringlist, sdhash-src/sdhash_threads.cc:
+    402-411,446-455): a group closes past 640 MB or at the last file, slot 0
+    stays in every later group, and the running size wraps as a C int."""
+    from sdhash_gb300.cli import MB, _index_groups
+    assert _index_groups([]) == []
+    assert _index_groups([10 * MB] * 3) == [[0, 1, 2]]
+    assert _index_groups([600 * MB, 50 * MB, 10 * MB, 700 * MB, 1]) == [[0, 1], [0, 2, 3], [0, 4]]
+    assert _index_groups([641 * MB, 641 * MB, 641 * MB]) == [[0], [0, 1], [0, 2]]
+    # 3 GiB is negative as an int; 3 GiB + 100 MiB + 1 GiB wraps to 100 MiB
+    assert _index_groups([3 << 30, 100 * MB, 1 << 30, 5]) == [[0, 1, 2, 3]]
+    assert _index_groups([3 << 30, 2 << 30]) == [[0, 1]]
