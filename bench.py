@@ -62,11 +62,12 @@ def parse():
     ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
     ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve", "load", "index"],
+    ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve", "load", "index",
+                                                         "index-build"],
                     help="stream: bulk digest generation (headline); allpairs: batched uneven all-pairs compare; "
                          "image: block-mode disk image + query fragments compared against it; serve: continuous-batching "
                          "server under Poisson load; load: bulk SDBF text load into a resident set; index: "
-                         "block-mode index search")
+                         "block-mode index search; index-build: sdhash --index for one 640 MiB group")
     ap.add_argument("--image-gib", type=int, default=16, help="image: disk image size (GiB, multiple of 128 MiB)")
     ap.add_argument("--queries", type=int, default=100000, help="image: query fragments")
     ap.add_argument("--ref-filters", type=int, default=244 * 8192, help="serve: block filters in the reference set")
@@ -951,6 +952,196 @@ def main_index(args):
     return 0
 
 
+IB_METRIC = "index build input GB/s"
+IB_KERNELS = ("k_stream_tiles", "k_stream_check", "k_stream_fix", "k_stream_commit_round", "k_words_diff",
+              "k_index_first_init", "k_stream_index_first", "k_stream_index_mark", "k_stream_commit_index",
+              "k_scan_offsets", "k_pack_filters", "k_block_digest", "k_index_first", "k_index_mark")
+
+
+def index_group_sizes(seed: int, lo: int, hi: int):
+    """File sizes of one sdhash --index group: log-uniform lo..hi, up to the
+    first file that takes the running total past 640 MiB (the group's end,
+    sdhash_threads.cc:409,455)."""
+    from sdhash_gb300 import synth
+    sizes = synth.log_uniform_sizes(seed, 100000, lo, hi)
+    k = int(np.searchsorted(np.cumsum(sizes.astype(np.int64)), 640 << 20, side="right")) + 1
+    return sizes[:k]
+
+
+def main_index_build(args):
+    """sdhash --index on the GPU (sdbfg_digest_batch_index): one group of
+    files below 16 MiB (sizes log-uniform 4 KiB..16 MiB, mixture content,
+    just over 640 MiB -- the group sdhash --index closes) digested in stream
+    mode into a fresh 64 MiB index, from pinned host memory, the index bits
+    copied in and out.  Every file's digest depends on the index inserts of
+    the files before it; the engine runs fixed-point rounds of the parallel
+    commit (index_rounds).  value: summed device time of the call's kernels
+    (CUDA events); e2e: the whole call.  Also measured: the same group cut
+    from one shared 96 MiB pool (most features recur across files), the
+    sequential one-warp commit, and a block-mode group (16 KiB blocks,
+    64 MiB files).  cpu_baseline: the oracle's sequential index build (one
+    core, as the reference builds a group with -p 1) on the first files of
+    the group, which also checks the GPU's digests of those files."""
+    import ctypes as C
+    import torch
+    import sdhash_gb300 as g
+    from sdhash_gb300 import DigestResult, lib, synth, _ptr
+    torch.cuda.set_device(0)
+    ctx = g.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+
+    def group(sizes, fill):
+        sizes = np.ascontiguousarray(sizes, dtype=np.uint64)
+        offs, total = synth.packed_layout(sizes)
+        data = torch.empty(max(16, total), dtype=torch.uint8, pin_memory=True).numpy()
+        fill(data, offs, sizes)
+        return data, np.ascontiguousarray(offs, dtype=np.uint64), sizes, int(sizes.sum())
+
+    def fill_mixture(seed):
+        def f(data, offs, sizes):
+            synth.fill_many(seed, "mixture", sizes, out=data)
+        return f
+
+    def fill_pool(data, offs, sizes):
+        pool = synth.mixture_bytes(args.seed + 6100, 0, 96 << 20)
+        rng = np.random.default_rng(args.seed + 6100)
+        for k in range(len(sizes)):
+            n, o = int(sizes[k]), int(offs[k])
+            a = int(rng.integers(0, pool.size - n + 1))
+            data[o:o + n] = pool[a:a + n]
+            m = min(n, 8192)
+            data[o:o + m] = synth.random_bytes(args.seed + 6101, k, m)
+
+    bits_host = torch.empty(64 << 20, dtype=torch.uint8, pin_memory=True).numpy()
+
+    def runner(data, offs, lens, dd):
+        n = len(lens)
+        cap = ctx.capacity(lens, dd)
+        out_f = torch.empty(max(1, cap) * 256, dtype=torch.uint8, pin_memory=True).numpy()
+        out_c = np.zeros(max(1, cap), dtype=np.uint16)
+        res = (DigestResult * n)()
+        ec = np.zeros(1, dtype=np.uint64)
+
+        def call():
+            bits_host[:] = 0
+            ec[0] = 0
+            ctx._check(lib().sdbfg_digest_batch_index(ctx.h, data.ctypes.data, _ptr(offs), _ptr(lens), n, dd,
+                                                      out_f.ctypes.data, cap, out_c.ctypes.data, res,
+                                                      bits_host.ctypes.data, bits_host.size, _ptr(ec)))
+            return int(ec[0])
+        return call, res, out_f, cap
+
+    def wall_of(call, steps):
+        for _ in range(max(3, args.warmup)):
+            call()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            call()
+        return (time.perf_counter() - t0) / steps
+
+    sizes = index_group_sizes(args.seed + 6000, 4096, (16 << 20) - 1)
+    data, offs, lens, total = group(sizes, fill_mixture(args.seed + 6000))
+    call, res, out_f, cap = runner(data, offs, lens, 0)
+    for _ in range(max(3, args.warmup)):
+        call()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ec = call()
+    wall = (time.perf_counter() - t0) / args.steps
+    clocks.stop()
+    rounds = ctx.index_rounds
+    ctx.profile(True)
+    l0 = ctx.launch_count
+    for _ in range(args.steps):
+        call()
+    kern = {}
+    for k in IB_KERNELS:
+        ms, cnt = ctx.kernel_time(k)
+        if cnt:
+            kern[k] = ms / args.steps
+    launches = (ctx.launch_count - l0) // args.steps
+    ctx.profile(False)
+    dev_ms = sum(kern.values())
+    # the sequential commit on the same group
+    ctx.set_index_rounds(0)
+    wall_seq = wall_of(call, 1)
+    ctx.set_index_rounds(16)
+    # parity + CPU baseline: the oracle's sequential build of the first files
+    # (a prefix of the group has the same digests as in the whole group)
+    from oracle import Oracle
+    O = Oracle()
+    call()
+    pre = int(np.searchsorted(np.cumsum(lens.astype(np.int64)), int(args.cpu_sample_gib * 2 ** 30 / 24),
+                              side="right")) + 1
+    pre = min(pre, len(lens))
+    sample = [data[int(offs[k]):int(offs[k]) + int(lens[k])] for k in range(pre)]
+    obits = np.zeros(64 << 20, dtype=np.uint8)
+    t1 = time.perf_counter()
+    want, _ = O.index_build_stream(sample, [f"f{k}" for k in range(pre)], obits)
+    t_cpu = time.perf_counter() - t1
+    for k in range(pre):
+        w = want[k]
+        if w is None:
+            assert res[k].status != 0
+            continue
+        o, nb = int(res[k].filter_offset), int(res[k].bf_count)
+        assert (nb, int(res[k].last_count)) == (w.bf_count, w.last_count), f"index build: file {k} differs"
+        assert out_f[o * 256:(o + nb) * 256].tobytes() == w.filters(), f"index build: file {k} filters differ"
+    sample_bytes = int(lens[:pre].sum())
+    # shared-pool content: the same sizes, features recurring across files
+    pdata, poffs, plens, ptotal = group(sizes, fill_pool)
+    pcall, _, _, _ = runner(pdata, poffs, plens, 0)
+    pwall = wall_of(pcall, args.steps)
+    prounds = ctx.index_rounds
+    ctx.set_index_rounds(0)
+    pwall_seq = wall_of(pcall, 1)
+    ctx.set_index_rounds(16)
+    del pdata
+    # block-mode group: 64 MiB files
+    bsizes = np.full(11, 64 << 20, dtype=np.uint64)
+    bdata, boffs, blens, btotal = group(bsizes, fill_mixture(args.seed + 6200))
+    bcall, _, _, _ = runner(bdata, boffs, blens, 16384)
+    bwall = wall_of(bcall, args.steps)
+    del bdata
+    hbm, src = peaks()
+    tiles_ms = kern.get("k_stream_tiles", 0.0)
+    d2h = int(cap) * 256 + len(lens) * 24 + (64 << 20)
+    line = {"metric": IB_METRIC, "value": total / (dev_ms / 1e3) / 1e9, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": dev_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": "stream-mode index build (sdhash --index, one group)", "files": len(lens),
+                       "input_bytes": total, "sizes": "log-uniform 4 KiB..16 MiB, up to the file past 640 MiB",
+                       "content": "mixture, distinct per file", "index_bytes": 64 << 20,
+                       "l2": "inputs larger than L2 (no flush needed)"},
+            "gpu_launches": int(launches), "clocks": clocks.summary(), "index_rounds": rounds,
+            "elements_inserted": ec, "kernel_ms_per_step": kern,
+            "roofline": {"bound": "hbm", "kernel": "k_stream_tiles",
+                         "achieved": total / (tiles_ms / 1e3) / 1e9 if tiles_ms else None, "peak": hbm,
+                         "unit": "GB/s", "frac": total / (tiles_ms / 1e3) / 1e9 / hbm if tiles_ms else None,
+                         "traffic": None, "peak_source": f"{src} hbm_gbs (MEASURED_PEAKS.json)",
+                         "algorithmic_bytes_per_step": total},
+            "e2e": {"value": total / wall / 1e9, "unit": "GB/s", "h2d_bytes_per_step": total + (64 << 20),
+                    "d2h_bytes_per_step": d2h, "ms_per_step": wall * 1e3,
+                    "path": "sdbfg_digest_batch_index from pinned host memory"},
+            "sequential_commit_e2e": {"value": total / wall_seq / 1e9, "unit": "GB/s",
+                                      "path": "the same call with index rounds off (one-warp commit)"},
+            "shared_pool_e2e": {"value": ptotal / pwall / 1e9, "unit": "GB/s", "index_rounds": prounds,
+                                "sequential_commit": ptotal / pwall_seq / 1e9,
+                                "content": "files cut from one 96 MiB mixture pool (first 8 KiB fresh)"},
+            "block_group_e2e": {"value": btotal / bwall / 1e9, "unit": "GB/s", "files": len(blens),
+                                "input_bytes": btotal, "block": 16384},
+            "cpu_baseline": {"value": sample_bytes / t_cpu / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                             "sample": f"the group's first {pre} files ({sample_bytes} bytes), oracle index build",
+                             "seconds": round(t_cpu, 3)}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 LD_METRIC = "SDBF text loaded GB/s"
 
 
@@ -1045,6 +1236,8 @@ def main():
         return main_load(args)
     if args.workload == "index":
         return main_index(args)
+    if args.workload == "index-build":
+        return main_index_build(args)
     if args.workload == "serve":
         return main_serve(args)
     if args.workload == "image":

@@ -80,6 +80,14 @@ int sdbfg_ctx_set_lead(sdbfg_ctx *ctx, uint32_t steps);
 int sdbfg_ctx_set_pipeline_depth(sdbfg_ctx *ctx, int depth);
 /* Tiles whose speculative popularity chain was re-walked (instrumentation). */
 uint64_t sdbfg_ctx_relinked_tiles(sdbfg_ctx *ctx);
+/* Stream-mode index build (sdbfg_digest_batch_index with dd == 0): the
+ * number of parallel fixed-point rounds tried per launch group before the
+ * one-warp sequential commit takes over (default 16; 0 = sequential only).
+ * Results are exact either way.  sdbfg_ctx_index_rounds: rounds the last
+ * launch group took (0 = it ran the sequential commit).  No counterpart in
+ * the reference (its index build is sequential). */
+int sdbfg_ctx_set_index_rounds(sdbfg_ctx *ctx, uint32_t max_rounds);
+uint32_t sdbfg_ctx_index_rounds(sdbfg_ctx *ctx);
 
 /* ----------------------------------------------------- digest generation */
 typedef struct {

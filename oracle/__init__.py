@@ -130,6 +130,9 @@ class Oracle:
         L.orc_index_search_many.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_uint32, C.c_uint32,
                                             C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                             C.c_uint32, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int)]
+        L.orc_index_build_stream.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.POINTER(C.c_char_p),
+                                             C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64),
+                                             C.POINTER(_Digest), C.POINTER(C.c_int)]
         L.orc_b64_encode.argtypes = [C.c_char_p, C.c_size_t, C.c_char_p]
         L.orc_b64_encode.restype = C.c_size_t
 
@@ -267,12 +270,9 @@ class Oracle:
                 out.append(rows[i][:nb, :nidx])
         return out
 
-    def digest_many(self, bufs, dd_block_size: int = 0, nthreads: int = 0, names=None):
-        """Digest a list of bytes-like buffers on nthreads threads (file-parallel)."""
+    @staticmethod
+    def _buffers(bufs):
         n = len(bufs)
-        cnames = None
-        if names is not None:
-            cnames = (C.c_char_p * n)(*[x.encode() for x in names])
         ptrs = (C.c_void_p * n)()
         lens = (C.c_uint64 * n)()
         keep = []
@@ -284,6 +284,32 @@ class Oracle:
             else:  # numpy array
                 ptrs[i] = b.ctypes.data
             lens[i] = len(b)
+        return ptrs, lens, keep
+
+    def index_build_stream(self, bufs, names, index_bits, elem_count: int = 0):
+        """Stream-mode digests of one sdhash --index group, in order, with
+        the shared index index_bits (uint8 numpy array, power-of-two size,
+        updated in place).  Returns (digests, elem_count after the group)."""
+        import numpy as np
+        assert isinstance(index_bits, np.ndarray) and index_bits.dtype == np.uint8 and index_bits.flags.c_contiguous
+        n = len(bufs)
+        ptrs, lens, keep = self._buffers(bufs)
+        cnames = (C.c_char_p * n)(*[x.encode() for x in names])
+        outs = (_Digest * n)()
+        status = (C.c_int * n)()
+        ec = C.c_uint64(elem_count)
+        self.L.orc_index_build_stream(ptrs, lens, cnames, n, index_bits.ctypes.data, index_bits.size * 8 - 1,
+                                      C.byref(ec), outs, status)
+        del keep
+        return [OracleDigest(self.L, outs[i]) if status[i] == 0 else None for i in range(n)], int(ec.value)
+
+    def digest_many(self, bufs, dd_block_size: int = 0, nthreads: int = 0, names=None):
+        """Digest a list of bytes-like buffers on nthreads threads (file-parallel)."""
+        n = len(bufs)
+        cnames = None
+        if names is not None:
+            cnames = (C.c_char_p * n)(*[x.encode() for x in names])
+        ptrs, lens, keep = self._buffers(bufs)
         outs = (_Digest * n)()
         status = (C.c_int * n)()
         self.L.orc_digest_many(ptrs, lens, cnames, n, dd_block_size, nthreads, outs, status)

@@ -223,8 +223,40 @@ static char *dup_name(const char *name) {
     return s;
 }
 
+static int index_insert5(uint8_t *bits, uint32_t mask, const uint32_t h[5]) {
+    /* bloom_filter::insert_sha1 = query_and_set(mode_set=true),
+     * bloom_filter.cc:311-359: sets the probed bits; true iff one was new. */
+    int fresh = 0;
+    for (int i = 0; i < 5; i++) {
+        uint32_t pos = h[i] & mask;
+        uint8_t bit = (uint8_t)(1u << (pos & 7));
+        if (!(bits[pos >> 3] & bit)) fresh = 1;
+        bits[pos >> 3] |= bit;
+    }
+    return fresh;
+}
+
 /* ----------------------------------------------------------- stream mode */
+static int digest_stream(const char *name, const uint8_t *x, uint64_t len, uint8_t *index_bits, uint32_t index_mask,
+                         uint64_t *elem_count, orc_digest *d);
+
 int orc_digest_stream(const char *name, const uint8_t *x, uint64_t len, orc_digest *d) {
+    return digest_stream(name, x, len, NULL, 0, NULL, d);
+}
+
+int orc_index_build_stream(const uint8_t *const *bufs, const uint64_t *lens, const char *const *names, uint32_t n,
+                           uint8_t *index_bits, uint32_t index_mask, uint64_t *elem_count, orc_digest *outs,
+                           int *status) {
+    /* hash_index_stringlist's stream path for one group (sdhash_threads.cc:
+     * 402-416 with -p 1: sdbf_hash_files, :249-270): files in order, one
+     * shared index */
+    for (uint32_t i = 0; i < n; i++)
+        status[i] = digest_stream(names[i], bufs[i], lens[i], index_bits, index_mask, elem_count, &outs[i]);
+    return 0;
+}
+
+static int digest_stream(const char *name, const uint8_t *x, uint64_t len, uint8_t *index_bits, uint32_t index_mask,
+                         uint64_t *elem_count, orc_digest *d) {
     memset(d, 0, sizeof *d);
     if (len < ORC_MIN_FILE) return -3;
     d->name = dup_name(name);
@@ -256,6 +288,11 @@ int orc_digest_stream(const char *name, const uint8_t *x, uint64_t len, orc_dige
             uint32_t h[5];
             sha1_words(x + pos + i, h);
             if (bf_insert5(cur, h) == 0) continue;
+            /* with an index being built (sdbf_core.cc:108-114) */
+            if (index_bits) {
+                if (!index_insert5(index_bits, index_mask, h)) continue;
+                (*elem_count)++;
+            }
             if (!big_insert5(big, h)) continue;
             d->last_count++;
             bigfi++;

@@ -109,6 +109,12 @@ int orc_index_search_block(const char *name, const uint8_t *x, uint64_t len, uin
 void orc_index_search_many(const uint8_t *const *bufs, const uint64_t *lens, uint32_t n, uint32_t dd,
                            const uint8_t *const *bits, const uint32_t *masks, const uint32_t *hash_counts,
                            uint32_t nidx, int nthreads, uint8_t *const *hits, int *status);
+/* Stream-mode digests of one sdhash --index group (files in order, one
+ * shared index of bit mask index_mask; *elem_count counts the inserts that
+ * set a new bit).  status[i] as orc_digest_stream returns it. */
+int orc_index_build_stream(const uint8_t *const *bufs, const uint64_t *lens, const char *const *names, uint32_t n,
+                           uint8_t *index_bits, uint32_t index_mask, uint64_t *elem_count, orc_digest *outs,
+                           int *status);
 void orc_digest_many(const uint8_t *const *bufs, const uint64_t *lens, const char *const *names, uint32_t n,
                      uint32_t dd_block_size, int nthreads, orc_digest *outs, int *status);
 

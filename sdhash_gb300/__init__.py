@@ -96,6 +96,9 @@ def lib() -> C.CDLL:
         L.sdbfg_ctx_kernel_time.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         L.sdbfg_ctx_relinked_tiles.argtypes = [vp]
         L.sdbfg_ctx_relinked_tiles.restype = C.c_uint64
+        L.sdbfg_ctx_set_index_rounds.argtypes = [vp, C.c_uint32]
+        L.sdbfg_ctx_index_rounds.argtypes = [vp]
+        L.sdbfg_ctx_index_rounds.restype = C.c_uint32
         L.sdbfg_digest_capacity.argtypes = [u64p, C.c_uint32, C.c_uint32]
         L.sdbfg_digest_capacity.restype = C.c_uint64
         L.sdbfg_digest_batch.argtypes = [vp, vp, u64p, u64p, C.c_uint32, C.c_uint32, vp, C.c_uint64, vp,
@@ -393,6 +396,16 @@ class Context:
     @property
     def relinked_tiles(self) -> int:
         return int(lib().sdbfg_ctx_relinked_tiles(self.h))
+
+    def set_index_rounds(self, max_rounds: int):
+        """Stream-mode index build: parallel fixed-point rounds per launch
+        group before the sequential commit (0 = sequential only; exact either way)."""
+        self._check(lib().sdbfg_ctx_set_index_rounds(self.h, max_rounds))
+
+    @property
+    def index_rounds(self) -> int:
+        """Rounds the last stream-mode index launch group took (0: sequential commit)."""
+        return int(lib().sdbfg_ctx_index_rounds(self.h))
 
     # ------------------------------------------------------------ digests
     @staticmethod

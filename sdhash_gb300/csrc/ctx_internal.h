@@ -131,6 +131,11 @@ struct sdbfg_ctx {
     // mode), the index bits, the first setter of every bit, the new-insert count
     uint32_t* feat_words = nullptr;
     DevBuf d_feats, d_idx_bits, d_idx_first, d_idx_count;
+    // stream-mode index build: fixed-point rounds before the sequential
+    // commit takes over (0: sequential only), rounds the last launch group took
+    uint32_t index_max_rounds = 16;
+    uint32_t index_rounds_used = 0;
+    DevBuf d_seen[2], d_diff;
 };
 
 // A resident index filter (bloom_filter of an index file).

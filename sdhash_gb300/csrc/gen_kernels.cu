@@ -707,13 +707,25 @@ __device__ __forceinline__ void stage_tile(uint32_t (*buf)[kTileCap], const uint
 // are written only for lanes up to the first roll-over, which is found
 // before anything is written; later lanes are re-run against the new state.
 //
-// With an index being built (kIdx, sdhash --index: sdbf_core.cc:108-114),
-// a feature whose filter insert set a new bit is inserted into the index
-// and is skipped unless that set a new index bit -- so each file depends on
-// every earlier file's features.  One warp then commits all files in input
-// order, one feature at a time (lane 0), the index in global memory.
-template <bool kIdx>
+// With an index being built (sdhash --index: sdbf_core.cc:108-114), a
+// feature whose filter insert set a new bit is inserted into the index and
+// is skipped unless that set a new index bit -- so each file depends on
+// every earlier file's features.  Two ways to get that order:
+// * kCommitSeq: one warp commits all files in input order, one feature at
+//   a time (lane 0), the index in global memory;
+// * kCommitRound: one round of a fixed point.  Files commit in parallel; a
+//   feature is taken as setting a new index bit iff no feature inserted in
+//   the previous round precedes it as the first setter of one of its bits
+//   (GenParams::index_first), and the inserted features are recorded
+//   (GenParams::index_seen).  A round that inserts the same features as
+//   the previous one reproduces the sequential result: by induction over
+//   the input order, every decision then depends only on earlier decisions
+//   that already agree.
+enum : int { kCommitPlain = 0, kCommitSeq = 1, kCommitRound = 2 };
+
+template <int kMode>
 __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) {
+    constexpr bool kIdx = kMode == kCommitSeq;
     const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (kIdx && (blockIdx.x != 0 || wid != 0)) return;
     CommitSmem& S = reinterpret_cast<CommitSmem*>(smem)[wid];
@@ -803,9 +815,18 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
                     for (int k = 0; k < 5; k++)
                         if (act && !((fpre >> k) & 1u) && (uint32_t)(__ffs(m[k]) - 1) == lane) fpass = true;
                     const uint32_t fmask = __ballot_sync(0xffffffffu, fpass);
-                    // index (kIdx): insert_sha1 of the filter-passing feature; it
-                    // goes on only if that set a new index bit
+                    // index: insert_sha1 of the filter-passing feature; it goes
+                    // on only if that set a new index bit
                     bool inew = true;
+                    const uint32_t ord = t * kTileCap + gi;  // feature ordinal in the launch
+                    if (kMode == kCommitRound) {
+                        inew = false;
+                        if (fpass) {
+#pragma unroll
+                            for (int k = 0; k < 5; k++)
+                                if (__ldg(P.index_first + (hw[k] & P.index_mask)) >= ord + 1u) inew = true;
+                        }
+                    }
                     if (kIdx) {
                         inew = false;
                         if (fpass) {
@@ -821,9 +842,10 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
                     // filter-passing lane holds the same 17-bit value
                     uint32_t gnew = 0, pend = 0;
                     uint32_t cand[5];
+                    const uint32_t imask = kMode == kCommitRound ? __ballot_sync(0xffffffffu, fpass && inew) : fmask;
 #pragma unroll
                     for (int k = 0; k < 5; k++) {
-                        cand[k] = m[k] & fmask & lanemask_lt();
+                        cand[k] = m[k] & imask & lanemask_lt();
                         if (fpass && inew && !((gpre >> k) & 1u)) {
                             if (cand[k]) pend |= 1u << k;
                             else gnew |= 1u << k;
@@ -862,6 +884,15 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
                     const bool hit_big = counted && (bigfi + before == (uint32_t)kBigElem);
                     const uint32_t hm = __ballot_sync(0xffffffffu, hit_small || hit_big);
                     const uint32_t r = hm ? (uint32_t)(__ffs(hm) - 1) : 31u;
+                    if (kMode == kCommitRound) {
+                        // the inserted features of this pass: filter-passing lanes up to r
+                        const uint32_t sm = __ballot_sync(0xffffffffu, act && lane <= r && fpass);
+                        if (lane == 0 && sm) {
+                            const uint32_t base = t * kTileCap + g0, sh = base & 31u;
+                            atomicOr(P.index_seen + (base >> 5), sm << sh);
+                            if (sh && (sm >> (32u - sh))) atomicOr(P.index_seen + (base >> 5) + 1, sm >> (32u - sh));
+                        }
+                    }
                     // write the bits of lanes up to r (all of them without a roll-over)
                     if (act && lane <= r) {
 #pragma unroll
@@ -930,12 +961,67 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
 
 __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
-    commit_files<false>(P, smem);
+    commit_files<kCommitPlain>(P, smem);
 }
 
 __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit_index(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
-    commit_files<true>(P, smem);
+    commit_files<kCommitSeq>(P, smem);
+}
+
+__global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit_round(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    commit_files<kCommitRound>(P, smem);
+}
+
+// Features of a stream launch recorded in a seen bitmap (ordinal = tile *
+// kTileCap + feature): the first setter of each of their index bits, then
+// (once the rounds agree) the bits and the count of first setters.
+__global__ void k_stream_index_first(const uint32_t* __restrict__ feats, const TileOut* __restrict__ tile_out,
+                                     uint32_t ntiles, const uint32_t* __restrict__ seen, uint32_t mask,
+                                     uint32_t* __restrict__ first) {
+    const uint64_t n = (uint64_t)ntiles * kTileCap;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (!((seen[i >> 5] >> (i & 31)) & 1u)) continue;
+        const uint32_t t = (uint32_t)(i / kTileCap), g = (uint32_t)(i - (uint64_t)t * kTileCap);
+        if (g >= tile_out[t].count) continue;
+        const uint32_t* w = feats + (size_t)t * 5 * kTileCap + g;
+#pragma unroll
+        for (int k = 0; k < 5; k++) atomicMin(first + (w[(size_t)k * kTileCap] & mask), (uint32_t)i + 1u);
+    }
+}
+
+__global__ void k_stream_index_mark(const uint32_t* __restrict__ feats, const TileOut* __restrict__ tile_out,
+                                    uint32_t ntiles, const uint32_t* __restrict__ seen, uint32_t mask,
+                                    const uint32_t* __restrict__ first, uint32_t* __restrict__ bits,
+                                    unsigned long long* __restrict__ count) {
+    const uint64_t n = (uint64_t)ntiles * kTileCap;
+    uint32_t mine = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (!((seen[i >> 5] >> (i & 31)) & 1u)) continue;
+        const uint32_t t = (uint32_t)(i / kTileCap), g = (uint32_t)(i - (uint64_t)t * kTileCap);
+        if (g >= tile_out[t].count) continue;
+        const uint32_t* w = feats + (size_t)t * 5 * kTileCap + g;
+        bool fresh = false;
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const uint32_t pos = w[(size_t)k * kTileCap] & mask;
+            fresh |= first[pos] == (uint32_t)i + 1u;
+            atomicOr(bits + (pos >> 5), 1u << (pos & 31));
+        }
+        mine += fresh;
+    }
+    for (int d = 16; d > 0; d >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, d);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(count, (unsigned long long)mine);
+}
+
+__global__ void k_words_diff(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t n,
+                             unsigned long long* __restrict__ diff) {
+    uint32_t mine = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        mine += a[i] != b[i];
+    for (int d = 16; d > 0; d >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, d);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(diff, (unsigned long long)mine);
 }
 
 // ------------------------------------------------------------ block mode
@@ -1089,6 +1175,32 @@ cudaError_t launch_stream_commit_index(const GenParams& P, cudaStream_t st) {
     cudaFuncSetAttribute(k_stream_commit_index, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(CommitSmem) * kCommitWarps));
     k_stream_commit_index<<<1, kCommitWarps * 32, sizeof(CommitSmem) * kCommitWarps, st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_commit_round(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    cudaFuncSetAttribute(k_stream_commit_round, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(CommitSmem) * kCommitWarps));
+    k_stream_commit_round<<<grid, kCommitWarps * 32, sizeof(CommitSmem) * kCommitWarps, st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_index_first(const GenParams& P, const uint32_t* seen, uint32_t* first, uint32_t grid,
+                                      cudaStream_t st) {
+    k_stream_index_first<<<grid, 256, 0, st>>>(P.features, P.tile_out, P.ntiles, seen, P.index_mask, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_index_mark(const GenParams& P, const uint32_t* seen, const uint32_t* first, uint32_t grid,
+                                     cudaStream_t st) {
+    k_stream_index_mark<<<grid, 256, 0, st>>>(P.features, P.tile_out, P.ntiles, seen, P.index_mask, first,
+                                              P.index_bits, P.index_new);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_words_diff(const uint32_t* a, const uint32_t* b, uint64_t nwords, unsigned long long* diff,
+                              uint32_t grid, cudaStream_t st) {
+    k_words_diff<<<grid, 256, 0, st>>>(a, b, nwords, diff);
     return cudaGetLastError();
 }
 

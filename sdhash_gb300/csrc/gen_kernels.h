@@ -95,6 +95,12 @@ struct GenParams {
     uint32_t index_mask;
     unsigned long long* index_new;
     uint32_t* feats;
+    // stream-mode index build by fixed-point rounds: first setter of every
+    // index bit over the previous round's inserted features (ordinal + 1 of
+    // tile * kTileCap + feature, 0 for bits set before the batch) and the
+    // bitmap of this round's inserted features, by the same ordinal
+    const uint32_t* index_first;
+    uint32_t* index_seen;
 };
 
 // Index search samples counted features 0, 4, 8, ... of a block
@@ -117,6 +123,20 @@ cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st
 cudaError_t launch_stream_commit(const GenParams& P, uint32_t grid, cudaStream_t st);
 // One warp, files in file_order, index inserts (GenParams::index_bits).
 cudaError_t launch_stream_commit_index(const GenParams& P, cudaStream_t st);
+// One fixed-point round of a stream-mode index build: files in parallel,
+// index acceptance read from GenParams::index_first, inserted features
+// recorded in GenParams::index_seen.
+cudaError_t launch_stream_commit_round(const GenParams& P, uint32_t grid, cudaStream_t st);
+// first[bit] = min(first[bit], ordinal + 1) over the features in seen.
+cudaError_t launch_stream_index_first(const GenParams& P, const uint32_t* seen, uint32_t* first, uint32_t grid,
+                                      cudaStream_t st);
+// Index bits of the features in seen; *index_new += those that own the
+// first setting of one of their bits.
+cudaError_t launch_stream_index_mark(const GenParams& P, const uint32_t* seen, const uint32_t* first, uint32_t grid,
+                                     cudaStream_t st);
+// *diff += number of words where a and b differ.
+cudaError_t launch_words_diff(const uint32_t* a, const uint32_t* b, uint64_t nwords, unsigned long long* diff,
+                              uint32_t grid, cudaStream_t st);
 cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st);
 
 }  // namespace sdbfg

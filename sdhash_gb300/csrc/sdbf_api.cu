@@ -162,6 +162,14 @@ extern "C" int sdbfg_ctx_set_lead(sdbfg_ctx* c, uint32_t steps) {
     return SDBFG_OK;
 }
 
+extern "C" int sdbfg_ctx_set_index_rounds(sdbfg_ctx* c, uint32_t max_rounds) {
+    if (!c || max_rounds > 1024) return SDBFG_ERR_ARG;
+    c->index_max_rounds = max_rounds;
+    return SDBFG_OK;
+}
+
+extern "C" uint32_t sdbfg_ctx_index_rounds(sdbfg_ctx* c) { return c ? c->index_rounds_used : 0; }
+
 extern "C" uint64_t sdbfg_ctx_relinked_tiles(sdbfg_ctx* c) {
     if (!c) return 0;
     uint32_t v = 0;
@@ -363,6 +371,55 @@ struct IndexBuild {
     unsigned long long* count;
 };
 
+// The commit of one stream launch group with an index being built: rounds
+// of the parallel commit against the first setters of the previous round's
+// inserted features until two rounds insert the same features (then the
+// digests are the sequential ones, and the index takes those features'
+// bits), else the one-warp sequential commit.
+static int commit_with_index(sdbfg_ctx* c, GenParams P, uint32_t cap_grid, cudaStream_t st) {
+    c->index_rounds_used = 0;
+    const uint64_t nfeat = (uint64_t)P.ntiles * kTileCap;
+    if (c->index_max_rounds && P.ntiles) {
+        const uint64_t nwords = nfeat / 32 + 2, nbits = (uint64_t)P.index_mask + 1;
+        for (DevBuf* b : {&c->d_seen[0], &c->d_seen[1]}) CUDA_TRY(c, b->ensure(nwords * 4));
+        CUDA_TRY(c, c->d_diff.ensure(8));
+        CUDA_TRY(c, c->d_idx_first.ensure(nbits * 4));
+        uint32_t* first = c->d_idx_first.as<uint32_t>();
+        int rc = index_first_init(c, P.index_bits, first, nbits, st);
+        if (rc) return rc;
+        CUDA_TRY(c, cudaMemsetAsync(c->d_seen[0].p, 0, nwords * 4, st));
+        const uint32_t commit_grid = std::min<uint32_t>((P.nfiles + kCommitWarps - 1) / kCommitWarps, cap_grid);
+        const uint32_t fgrid = (uint32_t)std::min<uint64_t>((nfeat + 255) / 256, (uint64_t)c->sms * 32);
+        const uint32_t wgrid = (uint32_t)std::min<uint64_t>((nwords + 255) / 256, (uint64_t)c->sms * 8);
+        int prev = 0;
+        for (uint32_t r = 1; r <= c->index_max_rounds; r++) {
+            uint32_t* cur = c->d_seen[prev ^ 1].as<uint32_t>();
+            CUDA_TRY(c, cudaMemsetAsync(cur, 0, nwords * 4, st));
+            CUDA_TRY(c, cudaMemsetAsync(c->d_diff.p, 0, 8, st));
+            P.index_first = first;
+            P.index_seen = cur;
+            TIMED_LAUNCH_ON(c, "k_stream_commit_round", st, launch_stream_commit_round(P, commit_grid, st));
+            TIMED_LAUNCH_ON(c, "k_words_diff", st,
+                            launch_words_diff(cur, c->d_seen[prev].as<uint32_t>(), nwords,
+                                              c->d_diff.as<unsigned long long>(), wgrid, st));
+            unsigned long long diff = 0;
+            CUDA_TRY(c, cudaMemcpyAsync(&diff, c->d_diff.p, 8, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(c, cudaStreamSynchronize(st));
+            if (diff == 0) {
+                TIMED_LAUNCH_ON(c, "k_stream_index_mark", st, launch_stream_index_mark(P, cur, first, fgrid, st));
+                c->index_rounds_used = r;
+                return SDBFG_OK;
+            }
+            prev ^= 1;
+            rc = index_first_init(c, P.index_bits, first, nbits, st);
+            if (rc) return rc;
+            TIMED_LAUNCH_ON(c, "k_stream_index_first", st, launch_stream_index_first(P, cur, first, fgrid, st));
+        }
+    }
+    TIMED_LAUNCH_ON(c, "k_stream_commit_index", st, launch_stream_commit_index(P, st));
+    return SDBFG_OK;
+}
+
 static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const uint8_t* dev_data,
                                    const uint64_t* offsets_in, const uint64_t* lens_in, uint32_t n, uint32_t* dev_out,
                                    uint64_t out_cap, sdbfg_digest_result* res, uint64_t* total_out,
@@ -515,7 +572,8 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             P.index_bits = ib->bits;
             P.index_mask = ib->mask;
             P.index_new = ib->count;
-            TIMED_LAUNCH_ON(c, "k_stream_commit_index", st, launch_stream_commit_index(P, st));
+            rc = commit_with_index(c, P, cap_grid, st);
+            if (rc) return rc;
         } else {
             TIMED_LAUNCH_ON(c, "k_stream_commit", st,
                             launch_stream_commit(P, std::min<uint32_t>((g.count + kCommitWarps - 1) / kCommitWarps,

@@ -10,9 +10,10 @@ filter), stored here gzip-compressed.  Then runs the reference's index
 search (sdhash --index-search idx, sdhash.cc:231-266 and 638-652) on five
 seeded query inputs in 16 KiB block mode and records index_results(), and
 records the sha256 of each index filter as the reference decompresses it.
-Also builds two more indexes from fresh (a stream-mode group whose later
-files repeat earlier ones, and a block-mode group) and records the set
-text, the index header and the filter's sha256 of each.
+Also builds three more indexes from fresh (a stream-mode group whose later
+files repeat earlier ones, a block-mode group, and a stream-mode group of
+40 files cut from one shared pool) and records the set text, the index
+header and the filter's sha256 of each.
 
 Inputs are seeded synthetic mixture content (sdhash_gb300/synth.py), so the
 GPU tests regenerate them on any machine.
@@ -68,7 +69,26 @@ def build_inputs():
               ("s2.bin", s2), ("s3.bin", s0), ("s4.bin", s2[:30_000] + s0[:30_000])]
     b0 = synth.mixture_bytes(95, 0, 300_000).tobytes()
     block = [("b0.bin", b0), ("b1.bin", b0[50_000:250_000] + synth.mixture_bytes(95, 1, 100_000).tobytes())]
-    return stream, block
+    return stream, block, dense_stream()
+
+
+def dense_stream():
+    """A stream-mode group of 40 files cut from one shared 400 KB pool
+    (three slices each, plus fresh bytes), so that most features recur in
+    several files and each file's digest depends on many earlier ones."""
+    import numpy as np
+    pool = synth.mixture_bytes(96, 0, 400_000).tobytes()
+    rng = np.random.default_rng(96)
+    out = []
+    for i in range(40):
+        parts = []
+        for _ in range(3):
+            n = int(rng.integers(8_000, 40_000))
+            o = int(rng.integers(0, len(pool) - n))
+            parts.append(pool[o:o + n])
+        parts.append(synth.random_bytes(96, i + 1, int(rng.integers(0, 6_000))).tobytes())
+        out.append((f"d{i}.bin", b"".join(parts)))
+    return out
 
 
 def _arr(items):
@@ -123,7 +143,7 @@ def main():
             shutil.copy(f"idx/{s}.sdbf", os.path.join(OUT, f"{s}.sdbf"))
         # index builds (stream and block groups) from fresh indexes
         rec["builds"] = []
-        for items, dd, stem in zip(build_inputs(), (0, 16384), ("S", "K")):
+        for items, dd, stem in zip(build_inputs(), (0, 16384, 0), ("S", "K", "D")):
             names, bufs, lens = _arr(items)
             rc = L.ref_index_build(names, bufs, lens, len(items), dd, f"idx/{stem}.sdbf".encode(),
                                    f"idx/{stem}.sdbf.idx".encode())

@@ -111,13 +111,16 @@ def test_hits_match_oracle_dense_indexes(ctx, oracle):
     assert sum(int((h > 4).sum()) for h in hits if h is not None) > 100
 
 
-@pytest.mark.parametrize("case", [0, 1], ids=["stream group", "block group"])
-def test_index_build_matches_reference(ctx, tmp_path, case):
+@pytest.mark.parametrize("case,rounds", [(0, 16), (0, 0), (1, 16), (2, 16), (2, 1), (2, 0)],
+                         ids=["stream group", "stream group, sequential commit", "block group",
+                              "shared-pool stream group", "shared-pool stream group, one round",
+                              "shared-pool stream group, sequential commit"])
+def test_index_build_matches_reference(ctx, tmp_path, case, rounds):
     """sdhash --index for one group: the digests (stream mode: features the
     index already holds are dropped), the index bits and its element count
-    are the reference's; the index file written here decodes to the same
-    filter and carries the reference's header fields."""
-    import ctypes as C
+    are the reference's -- from the fixed-point rounds, and from the
+    sequential commit when rounds are off or run out; the index file written
+    here decodes to the same filter and carries the reference's header fields."""
     import hashlib
     import importlib.util
     rec = _fixture()["builds"][case]
@@ -126,7 +129,19 @@ def test_index_build_matches_reference(ctx, tmp_path, case):
     spec.loader.exec_module(m)
     items = m.build_inputs()[case]
     bits = np.zeros(64 << 20, dtype=np.uint8)
-    digs, ec = ctx.digest_index([d for _, d in items], [n for n, _ in items], rec["dd"], bits)
+    ctx.set_index_rounds(rounds)
+    try:
+        digs, ec = ctx.digest_index([d for _, d in items], [n for n, _ in items], rec["dd"], bits)
+        used = ctx.index_rounds
+    finally:
+        ctx.set_index_rounds(16)
+    if rec["dd"] == 0:
+        # later files repeat earlier ones: round 1 inserts too much, so the
+        # rounds need at least two; one round is not enough and falls back
+        if rounds < 2:
+            assert used == 0
+        else:
+            assert 2 <= used <= rounds
     assert "".join(d.to_string() for d in digs) == rec["sdbf_text"]
     assert hashlib.sha256(bits.tobytes()).hexdigest() == rec["filter_sha256"]
     head = rec["header"].split(":")
@@ -143,6 +158,37 @@ def test_index_build_matches_reference(ctx, tmp_path, case):
     out = np.zeros(64 << 20, dtype=np.uint8)
     assert lib().sdbfg_lz4_decode(raw[nl + 1:], len(raw) - nl - 1, out.ctypes.data, out.size) == int(mine[5])
     assert np.array_equal(out, bits)
+
+
+def test_index_build_rounds_match_sequential_large(ctx):
+    """A 300 MiB stream-mode group (two launch groups: the first holds at
+    most 256 MiB) of files cut from a shared pool: the fixed-point rounds
+    give the digests, bits and element count of the sequential commit."""
+    from sdhash_gb300 import synth
+    pool = synth.mixture_bytes(97, 0, 48 << 20)
+    rng = np.random.default_rng(97)
+    bufs = []
+    for i in range(150):
+        n = int(rng.integers(1 << 20, 3 << 20))
+        o = int(rng.integers(0, pool.size - n))
+        b = pool[o:o + n].copy()
+        b[:4096] = synth.random_bytes(97, i + 1, 4096)
+        bufs.append(b)
+    names = [f"p{i}" for i in range(len(bufs))]
+    assert sum(b.size for b in bufs) > 256 << 20
+    out = []
+    for rounds in (16, 0):
+        bits = np.zeros(64 << 20, dtype=np.uint8)
+        ctx.set_index_rounds(rounds)
+        try:
+            digs, ec = ctx.digest_index(bufs, names, 0, bits)
+            used = ctx.index_rounds
+        finally:
+            ctx.set_index_rounds(16)
+        out.append(("".join(d.to_string() for d in digs), bits, ec, used))
+    (t1, b1, e1, u1), (t0, b0, e0, u0) = out
+    assert u0 == 0 and u1 >= 2
+    assert t1 == t0 and e1 == e0 and np.array_equal(b1, b0)
 
 
 def test_cli_index_matches_reference_group(ctx, tmp_path, monkeypatch):

@@ -146,3 +146,23 @@ def test_index_groups():
     # 3 GiB is negative as an int; 3 GiB + 100 MiB + 1 GiB wraps to 100 MiB
     assert _index_groups([3 << 30, 100 * MB, 1 << 30, 5]) == [[0, 1, 2, 3]]
     assert _index_groups([3 << 30, 2 << 30]) == [[0, 1]]
+
+
+@pytest.mark.parametrize("case", [0, 2], ids=["stream group", "shared-pool stream group"])
+def test_oracle_index_build_stream_matches_reference(oracle, case):
+    """The oracle's stream-mode index build (files in order, one shared
+    index) gives the reference's set text, index filter and element count
+    for the fixture groups."""
+    import hashlib
+    import importlib.util
+    import json
+    rec = json.load(open(os.path.join(GOLD, "index_search.json")))["builds"][case]
+    spec = importlib.util.spec_from_file_location("mkidx", os.path.join(os.path.dirname(GOLD), "make_index_golden.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    items = m.build_inputs()[case]
+    bits = np.zeros(64 << 20, dtype=np.uint8)
+    digs, ec = oracle.index_build_stream([d for _, d in items], [n for n, _ in items], bits)
+    assert "".join(d.to_string() for d in digs if d is not None) == rec["sdbf_text"]
+    assert ec == int(rec["header"].split(":")[2])
+    assert hashlib.sha256(bits.tobytes()).hexdigest() == rec["filter_sha256"]
