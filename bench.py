@@ -953,7 +953,7 @@ def main_index(args):
 
 
 IB_METRIC = "index build input GB/s"
-IB_KERNELS = ("k_stream_tiles", "k_stream_check", "k_stream_fix", "k_stream_commit_round", "k_words_diff",
+IB_KERNELS = ("k_stream_tiles", "k_stream_check", "k_stream_fix", "k_stream_commit_round", "k_stream_index_pred", "k_pred_dirty",
               "k_index_first_init", "k_stream_index_first", "k_stream_index_mark", "k_stream_commit_index",
               "k_scan_offsets", "k_pack_filters", "k_block_digest", "k_index_first", "k_index_mark")
 

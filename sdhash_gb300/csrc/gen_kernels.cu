@@ -716,8 +716,11 @@ __device__ __forceinline__ void stage_tile(uint32_t (*buf)[kTileCap], const uint
 // * kCommitRound: one round of a fixed point.  Files commit in parallel; a
 //   feature is taken as setting a new index bit iff no feature inserted in
 //   the previous round precedes it as the first setter of one of its bits
-//   (GenParams::index_first), and the inserted features are recorded
-//   (GenParams::index_seen).  A round that inserts the same features as
+//   (GenParams::index_pred, one bit per feature, read with the tile), and
+//   the inserted features are recorded (GenParams::index_seen).  A file's
+//   commit depends only on its own features and their predicate bits, so
+//   later rounds re-commit only the files whose bits changed
+//   (GenParams::commit_dirty), after clearing their seen bits.  A round that inserts the same features as
 //   the previous one reproduces the sequential result: by induction over
 //   the input order, every decision then depends only on earlier decisions
 //   that already agree.
@@ -734,6 +737,7 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
     constexpr uint32_t kGroup = kIdx ? 1u : 32u;
     for (uint32_t fi = kIdx ? 0u : blockIdx.x * kCommitWarps + wid; fi < P.nfiles; fi += fstep) {
         const uint32_t file = P.file_order[fi];
+        if (kMode == kCommitRound && P.commit_dirty && !P.commit_dirty[file]) continue;
         const GenFile Fd = P.files[file];
         if (Fd.nchunks == 0) continue;
         uint32_t* out = P.out_filters + (size_t)Fd.filter_base * 64;
@@ -745,9 +749,29 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
         const uint32_t t_first = c0.first_tile, t_end = cl.first_tile + cl.ntiles;
         uint32_t chunk = Fd.first_chunk;
         uint32_t next_chunk_tile = (Fd.nchunks > 1) ? P.chunks[chunk + 1].first_tile : 0xFFFFFFFFu;
+        if (kMode == kCommitRound && P.commit_dirty && t_first < t_end) {
+            // clear the file's seen bits, ordinals [t_first, t_end) * kTileCap;
+            // inner words are the file's alone, edge words shared with neighbours
+            const uint32_t o0 = t_first * kTileCap, o1 = t_end * kTileCap - 1;
+            for (uint32_t w = (o0 >> 5) + lane; w <= (o1 >> 5); w += 32) {
+                const uint32_t lo = w == (o0 >> 5) ? (o0 & 31u) : 0u, hi = w == (o1 >> 5) ? (o1 & 31u) : 31u;
+                const uint32_t m = (0xffffffffu >> (31u - hi)) & (0xffffffffu << lo);
+                if (m == 0xffffffffu) P.index_seen[w] = 0;
+                else atomicAnd(P.index_seen + w, ~m);
+            }
+            __syncwarp();
+        }
         uint32_t nf_cur = t_first < t_end ? P.tile_out[t_first].count : 0;
         uint32_t nf_next = t_first + 1 < t_end ? P.tile_out[t_first + 1].count : 0;
         if (t_first < t_end) stage_tile(S.feat[0], P.features + (size_t)t_first * 5 * kTileCap, nf_cur, lane);
+        // kCommitRound: the tile's predicate words (its <= 472 ordinals span
+        // at most 16 words), lane q holding word q; the next tile's in flight
+        uint32_t pw_cur = 0, pw_next = 0;
+        if (kMode == kCommitRound) {
+            if (t_first < t_end && lane < 16) pw_cur = __ldg(P.index_pred + ((t_first * kTileCap) >> 5) + lane);
+            if (t_first + 1 < t_end && lane < 16)
+                pw_next = __ldg(P.index_pred + (((t_first + 1) * kTileCap) >> 5) + lane);
+        }
         __syncwarp();
         uint32_t bf_count = 1, last_count = 0, bigfi = 0;
         long long t_file = clock64(), t_wait = 0;
@@ -769,6 +793,11 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
             const uint32_t nf = nf_cur;
             if (t + 1 < t_end)
                 stage_tile(S.feat[cur ^ 1u], P.features + (size_t)(t + 1) * 5 * kTileCap, nf_next, lane);
+            const uint32_t pw = pw_cur;
+            if (kMode == kCommitRound) {
+                pw_cur = pw_next;
+                pw_next = (t + 2 < t_end && lane < 16) ? __ldg(P.index_pred + (((t + 2) * kTileCap) >> 5) + lane) : 0u;
+            }
             nf_cur = nf_next;
             nf_next = t + 2 < t_end ? P.tile_out[t + 2].count : 0;
             for (uint32_t g0 = 0; g0 < nf; g0 += kGroup) {
@@ -781,6 +810,12 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
                     hw[k] = h;
                     a[k] = h & kBfMask;
                     b[k] = h & kBigMask;
+                }
+                bool ipred = false;
+                if (kMode == kCommitRound) {
+                    const uint32_t o = t * kTileCap + gi;
+                    const uint32_t w = __shfl_sync(0xffffffffu, pw, ((o >> 5) - ((t * kTileCap) >> 5)) & 31u);
+                    ipred = have && ((w >> (o & 31u)) & 1u);
                 }
                 uint32_t start = 0;
                 n_groups++;
@@ -818,15 +853,7 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
                     // index: insert_sha1 of the filter-passing feature; it goes
                     // on only if that set a new index bit
                     bool inew = true;
-                    const uint32_t ord = t * kTileCap + gi;  // feature ordinal in the launch
-                    if (kMode == kCommitRound) {
-                        inew = false;
-                        if (fpass) {
-#pragma unroll
-                            for (int k = 0; k < 5; k++)
-                                if (__ldg(P.index_first + (hw[k] & P.index_mask)) >= ord + 1u) inew = true;
-                        }
-                    }
+                    if (kMode == kCommitRound) inew = fpass && ipred;
                     if (kIdx) {
                         inew = false;
                         if (fpass) {
@@ -977,6 +1004,27 @@ __global__ void __launch_bounds__(kCommitWarps * 32) k_stream_commit_round(GenPa
 // Features of a stream launch recorded in a seen bitmap (ordinal = tile *
 // kTileCap + feature): the first setter of each of their index bits, then
 // (once the rounds agree) the bits and the count of first setters.
+// k_stream_index_pred: for every feature, whether it would own the first
+// setting of one of its bits (one bit per ordinal, a warp per word).
+__global__ void k_stream_index_pred(const uint32_t* __restrict__ feats, const TileOut* __restrict__ tile_out,
+                                    uint32_t ntiles, const uint32_t* __restrict__ first, uint32_t mask,
+                                    uint32_t* __restrict__ pred) {
+    const uint64_t n = (uint64_t)ntiles * kTileCap, npad = (n + 31) & ~31ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (uint64_t)gridDim.x * blockDim.x) {
+        bool p = false;
+        if (i < n) {
+            const uint32_t t = (uint32_t)(i / kTileCap), g = (uint32_t)(i - (uint64_t)t * kTileCap);
+            if (g < tile_out[t].count) {
+                const uint32_t* w = feats + (size_t)t * 5 * kTileCap + g;
+#pragma unroll
+                for (int k = 0; k < 5; k++) p |= __ldg(first + (w[(size_t)k * kTileCap] & mask)) >= (uint32_t)i + 1u;
+            }
+        }
+        const uint32_t word = __ballot_sync(0xffffffffu, p);
+        if ((threadIdx.x & 31) == 0) pred[i >> 5] = word;
+    }
+}
+
 __global__ void k_stream_index_first(const uint32_t* __restrict__ feats, const TileOut* __restrict__ tile_out,
                                      uint32_t ntiles, const uint32_t* __restrict__ seen, uint32_t mask,
                                      uint32_t* __restrict__ first) {
@@ -1015,13 +1063,24 @@ __global__ void k_stream_index_mark(const uint32_t* __restrict__ feats, const Ti
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(count, (unsigned long long)mine);
 }
 
-__global__ void k_words_diff(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t n,
-                             unsigned long long* __restrict__ diff) {
-    uint32_t mine = 0;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        mine += a[i] != b[i];
-    for (int d = 16; d > 0; d >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, d);
-    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(diff, (unsigned long long)mine);
+__global__ void k_pred_dirty(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t nwords,
+                             const GenTile* __restrict__ tiles, const GenChunk* __restrict__ chunks, uint32_t ntiles,
+                             uint8_t* __restrict__ dirty, unsigned int* __restrict__ ndirty) {
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nwords;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x = a[w] ^ b[w];
+        while (x) {
+            const uint64_t ord = w * 32 + (uint32_t)(__ffs(x) - 1);
+            x &= x - 1u;
+            const uint64_t t = ord / kTileCap;
+            if (t >= ntiles) continue;
+            const uint32_t f = chunks[tiles[t].chunk].file;
+            if (!dirty[f]) {
+                dirty[f] = 1;
+                atomicAdd(ndirty, 1u);
+            }
+        }
+    }
 }
 
 // ------------------------------------------------------------ block mode
@@ -1185,6 +1244,12 @@ cudaError_t launch_stream_commit_round(const GenParams& P, uint32_t grid, cudaSt
     return cudaGetLastError();
 }
 
+cudaError_t launch_stream_index_pred(const GenParams& P, const uint32_t* first, uint32_t* pred, uint32_t grid,
+                                     cudaStream_t st) {
+    k_stream_index_pred<<<grid, 256, 0, st>>>(P.features, P.tile_out, P.ntiles, first, P.index_mask, pred);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_stream_index_first(const GenParams& P, const uint32_t* seen, uint32_t* first, uint32_t grid,
                                       cudaStream_t st) {
     k_stream_index_first<<<grid, 256, 0, st>>>(P.features, P.tile_out, P.ntiles, seen, P.index_mask, first);
@@ -1198,9 +1263,9 @@ cudaError_t launch_stream_index_mark(const GenParams& P, const uint32_t* seen, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_words_diff(const uint32_t* a, const uint32_t* b, uint64_t nwords, unsigned long long* diff,
-                              uint32_t grid, cudaStream_t st) {
-    k_words_diff<<<grid, 256, 0, st>>>(a, b, nwords, diff);
+cudaError_t launch_pred_dirty(const GenParams& P, const uint32_t* a, const uint32_t* b, uint64_t nwords,
+                              uint8_t* dirty, unsigned int* ndirty, uint32_t grid, cudaStream_t st) {
+    k_pred_dirty<<<grid, 256, 0, st>>>(a, b, nwords, P.tiles, P.chunks, P.ntiles, dirty, ndirty);
     return cudaGetLastError();
 }
 

@@ -95,12 +95,16 @@ struct GenParams {
     uint32_t index_mask;
     unsigned long long* index_new;
     uint32_t* feats;
-    // stream-mode index build by fixed-point rounds: first setter of every
-    // index bit over the previous round's inserted features (ordinal + 1 of
-    // tile * kTileCap + feature, 0 for bits set before the batch) and the
-    // bitmap of this round's inserted features, by the same ordinal
-    const uint32_t* index_first;
+    // stream-mode index build by fixed-point rounds, bitmaps by feature
+    // ordinal (tile * kTileCap + feature): index_pred -- the feature owns the
+    // first setting of one of its index bits among the previous round's
+    // inserted features (k_stream_index_pred); index_seen -- this round's
+    // inserted features
+    const uint32_t* index_pred;
     uint32_t* index_seen;
+    // rounds after the first: only files flagged here commit again (their
+    // seen bits are cleared first); null = every file
+    const uint8_t* commit_dirty;
 };
 
 // Index search samples counted features 0, 4, 8, ... of a block
@@ -124,9 +128,13 @@ cudaError_t launch_stream_commit(const GenParams& P, uint32_t grid, cudaStream_t
 // One warp, files in file_order, index inserts (GenParams::index_bits).
 cudaError_t launch_stream_commit_index(const GenParams& P, cudaStream_t st);
 // One fixed-point round of a stream-mode index build: files in parallel,
-// index acceptance read from GenParams::index_first, inserted features
+// index acceptance read from GenParams::index_pred, inserted features
 // recorded in GenParams::index_seen.
 cudaError_t launch_stream_commit_round(const GenParams& P, uint32_t grid, cudaStream_t st);
+// pred bit of every feature ordinal: first[bit] >= ordinal + 1 for one of
+// its index bits (no earlier first setter).
+cudaError_t launch_stream_index_pred(const GenParams& P, const uint32_t* first, uint32_t* pred, uint32_t grid,
+                                     cudaStream_t st);
 // first[bit] = min(first[bit], ordinal + 1) over the features in seen.
 cudaError_t launch_stream_index_first(const GenParams& P, const uint32_t* seen, uint32_t* first, uint32_t grid,
                                       cudaStream_t st);
@@ -134,9 +142,11 @@ cudaError_t launch_stream_index_first(const GenParams& P, const uint32_t* seen, 
 // first setting of one of their bits.
 cudaError_t launch_stream_index_mark(const GenParams& P, const uint32_t* seen, const uint32_t* first, uint32_t grid,
                                      cudaStream_t st);
-// *diff += number of words where a and b differ.
-cudaError_t launch_words_diff(const uint32_t* a, const uint32_t* b, uint64_t nwords, unsigned long long* diff,
-                              uint32_t grid, cudaStream_t st);
+// dirty[file] = 1 for every file with a feature whose predicate bit
+// differs between pred words a and b (nwords words); *ndirty counts flags
+// set (at least once per flagged file).
+cudaError_t launch_pred_dirty(const GenParams& P, const uint32_t* a, const uint32_t* b, uint64_t nwords,
+                              uint8_t* dirty, unsigned int* ndirty, uint32_t grid, cudaStream_t st);
 cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st);
 
 }  // namespace sdbfg

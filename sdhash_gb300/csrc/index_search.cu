@@ -238,9 +238,14 @@ int index_query(sdbfg_ctx* c, const uint32_t* d_probes, const uint8_t* d_nprobes
 // Ordinal = (global slot + 1) << 8 | feature index (bits set before the
 // batch have first setter 0).
 
+// Four entries (one 16-byte store) per thread; nbits is a power of two >= 512.
 __global__ void k_index_first_init(const uint32_t* __restrict__ bits, uint32_t* __restrict__ first, uint64_t nbits) {
-    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nbits; p += (uint64_t)gridDim.x * blockDim.x)
-        first[p] = ((bits[p >> 5] >> (p & 31)) & 1u) ? 0u : 0xFFFFFFFFu;
+    uint4* out = reinterpret_cast<uint4*>(first);
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nbits / 4;
+         q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t b = (__ldg(bits + (q >> 3)) >> ((q & 7) * 4)) & 15u;
+        out[q] = make_uint4((b & 1u) ? 0u : ~0u, (b & 2u) ? 0u : ~0u, (b & 4u) ? 0u : ~0u, (b & 8u) ? 0u : ~0u);
+    }
 }
 
 __global__ void k_index_first(const uint32_t* __restrict__ feats, const uint16_t* __restrict__ counts, uint64_t nslots,
@@ -282,7 +287,7 @@ __global__ void k_index_mark(const uint32_t* __restrict__ feats, const uint16_t*
 }
 
 int index_first_init(sdbfg_ctx* c, const uint32_t* d_bits, uint32_t* d_first, uint64_t nbits, cudaStream_t st) {
-    const uint32_t grid = (uint32_t)std::min<uint64_t>((nbits + 255) / 256, (uint64_t)c->sms * 32);
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((nbits / 4 + 255) / 256, (uint64_t)c->sms * 32);
     TIMED_LAUNCH_ON(c, "k_index_first_init", st,
                     (k_index_first_init<<<grid, 256, 0, st>>>(d_bits, d_first, nbits), cudaGetLastError()));
     return SDBFG_OK;

@@ -371,49 +371,63 @@ struct IndexBuild {
     unsigned long long* count;
 };
 
-// The commit of one stream launch group with an index being built: rounds
-// of the parallel commit against the first setters of the previous round's
-// inserted features until two rounds insert the same features (then the
-// digests are the sequential ones, and the index takes those features'
-// bits), else the one-warp sequential commit.
+// The commit of one stream launch group with an index being built, as a
+// fixed point: round 1 commits every file with the predicate bits of the
+// index as it stands; then, from the first setters of the features the last
+// round inserted, new predicate bits; files whose bits changed commit again,
+// until none changes (the digests are then the sequential ones, and the index
+// takes the inserted features' bits).  After index_max_rounds commit rounds
+// without that, the one-warp sequential commit runs instead.
 static int commit_with_index(sdbfg_ctx* c, GenParams P, uint32_t cap_grid, cudaStream_t st) {
     c->index_rounds_used = 0;
     const uint64_t nfeat = (uint64_t)P.ntiles * kTileCap;
     if (c->index_max_rounds && P.ntiles) {
         const uint64_t nwords = nfeat / 32 + 2, nbits = (uint64_t)P.index_mask + 1;
-        for (DevBuf* b : {&c->d_seen[0], &c->d_seen[1]}) CUDA_TRY(c, b->ensure(nwords * 4));
-        CUDA_TRY(c, c->d_diff.ensure(8));
+        for (DevBuf* b : {&c->d_seen[0], &c->d_seen[1], &c->d_pred}) CUDA_TRY(c, b->ensure(nwords * 4));
+        CUDA_TRY(c, c->d_diff.ensure(8 + std::max<uint64_t>(1, P.nfiles)));
         CUDA_TRY(c, c->d_idx_first.ensure(nbits * 4));
         uint32_t* first = c->d_idx_first.as<uint32_t>();
-        int rc = index_first_init(c, P.index_bits, first, nbits, st);
-        if (rc) return rc;
-        CUDA_TRY(c, cudaMemsetAsync(c->d_seen[0].p, 0, nwords * 4, st));
+        uint32_t* seen = c->d_seen[0].as<uint32_t>();
+        uint32_t* pred[2] = {c->d_pred.as<uint32_t>(), c->d_seen[1].as<uint32_t>()};
+        unsigned int* ndirty = c->d_diff.as<unsigned int>();
+        uint8_t* dirty = c->d_diff.as<uint8_t>() + 8;
         const uint32_t commit_grid = std::min<uint32_t>((P.nfiles + kCommitWarps - 1) / kCommitWarps, cap_grid);
         const uint32_t fgrid = (uint32_t)std::min<uint64_t>((nfeat + 255) / 256, (uint64_t)c->sms * 32);
-        const uint32_t wgrid = (uint32_t)std::min<uint64_t>((nwords + 255) / 256, (uint64_t)c->sms * 8);
-        int prev = 0;
-        for (uint32_t r = 1; r <= c->index_max_rounds; r++) {
-            uint32_t* cur = c->d_seen[prev ^ 1].as<uint32_t>();
-            CUDA_TRY(c, cudaMemsetAsync(cur, 0, nwords * 4, st));
-            CUDA_TRY(c, cudaMemsetAsync(c->d_diff.p, 0, 8, st));
-            P.index_first = first;
-            P.index_seen = cur;
-            TIMED_LAUNCH_ON(c, "k_stream_commit_round", st, launch_stream_commit_round(P, commit_grid, st));
-            TIMED_LAUNCH_ON(c, "k_words_diff", st,
-                            launch_words_diff(cur, c->d_seen[prev].as<uint32_t>(), nwords,
-                                              c->d_diff.as<unsigned long long>(), wgrid, st));
-            unsigned long long diff = 0;
-            CUDA_TRY(c, cudaMemcpyAsync(&diff, c->d_diff.p, 8, cudaMemcpyDeviceToHost, st));
-            CUDA_TRY(c, cudaStreamSynchronize(st));
-            if (diff == 0) {
-                TIMED_LAUNCH_ON(c, "k_stream_index_mark", st, launch_stream_index_mark(P, cur, first, fgrid, st));
-                c->index_rounds_used = r;
-                return SDBFG_OK;
-            }
-            prev ^= 1;
+        const uint64_t pwords = (nfeat + 31) / 32;
+        const uint32_t wgrid = (uint32_t)std::min<uint64_t>((pwords + 255) / 256, (uint64_t)c->sms * 8);
+        int rc = index_first_init(c, P.index_bits, first, nbits, st);
+        if (rc) return rc;
+        CUDA_TRY(c, cudaMemsetAsync(seen, 0, nwords * 4, st));
+        TIMED_LAUNCH_ON(c, "k_stream_index_pred", st, launch_stream_index_pred(P, first, pred[0], fgrid, st));
+        P.index_seen = seen;
+        P.index_pred = pred[0];
+        P.commit_dirty = nullptr;
+        TIMED_LAUNCH_ON(c, "k_stream_commit_round", st, launch_stream_commit_round(P, commit_grid, st));
+        uint32_t commits = 1;
+        int cur = 0;
+        while (true) {
             rc = index_first_init(c, P.index_bits, first, nbits, st);
             if (rc) return rc;
-            TIMED_LAUNCH_ON(c, "k_stream_index_first", st, launch_stream_index_first(P, cur, first, fgrid, st));
+            TIMED_LAUNCH_ON(c, "k_stream_index_first", st, launch_stream_index_first(P, seen, first, fgrid, st));
+            TIMED_LAUNCH_ON(c, "k_stream_index_pred", st,
+                            launch_stream_index_pred(P, first, pred[cur ^ 1], fgrid, st));
+            CUDA_TRY(c, cudaMemsetAsync(c->d_diff.p, 0, 8 + P.nfiles, st));
+            TIMED_LAUNCH_ON(c, "k_pred_dirty", st,
+                            launch_pred_dirty(P, pred[cur], pred[cur ^ 1], pwords, dirty, ndirty, wgrid, st));
+            unsigned int nd = 0;
+            CUDA_TRY(c, cudaMemcpyAsync(&nd, ndirty, 4, cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(c, cudaStreamSynchronize(st));
+            if (nd == 0) {
+                TIMED_LAUNCH_ON(c, "k_stream_index_mark", st, launch_stream_index_mark(P, seen, first, fgrid, st));
+                c->index_rounds_used = commits;
+                return SDBFG_OK;
+            }
+            if (commits >= c->index_max_rounds) break;
+            cur ^= 1;
+            P.index_pred = pred[cur];
+            P.commit_dirty = dirty;
+            TIMED_LAUNCH_ON(c, "k_stream_commit_round", st, launch_stream_commit_round(P, commit_grid, st));
+            commits++;
         }
     }
     TIMED_LAUNCH_ON(c, "k_stream_commit_index", st, launch_stream_commit_index(P, st));
