@@ -61,7 +61,9 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
                       &c->d_order, &c->d_tile_out, &c->d_features, &c->d_work_filters, &c->d_info,
                       &c->d_counters, &c->d_pack_src, &c->d_pack_dst_off, &c->d_out_filters, &c->d_out_counts,
                       &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase,
-                      &c->d_match_counts, &c->d_match_offs, &c->d_matches, &c->d_mphase})
+                      &c->d_match_counts, &c->d_match_offs, &c->d_matches, &c->d_mphase, &c->d_probes,
+                      &c->d_nprobes, &c->d_hits, &c->d_index_tab, &c->d_feats, &c->d_idx_bits, &c->d_idx_first,
+                      &c->d_idx_count, &c->d_seen[0], &c->d_seen[1], &c->d_pred, &c->d_diff})
         b->release();
     for (auto& S : c->slot) {
         for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work,
@@ -372,8 +374,8 @@ struct IndexBuild {
 };
 
 // The commit of one stream launch group with an index being built, as a
-// fixed point: round 1 commits every file with the predicate bits of the
-// index as it stands; then, from the first setters of the features the last
+// fixed point: round 1 commits every file with the predicate bits of a first
+// guess (every selected feature inserted); then, from the first setters of the features the last
 // round inserted, new predicate bits; files whose bits changed commit again,
 // until none changes (the digests are then the sequential ones, and the index
 // takes the inserted features' bits).  After index_max_rounds commit rounds
@@ -395,10 +397,14 @@ static int commit_with_index(sdbfg_ctx* c, GenParams P, uint32_t cap_grid, cudaS
         const uint32_t fgrid = (uint32_t)std::min<uint64_t>((nfeat + 255) / 256, (uint64_t)c->sms * 32);
         const uint64_t pwords = (nfeat + 31) / 32;
         const uint32_t wgrid = (uint32_t)std::min<uint64_t>((pwords + 255) / 256, (uint64_t)c->sms * 8);
+        // first guess: every selected feature inserted (chance collisions of
+        // all five index bits are then predicted in round 1)
         int rc = index_first_init(c, P.index_bits, first, nbits, st);
         if (rc) return rc;
-        CUDA_TRY(c, cudaMemsetAsync(seen, 0, nwords * 4, st));
+        CUDA_TRY(c, cudaMemsetAsync(seen, 0xFF, nwords * 4, st));
+        TIMED_LAUNCH_ON(c, "k_stream_index_first", st, launch_stream_index_first(P, seen, first, fgrid, st));
         TIMED_LAUNCH_ON(c, "k_stream_index_pred", st, launch_stream_index_pred(P, first, pred[0], fgrid, st));
+        CUDA_TRY(c, cudaMemsetAsync(seen, 0, nwords * 4, st));
         P.index_seen = seen;
         P.index_pred = pred[0];
         P.commit_dirty = nullptr;
