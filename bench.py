@@ -79,6 +79,8 @@ def parse():
     ap.add_argument("--max-filters", type=int, default=2000, help="allpairs: largest digest (filters)")
     ap.add_argument("--plain-pairs", type=int, default=400, help="allpairs: pairs timed one call each")
     ap.add_argument("--cpu-pairs", type=int, default=256, help="allpairs: pairs timed on the host (oracle)")
+    ap.add_argument("--quick", action="store_true",
+                    help="index-build: skip the comparison runs (sequential commit, shared pool, block group)")
     ap.add_argument("--phases", action="store_true",
                     help="allpairs: one more run with the tensor-core kernel's per-phase cycle counters")
     ap.add_argument("--variant", type=int, default=-1,
@@ -981,7 +983,8 @@ def main_index_build(args):
     sequential one-warp commit, and a block-mode group (16 KiB blocks,
     64 MiB files).  cpu_baseline: the oracle's sequential index build (one
     core, as the reference builds a group with -p 1) on the first files of
-    the group, which also checks the GPU's digests of those files."""
+    the group, which also checks the GPU's digests of those files.
+    --quick leaves out the comparison runs (for profiling the main call)."""
     import ctypes as C
     import torch
     import sdhash_gb300 as g
@@ -1068,9 +1071,11 @@ def main_index_build(args):
     ctx.profile(False)
     dev_ms = sum(kern.values())
     # the sequential commit on the same group
-    ctx.set_index_rounds(0)
-    wall_seq = wall_of(call, 1)
-    ctx.set_index_rounds(16)
+    wall_seq = None
+    if not args.quick:
+        ctx.set_index_rounds(0)
+        wall_seq = wall_of(call, 1)
+        ctx.set_index_rounds(16)
     # parity + CPU baseline: the oracle's sequential build of the first files
     # (a prefix of the group has the same digests as in the whole group)
     from oracle import Oracle
@@ -1093,21 +1098,30 @@ def main_index_build(args):
         assert (nb, int(res[k].last_count)) == (w.bf_count, w.last_count), f"index build: file {k} differs"
         assert out_f[o * 256:(o + nb) * 256].tobytes() == w.filters(), f"index build: file {k} filters differ"
     sample_bytes = int(lens[:pre].sum())
-    # shared-pool content: the same sizes, features recurring across files
-    pdata, poffs, plens, ptotal = group(sizes, fill_pool)
-    pcall, _, _, _ = runner(pdata, poffs, plens, 0)
-    pwall = wall_of(pcall, args.steps)
-    prounds = ctx.index_rounds
-    ctx.set_index_rounds(0)
-    pwall_seq = wall_of(pcall, 1)
-    ctx.set_index_rounds(16)
-    del pdata
-    # block-mode group: 64 MiB files
-    bsizes = np.full(11, 64 << 20, dtype=np.uint64)
-    bdata, boffs, blens, btotal = group(bsizes, fill_mixture(args.seed + 6200))
-    bcall, _, _, _ = runner(bdata, boffs, blens, 16384)
-    bwall = wall_of(bcall, args.steps)
-    del bdata
+    extra = {}
+    if not args.quick:
+        # shared-pool content: the same sizes, features recurring across files
+        pdata, poffs, plens, ptotal = group(sizes, fill_pool)
+        pcall, _, _, _ = runner(pdata, poffs, plens, 0)
+        pwall = wall_of(pcall, args.steps)
+        prounds = ctx.index_rounds
+        ctx.set_index_rounds(0)
+        pwall_seq = wall_of(pcall, 1)
+        ctx.set_index_rounds(16)
+        del pdata
+        # block-mode group: 64 MiB files
+        bsizes = np.full(11, 64 << 20, dtype=np.uint64)
+        bdata, boffs, blens, btotal = group(bsizes, fill_mixture(args.seed + 6200))
+        bcall, _, _, _ = runner(bdata, boffs, blens, 16384)
+        bwall = wall_of(bcall, args.steps)
+        del bdata
+        extra = {"sequential_commit_e2e": {"value": total / wall_seq / 1e9, "unit": "GB/s",
+                                           "path": "the same call with index rounds off (one-warp commit)"},
+                 "shared_pool_e2e": {"value": ptotal / pwall / 1e9, "unit": "GB/s", "index_rounds": prounds,
+                                     "sequential_commit": ptotal / pwall_seq / 1e9,
+                                     "content": "files cut from one 96 MiB mixture pool (first 8 KiB fresh)"},
+                 "block_group_e2e": {"value": btotal / bwall / 1e9, "unit": "GB/s", "files": len(blens),
+                                     "input_bytes": btotal, "block": 16384}}
     hbm, src = peaks()
     tiles_ms = kern.get("k_stream_tiles", 0.0)
     d2h = int(cap) * 256 + len(lens) * 24 + (64 << 20)
@@ -1128,13 +1142,7 @@ def main_index_build(args):
             "e2e": {"value": total / wall / 1e9, "unit": "GB/s", "h2d_bytes_per_step": total + (64 << 20),
                     "d2h_bytes_per_step": d2h, "ms_per_step": wall * 1e3,
                     "path": "sdbfg_digest_batch_index from pinned host memory"},
-            "sequential_commit_e2e": {"value": total / wall_seq / 1e9, "unit": "GB/s",
-                                      "path": "the same call with index rounds off (one-warp commit)"},
-            "shared_pool_e2e": {"value": ptotal / pwall / 1e9, "unit": "GB/s", "index_rounds": prounds,
-                                "sequential_commit": ptotal / pwall_seq / 1e9,
-                                "content": "files cut from one 96 MiB mixture pool (first 8 KiB fresh)"},
-            "block_group_e2e": {"value": btotal / bwall / 1e9, "unit": "GB/s", "files": len(blens),
-                                "input_bytes": btotal, "block": 16384},
+            **extra,
             "cpu_baseline": {"value": sample_bytes / t_cpu / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
                              "sample": f"the group's first {pre} files ({sample_bytes} bytes), oracle index build",
                              "seconds": round(t_cpu, 3)}}
