@@ -153,6 +153,7 @@ struct sdbfg_ctx {
     int depth = 3;  // launch groups in flight
     DevBuf d_binfo, d_boff, d_total, d_phase;
     cudaEvent_t ev_scan[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev_tiles[3] = {nullptr, nullptr, nullptr};  // a group's tile kernels done
     cudaEvent_t ev_start = nullptr;
     // comparison engine: tuning and cached plans (work units + CUDA graph)
     int mat_variant = kMatVariantTc;  // tensor-core counting

@@ -75,6 +75,8 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
     }
     for (cudaEvent_t e : c->ev_scan)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->ev_tiles)
+        if (e) cudaEventDestroy(e);
     if (c->ev_start) cudaEventDestroy(c->ev_start);
     c->h_stage.release();
     timer_collect(c);
@@ -352,6 +354,7 @@ static int ensure_pipeline(sdbfg_ctx* c) {
             CUDA_TRY(c, cudaStreamCreateWithFlags(&c->slot[k].stream, cudaStreamNonBlocking));
             CUDA_TRY(c, cudaEventCreateWithFlags(&c->slot[k].done, cudaEventDisableTiming));
             CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_scan[k], cudaEventDisableTiming));
+            CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_tiles[k], cudaEventDisableTiming));
         }
     }
     if (!c->ev_start) CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming));
@@ -470,7 +473,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
     CUDA_TRY(c, cudaMemsetAsync(c->d_total.p, 0, 64, c->stream));
     CUDA_TRY(c, cudaEventRecord(c->ev_start, c->stream));
     const std::vector<Group> groups = make_groups(lens, n, 0, host_data ? kFirstHostGroupBytes : kMaxBytesPerLaunch);
-    cudaEvent_t prev_scan = c->ev_start;
+    cudaEvent_t prev_scan = c->ev_start, prev_tiles = c->ev_start;
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
         const int depth = ib ? 1 : std::max(1, std::min(c->depth, kSlots));
@@ -581,6 +584,11 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         P.out_info = c->d_binfo.as<FileInfoDev>() + g.first;
         P.chunk_redo = S.redo.as<uint32_t>();
         const uint32_t cap_grid = (uint32_t)c->sms * 3 * 16;
+        // the groups' tile kernels run one after another (each fills the GPU),
+        // so a group's commit overlaps the next group's tiles instead of all
+        // groups in flight finishing their tiles together and then waiting
+        // on their commits
+        CUDA_TRY(c, cudaStreamWaitEvent(st, prev_tiles, 0));
         if (P.ntiles)
             TIMED_LAUNCH_ON(c, "k_stream_tiles", st, launch_stream_tiles(P, std::min<uint32_t>(P.ntiles, cap_grid), st));
         if (P.nchunks) {
@@ -588,6 +596,8 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             TIMED_LAUNCH_ON(c, "k_stream_fix", st,
                             launch_stream_fix(P, std::min<uint32_t>(P.nchunks, cap_grid), st));
         }
+        CUDA_TRY(c, cudaEventRecord(c->ev_tiles[gi % depth], st));
+        prev_tiles = c->ev_tiles[gi % depth];
         if (ib) {
             P.index_bits = ib->bits;
             P.index_mask = ib->mask;
