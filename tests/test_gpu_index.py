@@ -213,3 +213,45 @@ def test_cli_index_matches_reference_group(ctx, tmp_path, monkeypatch):
     out = np.zeros(64 << 20, dtype=np.uint8)
     assert lib().sdbfg_lz4_decode(raw[nl + 1:], len(raw) - nl - 1, out.ctypes.data, out.size) == int(head[5])
     assert hashlib.sha256(out.tobytes()).hexdigest() == rec["filter_sha256"]
+
+
+@pytest.mark.parametrize("dd", [0, 16384], ids=["stream", "block"])
+def test_index_build_in_two_calls(ctx, oracle, dd):
+    """An index built over a group in two calls (the second starting from
+    the first call's bits and element count) gives the digests, bits and
+    count of one call over the whole group: the second call's features see
+    the first call's bits as set before them.  Files below 512 bytes are
+    too small and leave the index alone."""
+    from sdhash_gb300 import synth
+    pool = synth.mixture_bytes(98, 0, 3 << 20)
+    rng = np.random.default_rng(98)
+    bufs = []
+    for i in range(24):
+        n = int(rng.integers(20_000, 400_000))
+        o = int(rng.integers(0, pool.size - n))
+        b = pool[o:o + n].copy()
+        b[:2048] = synth.random_bytes(98, i + 1, 2048)
+        bufs.append(b)
+    bufs[5] = synth.random_bytes(98, 100, 300)    # too small
+    bufs[17] = synth.random_bytes(98, 101, 511)   # too small
+    names = [f"t{i}" for i in range(len(bufs))]
+    whole = np.zeros(64 << 20, dtype=np.uint8)
+    d_all, ec_all = ctx.digest_index(bufs, names, dd, whole)
+    assert d_all[5] is None and d_all[17] is None
+    split = np.zeros(64 << 20, dtype=np.uint8)
+    d1, ec1 = ctx.digest_index(bufs[:10], names[:10], dd, split)
+    d2, ec2 = ctx.digest_index(bufs[10:], names[10:], dd, split, ec1)
+    assert ec2 == ec_all and np.array_equal(split, whole)
+    for a, b in zip(d_all, d1 + d2):
+        assert (a is None) == (b is None)
+        if a is not None:
+            assert a.to_string() == b.to_string()
+    if dd == 0:
+        # the oracle's sequential build agrees
+        obits = np.zeros(64 << 20, dtype=np.uint8)
+        want, oec = oracle.index_build_stream(bufs, names, obits)
+        assert oec == ec_all and np.array_equal(obits, whole)
+        for a, w in zip(d_all, want):
+            assert (a is None) == (w is None)
+            if a is not None:
+                assert a.to_string() == w.to_string()
