@@ -66,6 +66,7 @@ struct TileSmem {
     uint32_t* list;        // selected positions (relative to t0)
     uint64_t* sig;         // per-segment entry state
     uint64_t* tau;         // per-segment exit state
+    uint32_t* own;         // block mode, insert phase: 2,048 owner masks over dead space
     uint32_t* misc;        // scalars
 };
 
@@ -92,13 +93,25 @@ __host__ __device__ inline uint32_t phase3_bytes(uint32_t Lmax) {
            align_up(Lmax + 16, 16) + align_up(((Lmax + 64) / 15 + 8) * 4, 16) + 2 * kSegs * 8;
 }
 
+// Offset in the union of the block-mode insert's owner table (8 KiB): the
+// full-rescan table when it is that large (dead once the scores are
+// known), else past the phase-3 layout.
+constexpr uint32_t kOwnBytes = 2048 * 4;
+__host__ __device__ inline uint32_t own_offset(uint32_t Lmax) {
+    return align_up(padded_len(Lmax + 64 + kLead) * 2, 16) >= kOwnBytes ? 0u : phase3_bytes(Lmax);
+}
+
+__host__ __device__ inline uint32_t union_bytes(uint32_t Lmax) {
+    const uint32_t hist = 256 * kRankThreads, p3 = phase3_bytes(Lmax), own = own_offset(Lmax) + kOwnBytes;
+    return max(max(hist, p3), own);
+}
+
 __host__ __device__ inline uint32_t tile_smem_bytes(uint32_t Lmax) {
     const uint32_t span = Lmax + 64 + kLead + 64;           // rank positions
     uint32_t b = 0;
     b += align_up(span + 64 + 16, 16);                       // bytes
     b += align_up(padded_len(span) * 2, 16);                 // ranks
-    const uint32_t hist = 256 * kRankThreads, p3 = phase3_bytes(Lmax);
-    b += hist > p3 ? hist : p3;                              // union
+    b += union_bytes(Lmax);                                  // union
     b += 64 * 4;                                             // misc
     return b;
 }
@@ -117,8 +130,8 @@ __device__ inline TileSmem carve(uint8_t* base, uint32_t Lmax) {
     s.list = reinterpret_cast<uint32_t*>(u); u += align_up(((Lmax + 64) / 15 + 8) * 4, 16);
     s.sig = reinterpret_cast<uint64_t*>(u); u += kSegs * 8;
     s.tau = reinterpret_cast<uint64_t*>(u); u += kSegs * 8;
-    const uint32_t hist = 256 * kRankThreads, p3 = phase3_bytes(Lmax);
-    p += hist > p3 ? hist : p3;
+    s.own = reinterpret_cast<uint32_t*>(p + own_offset(Lmax));
+    p += union_bytes(Lmax);
     s.misc = reinterpret_cast<uint32_t*>(p);
     return s;
 }
@@ -1144,6 +1157,11 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
         __syncthreads();
         const uint32_t k = (uint32_t)state[0];
         const uint32_t ncand = compact(s, nown, k, true, counts);
+        // owner masks of the insert passes, over space dead once the scores
+        // are known
+        uint32_t* own = s.own;
+        for (uint32_t i = threadIdx.x; i < 2048; i += blockDim.x) own[i] = 0;
+        __syncthreads();
         for (uint32_t base = 0; base < ncand; base += blockDim.x) {
             if (state[3]) break;
             const uint32_t ci = base + threadIdx.x;
@@ -1156,38 +1174,97 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
                 for (int q = 0; q < 5; q++) hsh[threadIdx.x][q] = h[q];
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                // gen_block_hash ordered insert (sdbf_core.cc:157-183)
+            if (threadIdx.x < 32) {
+                // gen_block_hash ordered insert (sdbf_core.cc:157-183) by warp 0,
+                // 32 candidates per pass: a candidate is eligible if its score
+                // is above k, or equal to k while `allowed` lasts; an eligible
+                // one sets its 5 filter bits and is counted if one was new.
+                // A pass takes every lane as eligible, then keeps the lanes
+                // before the first one that was counted past the allowance
+                // (that lane is skipped and the rest re-run with the allowance
+                // spent) and stops after the lane that reaches 192.
+                const uint32_t lane = threadIdx.x;
                 int allowed = state[1];
                 int hashed = state[2];
                 const uint32_t lim = min(ncand - base, (uint32_t)blockDim.x);
-                for (uint32_t q = 0; q < lim && hashed < kMaxElemDD; q++) {
-                    const uint32_t v = sc[s.list[base + q]];
-                    if (!(v > k || (v == k && allowed > 0))) continue;
-                    uint32_t added = 0;
-                    for (int z = 0; z < 5; z++) {
-                        const uint32_t idx = hsh[q][z] & kBfMask;
-                        const uint32_t bit = 1u << (idx & 31);
-                        if (!(filt[idx >> 5] & bit)) added++;
-                        filt[idx >> 5] |= bit;
-                    }
-                    if (!added) continue;
-                    if (P.feats) {  // index build: every counted feature (sdbf_core.cc:164-167)
-                        uint32_t* fw = P.feats + (size_t)C.filter * kFeatWords + hashed * 5;
+                for (uint32_t g0 = 0; g0 < lim && hashed < kMaxElemDD; g0 += 32) {
+                    const uint32_t q = g0 + lane;
+                    const bool have = q < lim;
+                    const bool isK = have && sc[s.list[base + (have ? q : 0)]] == k;
+                    uint32_t a[5];
 #pragma unroll
-                        for (int z = 0; z < 5; z++) fw[z] = hsh[q][z];
-                    }
-                    if (P.probes && (hashed & 3) == 0) {  // index search sample (sdbf_core.cc:168-175)
-                        uint32_t* pr = P.probes + (size_t)C.filter * kProbeWords + (hashed >> 2) * 5;
+                    for (int z = 0; z < 5; z++) a[z] = have ? (hsh[q][z] & kBfMask) : 0u;
+                    uint32_t start = 0;
+                    bool stop = false;
+                    while (true) {
+                        const bool act = have && lane >= start && (!isK || allowed > 0);
+                        if (!__any_sync(0xffffffffu, act)) break;
+                        uint32_t fpre = 0;
+                        if (act) {
 #pragma unroll
-                        for (int z = 0; z < 5; z++) pr[z] = hsh[q][z];
+                            for (int z = 0; z < 5; z++) {
+                                fpre |= ((filt[a[z] >> 5] >> (a[z] & 31)) & 1u) << z;
+                                atomicOr(&own[a[z]], 1u << lane);
+                            }
+                        }
+                        __syncwarp();
+                        uint32_t m[5];
+#pragma unroll
+                        for (int z = 0; z < 5; z++) m[z] = act ? own[a[z]] : 0u;
+                        __syncwarp();
+                        if (act) {
+#pragma unroll
+                            for (int z = 0; z < 5; z++) own[a[z]] = 0;
+                        }
+                        bool added = false;
+#pragma unroll
+                        for (int z = 0; z < 5; z++)
+                            if (act && !((fpre >> z) & 1u) && (uint32_t)(__ffs(m[z]) - 1) == lane) added = true;
+                        const uint32_t cm = __ballot_sync(0xffffffffu, added);
+                        const uint32_t ckm = __ballot_sync(0xffffffffu, added && isK);
+                        const uint32_t le = lanemask_le();
+                        const uint32_t om =
+                            __ballot_sync(0xffffffffu, added && isK && __popc(ckm & le) > allowed);
+                        const uint32_t L = om ? (uint32_t)(__ffs(om) - 1) : 32u;
+                        const uint32_t fm =
+                            __ballot_sync(0xffffffffu, added && hashed + __popc(cm & le) == kMaxElemDD);
+                        const uint32_t H = fm ? (uint32_t)(__ffs(fm) - 1) : 32u;
+                        const uint32_t rx = min(L, H + 1);  // lanes [0, rx) stand
+                        const uint32_t keep = rx >= 32 ? 0xffffffffu : ((1u << rx) - 1u);
+                        if (act && lane < rx) {
+#pragma unroll
+                            for (int z = 0; z < 5; z++) atomicOr(&filt[a[z] >> 5], 1u << (a[z] & 31));
+                            if (added) {
+                                const uint32_t idx = (uint32_t)hashed + __popc(cm & lanemask_lt());
+                                if (P.feats) {  // index build: every counted feature (sdbf_core.cc:164-167)
+                                    uint32_t* fw = P.feats + (size_t)C.filter * kFeatWords + idx * 5;
+#pragma unroll
+                                    for (int z = 0; z < 5; z++) fw[z] = hsh[q][z];
+                                }
+                                if (P.probes && (idx & 3) == 0) {  // index search sample (sdbf_core.cc:168-175)
+                                    uint32_t* pr = P.probes + (size_t)C.filter * kProbeWords + (idx >> 2) * 5;
+#pragma unroll
+                                    for (int z = 0; z < 5; z++) pr[z] = hsh[q][z];
+                                }
+                            }
+                        }
+                        hashed += __popc(cm & keep);
+                        allowed -= __popc(ckm & keep);
+                        __syncwarp();
+                        if (H < L) {  // the 192nd element: the block is full
+                            stop = true;
+                            break;
+                        }
+                        if (L >= 32) break;
+                        start = L + 1;  // lane L is skipped (allowance spent)
                     }
-                    hashed++;
-                    if (v == k) allowed--;
+                    if (stop) break;
                 }
-                state[1] = allowed;
-                state[2] = hashed;
-                if (hashed >= kMaxElemDD) state[3] = 1;
+                if (lane == 0) {
+                    state[1] = allowed;
+                    state[2] = hashed;
+                    if (hashed >= kMaxElemDD) state[3] = 1;
+                }
             }
             __syncthreads();
         }
