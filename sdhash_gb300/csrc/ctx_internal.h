@@ -174,7 +174,7 @@ struct sdbfg_ctx {
     // commit takes over (0: sequential only), rounds the last launch group took
     uint32_t index_max_rounds = 16;
     uint32_t index_rounds_used = 0;
-    DevBuf d_seen[2], d_pred, d_diff;
+    DevBuf d_seen[2], d_pred, d_diff, d_ckpt, d_from;
 };
 
 // A resident index filter (bloom_filter of an index file).

@@ -754,18 +754,44 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
         const GenFile Fd = P.files[file];
         if (Fd.nchunks == 0) continue;
         uint32_t* out = P.out_filters + (size_t)Fd.filter_base * 64;
-        for (uint32_t i = lane; i < 64; i += 32) S.F[i] = 0;
-        for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
         // the file's tiles are one contiguous range
         const GenChunk c0 = P.chunks[Fd.first_chunk];
         const GenChunk cl = P.chunks[Fd.first_chunk + Fd.nchunks - 1];
         const uint32_t t_first = c0.first_tile, t_end = cl.first_tile + cl.ntiles;
         uint32_t chunk = Fd.first_chunk;
         uint32_t next_chunk_tile = (Fd.nchunks > 1) ? P.chunks[chunk + 1].first_tile : 0xFFFFFFFFu;
-        if (kMode == kCommitRound && P.commit_dirty && t_first < t_end) {
-            // clear the file's seen bits, ordinals [t_first, t_end) * kTileCap;
+        uint32_t bf_count = 1, last_count = 0, bigfi = 0;
+        // tiles [ts, t_end) commit now: a later index round restarts from the
+        // last checkpoint at or before the first changed predicate (nothing
+        // before it changed, so the state there is the one recorded)
+        uint32_t ts = t_first;
+        if (kMode == kCommitRound && P.commit_dirty) {
+            const uint32_t from = P.commit_from[file];
+            const uint32_t tc = from == 0xFFFFFFFFu ? 0u : from / kTileCap / kCkptTiles * kCkptTiles;
+            if (tc > t_first && tc < t_end) ts = tc;
+        }
+        if (ts > t_first) {
+            const uint32_t* ck = P.commit_ckpt + (size_t)(ts / kCkptTiles) * kCkptWords;
+            for (uint32_t i = lane; i < 64; i += 32) S.F[i] = ck[i];
+            const uint4* g4 = reinterpret_cast<const uint4*>(ck + 64);
+            for (uint32_t i = lane; i < kBigBytes / 16; i += 32) reinterpret_cast<uint4*>(S.G)[i] = g4[i];
+            bf_count = ck[64 + 4096];
+            last_count = ck[64 + 4096 + 1];
+            bigfi = ck[64 + 4096 + 2];
+            // the chunk holding tile ts - 1, as the loop leaves it
+            while (next_chunk_tile < ts) {
+                chunk++;
+                next_chunk_tile = (chunk + 1 < Fd.first_chunk + Fd.nchunks) ? P.chunks[chunk + 1].first_tile
+                                                                             : 0xFFFFFFFFu;
+            }
+        } else {
+            for (uint32_t i = lane; i < 64; i += 32) S.F[i] = 0;
+            for (uint32_t i = lane; i < kBigBytes / 4; i += 32) S.G[i] = 0;
+        }
+        if (kMode == kCommitRound && P.commit_dirty && ts < t_end) {
+            // clear the file's seen bits, ordinals [ts, t_end) * kTileCap;
             // inner words are the file's alone, edge words shared with neighbours
-            const uint32_t o0 = t_first * kTileCap, o1 = t_end * kTileCap - 1;
+            const uint32_t o0 = ts * kTileCap, o1 = t_end * kTileCap - 1;
             for (uint32_t w = (o0 >> 5) + lane; w <= (o1 >> 5); w += 32) {
                 const uint32_t lo = w == (o0 >> 5) ? (o0 & 31u) : 0u, hi = w == (o1 >> 5) ? (o1 & 31u) : 31u;
                 const uint32_t m = (0xffffffffu >> (31u - hi)) & (0xffffffffu << lo);
@@ -774,23 +800,33 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
             }
             __syncwarp();
         }
-        uint32_t nf_cur = t_first < t_end ? P.tile_out[t_first].count : 0;
-        uint32_t nf_next = t_first + 1 < t_end ? P.tile_out[t_first + 1].count : 0;
-        if (t_first < t_end) stage_tile(S.feat[0], P.features + (size_t)t_first * 5 * kTileCap, nf_cur, lane);
+        uint32_t nf_cur = ts < t_end ? P.tile_out[ts].count : 0;
+        uint32_t nf_next = ts + 1 < t_end ? P.tile_out[ts + 1].count : 0;
+        if (ts < t_end) stage_tile(S.feat[0], P.features + (size_t)ts * 5 * kTileCap, nf_cur, lane);
         // kCommitRound: the tile's predicate words (its <= 472 ordinals span
         // at most 16 words), lane q holding word q; the next tile's in flight
         uint32_t pw_cur = 0, pw_next = 0;
         if (kMode == kCommitRound) {
-            if (t_first < t_end && lane < 16) pw_cur = __ldg(P.index_pred + ((t_first * kTileCap) >> 5) + lane);
-            if (t_first + 1 < t_end && lane < 16)
-                pw_next = __ldg(P.index_pred + (((t_first + 1) * kTileCap) >> 5) + lane);
+            if (ts < t_end && lane < 16) pw_cur = __ldg(P.index_pred + ((ts * kTileCap) >> 5) + lane);
+            if (ts + 1 < t_end && lane < 16) pw_next = __ldg(P.index_pred + (((ts + 1) * kTileCap) >> 5) + lane);
         }
         __syncwarp();
-        uint32_t bf_count = 1, last_count = 0, bigfi = 0;
         long long t_file = clock64(), t_wait = 0;
         uint32_t n_groups = 0, n_loops = 0;
-        for (uint32_t t = t_first; t < t_end; t++) {
-            const uint32_t cur = (t - t_first) & 1u;
+        for (uint32_t t = ts; t < t_end; t++) {
+            const uint32_t cur = (t - ts) & 1u;
+            if (kMode == kCommitRound && t > ts && t % kCkptTiles == 0) {
+                // checkpoint of the state entering tile t
+                uint32_t* ck = P.commit_ckpt + (size_t)(t / kCkptTiles) * kCkptWords;
+                for (uint32_t i = lane; i < 64; i += 32) ck[i] = S.F[i];
+                uint4* g4 = reinterpret_cast<uint4*>(ck + 64);
+                for (uint32_t i = lane; i < kBigBytes / 16; i += 32) g4[i] = reinterpret_cast<const uint4*>(S.G)[i];
+                if (lane == 0) {
+                    ck[64 + 4096] = bf_count;
+                    ck[64 + 4096 + 1] = last_count;
+                    ck[64 + 4096 + 2] = bigfi;
+                }
+            }
             // chunk boundary: the big-filter counter is local to each chunk
             // (sdbf_core.cc:100); the big filter itself continues
             while (t >= next_chunk_tile) {
@@ -1078,7 +1114,8 @@ __global__ void k_stream_index_mark(const uint32_t* __restrict__ feats, const Ti
 
 __global__ void k_pred_dirty(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t nwords,
                              const GenTile* __restrict__ tiles, const GenChunk* __restrict__ chunks, uint32_t ntiles,
-                             uint8_t* __restrict__ dirty, unsigned int* __restrict__ ndirty) {
+                             uint8_t* __restrict__ dirty, uint32_t* __restrict__ from,
+                             unsigned int* __restrict__ ndirty) {
     for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nwords;
          w += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t x = a[w] ^ b[w];
@@ -1088,6 +1125,7 @@ __global__ void k_pred_dirty(const uint32_t* __restrict__ a, const uint32_t* __r
             const uint64_t t = ord / kTileCap;
             if (t >= ntiles) continue;
             const uint32_t f = chunks[tiles[t].chunk].file;
+            atomicMin(from + f, (uint32_t)ord);
             if (!dirty[f]) {
                 dirty[f] = 1;
                 atomicAdd(ndirty, 1u);
@@ -1341,8 +1379,8 @@ cudaError_t launch_stream_index_mark(const GenParams& P, const uint32_t* seen, c
 }
 
 cudaError_t launch_pred_dirty(const GenParams& P, const uint32_t* a, const uint32_t* b, uint64_t nwords,
-                              uint8_t* dirty, unsigned int* ndirty, uint32_t grid, cudaStream_t st) {
-    k_pred_dirty<<<grid, 256, 0, st>>>(a, b, nwords, P.tiles, P.chunks, P.ntiles, dirty, ndirty);
+                              uint8_t* dirty, uint32_t* from, unsigned int* ndirty, uint32_t grid, cudaStream_t st) {
+    k_pred_dirty<<<grid, 256, 0, st>>>(a, b, nwords, P.tiles, P.chunks, P.ntiles, dirty, from, ndirty);
     return cudaGetLastError();
 }
 

@@ -103,8 +103,13 @@ struct GenParams {
     const uint32_t* index_pred;
     uint32_t* index_seen;
     // rounds after the first: only files flagged here commit again (their
-    // seen bits are cleared first); null = every file
+    // seen bits are cleared first); null = every file.  commit_from: the
+    // first feature ordinal whose predicate changed, per file; a file
+    // restarts from the checkpoint (commit_ckpt, one per kCkptTiles tiles)
+    // at or before it
     const uint8_t* commit_dirty;
+    const uint32_t* commit_from;
+    uint32_t* commit_ckpt;
 };
 
 // Index search samples counted features 0, 4, 8, ... of a block
@@ -146,7 +151,11 @@ cudaError_t launch_stream_index_mark(const GenParams& P, const uint32_t* seen, c
 // differs between pred words a and b (nwords words); *ndirty counts flags
 // set (at least once per flagged file).
 cudaError_t launch_pred_dirty(const GenParams& P, const uint32_t* a, const uint32_t* b, uint64_t nwords,
-                              uint8_t* dirty, unsigned int* ndirty, uint32_t grid, cudaStream_t st);
+                              uint8_t* dirty, uint32_t* from, unsigned int* ndirty, uint32_t grid, cudaStream_t st);
+// Commit-state checkpoints of the index rounds: every kCkptTiles tiles the
+// 256-byte filter, the big filter and bf_count / last_count / big-filter count.
+constexpr uint32_t kCkptTiles = 32;
+constexpr uint32_t kCkptWords = 64 + 4096 + 4;
 cudaError_t launch_block(const GenParams& P, uint32_t grid, cudaStream_t st);
 
 }  // namespace sdbfg

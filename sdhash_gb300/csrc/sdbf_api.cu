@@ -63,7 +63,8 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
                       &c->d_pairs, &c->d_scores, &c->d_binfo, &c->d_boff, &c->d_total, &c->d_phase,
                       &c->d_match_counts, &c->d_match_offs, &c->d_matches, &c->d_mphase, &c->d_probes,
                       &c->d_nprobes, &c->d_hits, &c->d_index_tab, &c->d_feats, &c->d_idx_bits, &c->d_idx_first,
-                      &c->d_idx_count, &c->d_seen[0], &c->d_seen[1], &c->d_pred, &c->d_diff})
+                      &c->d_idx_count, &c->d_seen[0], &c->d_seen[1], &c->d_pred, &c->d_diff, &c->d_ckpt,
+                      &c->d_from})
         b->release();
     for (auto& S : c->slot) {
         for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work,
@@ -390,6 +391,10 @@ static int commit_with_index(sdbfg_ctx* c, GenParams P, uint32_t cap_grid, cudaS
         const uint64_t nwords = nfeat / 32 + 2, nbits = (uint64_t)P.index_mask + 1;
         for (DevBuf* b : {&c->d_seen[0], &c->d_seen[1], &c->d_pred}) CUDA_TRY(c, b->ensure(nwords * 4));
         CUDA_TRY(c, c->d_diff.ensure(8 + std::max<uint64_t>(1, P.nfiles)));
+        CUDA_TRY(c, c->d_from.ensure(std::max<uint64_t>(1, P.nfiles) * 4));
+        CUDA_TRY(c, c->d_ckpt.ensure(((uint64_t)P.ntiles / kCkptTiles + 1) * kCkptWords * 4));
+        P.commit_ckpt = c->d_ckpt.as<uint32_t>();
+        P.commit_from = c->d_from.as<uint32_t>();
         CUDA_TRY(c, c->d_idx_first.ensure(nbits * 4));
         uint32_t* first = c->d_idx_first.as<uint32_t>();
         uint32_t* seen = c->d_seen[0].as<uint32_t>();
@@ -421,8 +426,10 @@ static int commit_with_index(sdbfg_ctx* c, GenParams P, uint32_t cap_grid, cudaS
             TIMED_LAUNCH_ON(c, "k_stream_index_pred", st,
                             launch_stream_index_pred(P, first, pred[cur ^ 1], fgrid, st));
             CUDA_TRY(c, cudaMemsetAsync(c->d_diff.p, 0, 8 + P.nfiles, st));
+            CUDA_TRY(c, cudaMemsetAsync(c->d_from.p, 0xFF, (size_t)P.nfiles * 4, st));
             TIMED_LAUNCH_ON(c, "k_pred_dirty", st,
-                            launch_pred_dirty(P, pred[cur], pred[cur ^ 1], pwords, dirty, ndirty, wgrid, st));
+                            launch_pred_dirty(P, pred[cur], pred[cur ^ 1], pwords, dirty, c->d_from.as<uint32_t>(),
+                                              ndirty, wgrid, st));
             unsigned int nd = 0;
             CUDA_TRY(c, cudaMemcpyAsync(&nd, ndirty, 4, cudaMemcpyDeviceToHost, st));
             CUDA_TRY(c, cudaStreamSynchronize(st));
