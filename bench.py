@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--max-bytes", type=int, default=64 << 20, help="largest file")
     ap.add_argument("--cpu-sample-gib", type=float, default=3.0)
+    ap.add_argument("--plain-gib", type=float, default=2.0,
+                    help="stream: sample timed through the plain per-file GPU path (0: off)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="stream", choices=["stream", "allpairs", "image", "serve", "load", "index",
                                                          "index-build"],
@@ -223,30 +225,100 @@ def profiled_traffic(kernel: str):
     return None
 
 
-def cpu_baseline(args, data, offs, sizes, nthreads=None, seed=7):
-    """The oracle port of sdhash's generation (file-parallel on all host
-    threads, as sdhash -p N) on a bounded random sample of the workload."""
-    from oracle import Oracle
-    O = Oracle()
+def sample_files(sizes, gib: float, seed: int):
+    """Indices of files drawn at random until they hold `gib` GiB."""
     rng = np.random.default_rng(seed)
-    order = rng.permutation(len(sizes))
-    target = int(args.cpu_sample_gib * (1 << 30))
+    target = int(gib * (1 << 30))
     pick, tot = [], 0
-    for i in order:
+    for i in rng.permutation(len(sizes)):
         if tot >= target:
             break
         pick.append(int(i))
         tot += int(sizes[i])
+    return pick, tot
+
+
+def cpu_baseline(args, data, offs, sizes, nthreads=None, seed=7, keep=False):
+    """The oracle port of sdhash's generation (file-parallel on all host
+    threads, as sdhash -p N) on a bounded random sample of the workload.
+    keep=True also returns the sample's indices and oracle digests (the
+    parity check of the GPU output reads them after the timing)."""
+    from oracle import Oracle
+    O = Oracle()
+    pick, tot = sample_files(sizes, args.cpu_sample_gib, seed)
     nt = nthreads or (os.cpu_count() or 1)
     bufs = [data[int(offs[i]):int(offs[i]) + int(sizes[i])] for i in pick]
     t0 = time.perf_counter()
     res = O.digest_many(bufs, 0, nt)
     dt = time.perf_counter() - t0
     assert all(r is not None or int(sizes[i]) < 512 for r, i in zip(res, pick))
-    del res
-    return {"value": tot / dt / 1e9, "unit": UNIT, "cores": nt, "kind": "port",
+    info = {"value": tot / dt / 1e9, "unit": UNIT, "cores": nt, "kind": "port",
             "sample": f"{len(pick)} files, {tot / (1 << 30):.2f} GiB drawn at random from the same workload",
             "seconds": round(dt, 3)}
+    if keep:
+        return info, pick, res
+    del res
+    return info
+
+
+def parity_vs_oracle(pick, oracle_res, sizes, dev_res, out_host):
+    """Files of the oracle sample whose GPU digest (filters, bf_count,
+    last_count of the timed step's device output) differs from the oracle's."""
+    bad, nbytes = [], 0
+    for i, od in zip(pick, oracle_res):
+        r = dev_res[i]
+        nbytes += int(sizes[i])
+        if od is None:
+            if r.status == 0:
+                bad.append(i)
+            continue
+        got = out_host[r.filter_offset * 256:(r.filter_offset + r.bf_count) * 256].tobytes()
+        if r.status != 0 or (r.bf_count, r.last_count) != (od.bf_count, od.last_count) or got != od.filters():
+            bad.append(i)
+    return bad, nbytes
+
+
+def parity_host_vs_device(res_dev, out_dev_host, res_host, out_host, n):
+    """Files whose host-buffer C-ABI result differs from the device-resident one."""
+    bad = []
+    for i in range(n):
+        a, b = res_dev[i], res_host[i]
+        if (a.status, a.bf_count, a.last_count) != (b.status, b.bf_count, b.last_count):
+            bad.append(i)
+            continue
+        if a.status == 0:
+            x = out_dev_host[a.filter_offset * 256:(a.filter_offset + a.bf_count) * 256]
+            y = out_host[b.filter_offset * 256:(b.filter_offset + b.bf_count) * 256]
+            if not np.array_equal(x, y):
+                bad.append(i)
+    return bad
+
+
+def plain_per_call(ctx, dev, offs, sizes, gib: float, seed: int = 11):
+    """The plain per-file GPU path: one sdbfg_digest_batch_device call per
+    file (as the reference's worker threads build one sdbf per file,
+    sdhash_threads.cc:152-186), on a random sample of the workload with the
+    inputs already in HBM.  Returns the sample's GB/s and description."""
+    import torch
+    pick, tot = sample_files(sizes, gib, seed)
+    cap = max(ctx.capacity([int(sizes[i])], 0) for i in pick)
+    out = torch.empty(max(1, cap) * 256, dtype=torch.uint8, device="cuda")
+    base = dev.data_ptr()
+
+    def one(i):
+        return ctx.digest_device(base + int(offs[i]), [0], [int(sizes[i])], 0, out.data_ptr(), cap)
+
+    for i in pick[:4]:
+        one(i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in pick:
+        one(i)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"value": tot / dt / 1e9, "unit": UNIT, "calls": len(pick), "seconds": round(dt, 3),
+            "sample": f"{len(pick)} files, {tot / (1 << 30):.2f} GiB drawn at random from the same workload, "
+                      "one sdbfg_digest_batch_device call per file (inputs in HBM)"}
 
 
 def run_reference(args):
@@ -395,7 +467,7 @@ def main_allpairs(args):
     assert [int(x) for x in cpu_scores] == [int(x) for x in scores[idx[: len(ci)]]], "oracle and GPU scores differ"
     cpu_work = int(sum(int(counts[a]) * int(counts[b]) for a, b in zip(ci, cj)))
 
-    e2e = None
+    e2e, e2e_bad = None, None
     if not args.no_e2e:
         # public host API: upload the set (H2D), all pairs, scores back (D2H)
         torch.cuda.synchronize()
@@ -1293,6 +1365,8 @@ def main():
     clocks.stop()
     dev_ms = e0.elapsed_time(e1)
     launches = ctx.launch_count - launches0
+    # the last timed step's device output and results, for the parity checks
+    out_dev_host = out.cpu().numpy()
 
     # One more step, outside the timed region, with launch groups run one
     # after another and per-kernel CUDA events on the launch stream: the
@@ -1313,11 +1387,12 @@ def main():
     bytes_all = allsum(world, total_bytes)
     value = bytes_all / (ms_per_step / 1e3) / 1e9
     out_filters = sum(int(r.bf_count) for r in res[: len(sizes)]) if len(sizes) else 0
+    plain = plain_per_call(ctx, dev, offs, sizes, args.plain_gib) if args.plain_gib > 0 else None
 
     # e2e through the C ABI's host-buffer entry point (sdbfg_digest_batch):
     # the caller's pinned input in, the packed filters and per-file results
     # out into the caller's host buffers, every step
-    e2e = None
+    e2e, e2e_bad = None, None
     if not args.no_e2e:
         import ctypes as C
         from sdhash_gb300 import DigestResult, lib, _ptr, _u64
@@ -1340,6 +1415,7 @@ def main():
         torch.cuda.synchronize()
         e2e_s = allmax(world, (time.perf_counter() - t0) / args.steps)
         d2h = sum(int(res_c[i].bf_count) for i in range(nf) if res_c[i].status == 0) * 256 + C.sizeof(res_c)
+        e2e_bad = parity_host_vs_device(res, out_dev_host, res_c, out_host, nf)
         # the Python object API on the same batch, once (Digest objects built on the host)
         t1 = time.perf_counter()
         ds = ctx.digest_packed(data, offs, sizes, 0)
@@ -1370,8 +1446,25 @@ def main():
                            parallelism=f"files sharded over {world} GPU(s)", wall_s_timed=round(wall, 3),
                            out_filters_per_step=out_filters),
             "gpu_launches": launches, "clocks": clocks.summary(), "roofline": roofline, "e2e": e2e}
+    if plain:
+        line["plain_per_call"] = plain
+        line["batched_over_plain"] = value / plain["value"]
+    parity = {"files_checked": 0, "mismatches": 0}
     if rank == 0 and world == 1:
-        line["cpu_baseline"] = cpu_baseline(args, data, offs, sizes)
+        cb, pick, ores = cpu_baseline(args, data, offs, sizes, keep=True)
+        line["cpu_baseline"] = cb
+        bad, nb = parity_vs_oracle(pick, ores, sizes, res, out_dev_host)
+        del ores
+        parity.update(files_checked=len(pick), mismatches=len(bad), bytes_checked=nb,
+                      checked="oracle digests of the cpu_baseline sample against the last timed step's device "
+                              "output (filters, bf_count, last_count)")
+        if bad:
+            parity["mismatched_files"] = bad[:16]
+    if e2e_bad is not None:
+        parity.update(e2e_files_checked=len(sizes), e2e_mismatches=len(e2e_bad),
+                      e2e_checked="every file: sdbfg_digest_batch host output against the device-resident output")
+        parity["mismatches"] += len(e2e_bad)
+    line["parity"] = parity
     if rank == 0:
         print(json.dumps(line), flush=True)
     barrier(world)

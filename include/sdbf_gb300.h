@@ -145,8 +145,10 @@ int sdbfg_digest_batch_device(sdbfg_ctx *ctx, const uint8_t *dev_data, const uin
  * returns after the work is complete.
  * The first call on a device resolves the scratch array's device address
  * and loads the digest tables into it; make that first call before any
- * stream capture.  All calls share the one array: calls whose work overlaps
- * on the GPU race and corrupt each other's results -- serialise them. */
+ * stream capture.  That set-up is not repeated: after cudaDeviceReset on a
+ * device this entry point must not be used on it again in the process.
+ * All calls share the one array: calls whose work overlaps on the GPU race
+ * and corrupt each other's results -- serialise them. */
 #define SDBFG_NOALLOC_MAX_INPUTS 256u
 #define SDBFG_NOALLOC_MAX_INPUT_BYTES (8ull << 20)
 #define SDBFG_NOALLOC_SCRATCH_BYTES (14ull << 20)

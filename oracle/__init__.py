@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle_sdbf.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libsdbf_ref.so")
-REFERENCE_SRC = os.environ.get("SDHASH_REFERENCE_SRC", "/root/reference")
+REFERENCE_SRC = os.environ.get("SDHASH_REFERENCE_SRC", "")
 
 
 def build_oracle(quiet: bool = True) -> str:
@@ -30,13 +30,15 @@ def build_oracle(quiet: bool = True) -> str:
     return ORACLE_SO
 
 
-def build_reference(quiet: bool = True) -> str | None:
+def build_reference(quiet: bool = True, src: str | None = None) -> str | None:
     """Compile the reference from its sources into oracle/_ref (only where the
-    reference tree exists; it does not travel to other machines)."""
-    if not os.path.isdir(os.path.join(REFERENCE_SRC, "sdbf")):
+    reference tree exists; it does not travel to other machines).  The tree
+    is `src`, else $SDHASH_REFERENCE_SRC; neither set: nothing is built."""
+    src = src or REFERENCE_SRC
+    if not src or not os.path.isdir(os.path.join(src, "sdbf")):
         return None
     repo = os.path.dirname(HERE)
-    out = subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile.ref", f"REF={REFERENCE_SRC}"],
+    out = subprocess.run(["make", "-s", "-j8", "-f", "oracle/Makefile.ref", f"REF={src}"],
                          cwd=repo, capture_output=quiet, text=True)
     if out.returncode != 0:
         raise RuntimeError("reference build failed:\n" + (out.stdout or "") + (out.stderr or ""))

@@ -769,6 +769,7 @@ __device__ __forceinline__ void commit_files(const GenParams& P, uint8_t* smem) 
             const uint32_t from = P.commit_from[file];
             const uint32_t tc = from == 0xFFFFFFFFu ? 0u : from / kTileCap / kCkptTiles * kCkptTiles;
             if (tc > t_first && tc < t_end) ts = tc;
+            if (P.phase && lane == 0 && ts > t_first) atomicAdd(P.phase + kPhCkptRestarts, 1ull);
         }
         if (ts > t_first) {
             const uint32_t* ck = P.commit_ckpt + (size_t)(ts / kCkptTiles) * kCkptWords;

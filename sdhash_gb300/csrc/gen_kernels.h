@@ -121,7 +121,8 @@ constexpr uint32_t kFeatWords = 192 * 5;
 // Phase counters (cycles summed over CTAs / warps) when GenParams::phase is set.
 enum : int {
     kPhLoad = 0, kPhRanks, kPhFres, kPhWalk, kPhLink, kPhCompact, kPhSha, kPhTiles,
-    kPhCommitWait, kPhCommitBusy, kPhCommitGroups, kPhCommitLoops, kPhCommitMaxFile, kPhFixups, kPhCount
+    kPhCommitWait, kPhCommitBusy, kPhCommitGroups, kPhCommitLoops, kPhCommitMaxFile, kPhFixups,
+    kPhCkptRestarts, kPhCount
 };
 
 size_t stream_tile_smem();
@@ -148,8 +149,9 @@ cudaError_t launch_stream_index_first(const GenParams& P, const uint32_t* seen, 
 cudaError_t launch_stream_index_mark(const GenParams& P, const uint32_t* seen, const uint32_t* first, uint32_t grid,
                                      cudaStream_t st);
 // dirty[file] = 1 for every file with a feature whose predicate bit
-// differs between pred words a and b (nwords words); *ndirty counts flags
-// set (at least once per flagged file).
+// differs between pred words a and b (nwords words).  *ndirty is only a
+// nonzero flag: it is zero iff no file was flagged (racing threads may add
+// more than once for the same file, so it is not a file count).
 cudaError_t launch_pred_dirty(const GenParams& P, const uint32_t* a, const uint32_t* b, uint64_t nwords,
                               uint8_t* dirty, uint32_t* from, unsigned int* ndirty, uint32_t grid, cudaStream_t st);
 // Commit-state checkpoints of the index rounds: every kCkptTiles tiles the

@@ -81,7 +81,10 @@ uint8_t* g_scratch_dev[64];  // per device id: device address of g_noalloc_scrat
 int g_sms[64];
 
 // Once per device, with that device current: resolve the array's device
-// address and load the constant tables into it.
+// address and load the constant tables into it.  The address and the tables
+// belong to the device's context at that time: after cudaDeviceReset (or
+// anything else that destroys the primary context) they are stale, so the
+// entry point must not be called again in that process.
 int setup_device(int dev, uint8_t** base, int* sms) {
     if (dev < 0 || dev >= 64) return SDBFG_ERR_ARG;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -120,15 +123,17 @@ extern "C" int sdbfg_digest_stream_noalloc(const uint8_t* dev_data, const uint64
         fprintf(stderr, "sdbfg_digest_stream_noalloc: %u inputs exceed the limit of %u\n", n, kMaxInputs);
         return SDBFG_ERR_CAPACITY;
     }
+    // each length is checked before it is added, so no sum of huge lengths
+    // can wrap below the limit
     uint64_t total = 0;
     for (uint32_t i = 0; i < n; i++) {
         if (offsets[i] % 16) return SDBFG_ERR_ARG;
+        if (lens[i] > kMaxBytes - total) {
+            fprintf(stderr, "sdbfg_digest_stream_noalloc: inputs 0..%u hold more than the limit of %llu bytes\n", i,
+                    (unsigned long long)kMaxBytes);
+            return SDBFG_ERR_CAPACITY;
+        }
         total += lens[i];
-    }
-    if (total > kMaxBytes) {
-        fprintf(stderr, "sdbfg_digest_stream_noalloc: %llu input bytes exceed the limit of %llu\n",
-                (unsigned long long)total, (unsigned long long)kMaxBytes);
-        return SDBFG_ERR_CAPACITY;
     }
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SDBFG_ERR_CUDA;

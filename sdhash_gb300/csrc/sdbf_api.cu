@@ -119,7 +119,7 @@ static const char* kPhaseNames[kPhCount] = {
     "k_stream_tiles.load", "k_stream_tiles.ranks", "k_stream_tiles.fres", "k_stream_tiles.walk",
     "k_stream_tiles.link", "k_stream_tiles.compact", "k_stream_tiles.sha1", "k_stream_tiles.count",
     "k_stream_commit.wait", "k_stream_commit.busy", "k_stream_commit.groups", "k_stream_commit.loops",
-    "k_stream_commit.max_file", "k_stream_tiles.fixups"};
+    "k_stream_commit.max_file", "k_stream_tiles.fixups", "k_stream_commit_round.restarts"};
 
 extern "C" int sdbfg_ctx_kernel_time(sdbfg_ctx* c, const char* name, double* total_ms, uint64_t* launches) {
     if (!c || !name) return SDBFG_ERR_ARG;

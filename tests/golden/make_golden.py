@@ -10,8 +10,8 @@ inputs of tests/cases.py and records what it produces:
   digest and the full ``compare_all`` result text at threshold 1;
 * a block-mode query/target ``compare_to`` result.
 
-Needs the reference tree (only in the build container):
-    python tests/golden/make_golden.py
+Needs the reference source tree (only in the build container):
+    SDHASH_REFERENCE_SRC=<tree> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

@@ -18,8 +18,8 @@ header and the filter's sha256 of each.
 Inputs are seeded synthetic mixture content (sdhash_gb300/synth.py), so the
 GPU tests regenerate them on any machine.
 
-Needs the reference tree (only in the build container):
-    python tests/golden/make_index_golden.py
+Needs the reference source tree (only in the build container):
+    SDHASH_REFERENCE_SRC=<tree> python tests/golden/make_index_golden.py
 """
 from __future__ import annotations
 

@@ -13,8 +13,8 @@ header field that fails boost::lexical_cast (it throws a non-int), no
 block record field shorter than 344 characters (the reference decodes 344
 characters from it regardless).
 
-Needs the reference tree (only in the build container):
-    python tests/golden/make_text_golden.py
+Needs the reference source tree (only in the build container):
+    SDHASH_REFERENCE_SRC=<tree> python tests/golden/make_text_golden.py
 """
 from __future__ import annotations
 

@@ -82,3 +82,10 @@ def test_noalloc_rejects_requests_above_its_limits():
     rc = noalloc(C.c_void_p(16), offs.ctypes.data_as(C.POINTER(C.c_uint64)),
                  lens.ctypes.data_as(C.POINTER(C.c_uint64)), 1, C.c_void_p(16), 1, C.addressof(res), None)
     assert rc == ERR_CAPACITY
+    # two lengths whose 64-bit sum wraps below the limit are rejected too
+    lens2 = np.array([2 ** 64 - 16, 32], dtype=np.uint64)
+    offs2 = np.zeros(2, dtype=np.uint64)
+    res2 = (g.DigestResult * 2)()
+    rc = noalloc(C.c_void_p(16), offs2.ctypes.data_as(C.POINTER(C.c_uint64)),
+                 lens2.ctypes.data_as(C.POINTER(C.c_uint64)), 2, C.c_void_p(16), 1, C.addressof(res2), None)
+    assert rc == ERR_CAPACITY
