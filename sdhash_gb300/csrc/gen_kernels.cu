@@ -58,10 +58,9 @@ struct TileGeom {
 // Shared-memory carve-up for a tile of at most Lmax owned positions.
 struct TileSmem {
     uint32_t* bytes32;     // chunk bytes [Q0, BE) (+pad)
-    uint16_t* ranks;       // ranks [Q0, RE); from the full-rescan phase on, bits 10-15 hold run lengths
+    uint16_t* ranks;       // ranks [Q0, RE)
     uint8_t* hist;         // per-thread byte histograms (phase 2 only)
     uint16_t* fres;        // full-rescan result per step [Q0, SE)
-    uint32_t* eqw;         // run bits: bit o = rank[o]==rank[o+1]
     uint32_t* score32;     // u8 scores of [t0, t0+L) packed 4 per word
     uint32_t* list;        // selected positions (relative to t0)
     uint64_t* sig;         // per-segment entry state
@@ -86,11 +85,10 @@ __device__ __forceinline__ uint32_t hist_off(uint32_t t, uint32_t v) {
 }
 
 // Layout: bytes | ranks | union { histograms (ranks phase) ;
-//                                 fres | run bits | scores | list | sig | tau } | misc
+//                                 fres | scores | list | sig | tau } | misc
 __host__ __device__ inline uint32_t phase3_bytes(uint32_t Lmax) {
-    const uint32_t span = Lmax + 64 + kLead + 64;
-    return align_up(padded_len(Lmax + 64 + kLead) * 2, 16) + align_up((span / 32 + 4) * 4, 16) +
-           align_up(Lmax + 16, 16) + align_up(((Lmax + 64) / 15 + 8) * 4, 16) + 2 * kSegs * 8;
+    return align_up(padded_len(Lmax + 64 + kLead) * 2, 16) + align_up(Lmax + 16, 16) +
+           align_up(((Lmax + 64) / 15 + 8) * 4, 16) + 2 * kSegs * 8;
 }
 
 // Offset in the union of the block-mode insert's owner table (8 KiB): the
@@ -125,7 +123,6 @@ __device__ inline TileSmem carve(uint8_t* base, uint32_t Lmax) {
     uint8_t* u = p;
     s.hist = u;
     s.fres = reinterpret_cast<uint16_t*>(u); u += align_up(padded_len(Lmax + 64 + kLead) * 2, 16);
-    s.eqw = reinterpret_cast<uint32_t*>(u); u += align_up((span / 32 + 4) * 4, 16);
     s.score32 = reinterpret_cast<uint32_t*>(u); u += align_up(Lmax + 16, 16);
     s.list = reinterpret_cast<uint32_t*>(u); u += align_up(((Lmax + 64) / 15 + 8) * 4, 16);
     s.sig = reinterpret_cast<uint64_t*>(u); u += kSegs * 8;
@@ -234,77 +231,64 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
 // smallest non-zero rank m of window [k, k+63], at its leftmost position f,
 // extended right over the run of equal ranks (capped at k+63).  Stored as
 // (m << 6) | (p - k); 0 when rank[k] == 0 (no credit, next step rescans).
+//
+// One thread per aligned 64-step block A (steps base..base+63); the window
+// of step base+u is A[u..63] followed by B[0..u-1], B the next block.
+//  pass 1, u = 63..0: the leftmost minimum of A[u..63] and the end of its
+//    run inside A, as a running state -- a rank equal to the minimum
+//    becomes the new leftmost one, keeping the run end only when its right
+//    neighbour continues the run.  Written to fres[base+u] (0 when
+//    rank[base+u] == 0).
+//  pass 2, v = 0..62: the same state for the prefix B[0..v] (a run end
+//    advances only while the run is contiguous) and the end of B's leading
+//    run; step u = v+1 takes A's minimum on ties (leftmost), continuing its
+//    run into B when it reaches A's last position and B starts with the
+//    same rank.  Both run ends stay within the window, so no cap is needed.
+// Positions past the ranks (the last block's B) count as rank 0.
 __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
     const uint32_t np = g.RE - g.Q0;
-    // run bits
-    const uint32_t nw = (np + 31) / 32;
-    for (uint32_t w = threadIdx.x / 32; w < nw; w += blockDim.x / 32) {
-        const uint32_t o = w * 32 + (threadIdx.x & 31);
-        const bool eq = (o + 1 < np) && s.ranks[pidx(o)] == s.ranks[pidx(o + 1)];
-        const uint32_t bits = __ballot_sync(0xffffffffu, eq);
-        if ((threadIdx.x & 31) == 0) s.eqw[w] = bits;
-    }
-    if (threadIdx.x < 4) s.eqw[nw + threadIdx.x] = 0;
-    __syncthreads();
-    // run lengths: bits 10-15 of each rank entry (ranks are <= 990) hold how
-    // many of the following ranks equal it, capped at 63 (a run that long
-    // reaches the end of any window that starts at or before it)
-    for (uint32_t o = threadIdx.x; o < np; o += blockDim.x) {
-        const uint32_t w = o >> 5, sh = o & 31;
-        const uint32_t lo32 = __funnelshift_r(s.eqw[w], s.eqw[w + 1], sh);
-        const uint32_t hi32 = __funnelshift_r(s.eqw[w + 1], s.eqw[w + 2], sh);
-        const uint64_t bits = ((uint64_t)hi32 << 32) | lo32;
-        const uint32_t len = (~bits == 0ull) ? 63u : min(63u, (uint32_t)__ffsll((long long)~bits) - 1);
-        s.ranks[pidx(o)] = (uint16_t)(s.ranks[pidx(o)] | (len << 10));
-    }
-    __syncthreads();
     const uint32_t nsteps = g.SE - g.Q0;
     const uint32_t nblk = (nsteps + 63) / 64;
+    const uint16_t* __restrict__ R = s.ranks;
+    uint16_t* __restrict__ Fr = s.fres;
     for (uint32_t j = threadIdx.x; j < nblk; j += blockDim.x) {
         const uint32_t base = j * 64;
-        // prefix minima of the next aligned block (keys: rank<<6 | offset;
-        // rank 0 is "infinite" = 1023)
-        uint16_t pre[64];
-        uint32_t run = 0xFFFFu;
-#pragma unroll
-        for (int u = 0; u < 64; u++) {
-            const uint32_t o = base + 64 + u;
-            uint32_t r = (o < np) ? s.ranks[pidx(o)] & 1023u : 0;
-            const uint32_t key = ((r == 0 ? 1023u : r) << 6) | (uint32_t)u;
-            run = min(run, key);
-            pre[u] = (uint16_t)run;
-        }
-        uint32_t suf = 0xFFFFu;
-#pragma unroll
+        const uint32_t ulim = min(64u, nsteps - base);
+        const uint16_t* Ra = R + pidx(base);   // block A (pidx is contiguous inside a block)
+        const uint16_t* Rb = R + pidx(base + 64);
+        uint16_t* Fa = Fr + pidx(base);
+        uint32_t m = 1023, e = 63, rn = 0;
+#pragma unroll 8
         for (int u = 63; u >= 0; u--) {
-            const uint32_t k = base + u;
-            const uint32_t rk = (k < np) ? s.ranks[pidx(k)] & 1023u : 0;
-            suf = min(suf, ((rk == 0 ? 1023u : rk) << 6) | (uint32_t)u);
-            if (k < nsteps) {
-                uint16_t out = 0;
-                if (rk != 0) {
-                    uint32_t f, m;
-                    if (u == 0) {
-                        f = base + (suf & 63);
-                        m = suf >> 6;
-                    } else {
-                        const uint32_t pk = pre[u - 1];
-                        if ((suf >> 6) <= (pk >> 6)) {
-                            f = base + (suf & 63);
-                            m = suf >> 6;
-                        } else {
-                            f = base + 64 + (pk & 63);
-                            m = pk >> 6;
-                        }
-                    }
-                    // end of the run of equal ranks starting at f (f >= k, so a
-                    // run length capped at 63 gives the same cap at k + 63)
-                    uint32_t p = f + (s.ranks[pidx(f)] >> 10);
-                    if (p > k + 63) p = k + 63;
-                    out = (uint16_t)((m << 6) | (p - k));
-                }
-                s.fres[pidx(k)] = out;
+            const uint32_t r = (base + u < np) ? Ra[u] : 0u;
+            const bool take = r != 0 && (r < m || (r == m && rn != m));
+            m = take ? r : m;
+            e = take ? (uint32_t)u : e;
+            rn = r;
+            if ((uint32_t)u < ulim) Fa[u] = r == 0 ? (uint16_t)0 : (uint16_t)((m << 6) | e);
+        }
+        uint32_t pm = 1023, pe = 0, lead_end = 0;
+        const uint32_t rb0 = (base + 64 < np) ? Rb[0] : 0u;
+#pragma unroll 4
+        for (uint32_t v = 0; v + 1 < ulim; v++) {
+            const uint32_t r = (base + 64 + v < np) ? Rb[v] : 0u;
+            lead_end = (v != 0 && r == rb0 && lead_end + 1 == v) ? v : lead_end;
+            const bool lower = r != 0 && r < pm;
+            const bool cont = r != 0 && r == pm && pe + 1 == v;
+            pm = lower ? r : pm;
+            pe = (lower || cont) ? v : pe;
+            const uint32_t u = v + 1;
+            const uint32_t sv = Fa[u];
+            const uint32_t sm = sv >> 6, se = sv & 63;
+            uint32_t mm, p;
+            if (sm <= pm) {
+                mm = sm;
+                p = (se == 63 && rb0 == sm) ? 64 + lead_end : se;
+            } else {
+                mm = pm;
+                p = 64 + pe;
             }
+            Fa[u] = sv == 0 ? (uint16_t)0 : (uint16_t)((mm << 6) | (p - u));
         }
     }
 }
@@ -346,10 +330,9 @@ __device__ __forceinline__ ChainState walk(const TileGeom& g, const TileSmem& s,
     if (a >= b) return st;
     const uint16_t* __restrict__ R = s.ranks;
     const uint16_t* __restrict__ Fr = s.fres;
-    // (rank entries carry a run length in bits 10-15: masked off here)
-    uint32_t r64 = R[pidx(a + 64 - g.Q0)] & 1023u, f = Fr[pidx(a - g.Q0)];
+    uint32_t r64 = R[pidx(a + 64 - g.Q0)], f = Fr[pidx(a - g.Q0)];
     for (uint32_t i = a; i < b; i++) {
-        const uint32_t r64n = R[pidx(i + 65 - g.Q0)] & 1023u, fn = Fr[pidx(i + 1 - g.Q0)];
+        const uint32_t r64n = R[pidx(i + 65 - g.Q0)], fn = Fr[pidx(i + 1 - g.Q0)];
         const bool cheap = (st.M != 0) & (r64 >= st.M) & (i < st.P);
         const uint32_t cheapP = (r64 == st.M) ? i + 64 : st.P;
         st.P = cheap ? cheapP : i + (f & 63);
