@@ -73,7 +73,7 @@ int sdbfg_ctx_kernel_time(sdbfg_ctx *ctx, const char *kernel, double *total_ms, 
  * exercise it.  No counterpart in the reference (its walk is sequential). */
 int sdbfg_ctx_set_lead(sdbfg_ctx *ctx, uint32_t steps);
 /* Stream-mode launch groups (<= 2 GiB of input each) kept in flight on
- * separate streams, 1..3 (default 3): the ordered commit of one group
+ * separate streams, 1..8 (default 3): the ordered commit of one group
  * overlaps the next groups' tile kernels.  Depth 1 runs groups one after
  * another (used to time kernels without overlap).  Tuning knob without a
  * counterpart in the reference. */

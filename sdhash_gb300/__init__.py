@@ -376,7 +376,7 @@ class Context:
         self._check(lib().sdbfg_ctx_set_lead(self.h, steps))
 
     def set_pipeline_depth(self, depth: int):
-        """Stream-mode launch groups in flight (1..3); 1 = no overlap."""
+        """Stream-mode launch groups in flight (1..8); 1 = no overlap."""
         self._check(lib().sdbfg_ctx_set_pipeline_depth(self.h, depth))
 
     def profile(self, enable: bool = True):

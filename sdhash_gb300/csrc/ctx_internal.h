@@ -25,7 +25,7 @@ constexpr uint64_t kMaxBytesPerLaunch = 2ull << 30;
 constexpr uint64_t kFirstHostGroupBytes = 256ull << 20;  // first group of a host-input stream batch
 constexpr uint32_t kMinFile = 512;                 // MIN_FILE_SIZE (sdbf_defines.h:56)
 constexpr uint64_t kPairsPerLaunch = 1ull << 22;
-constexpr int kSlots = 3;  // stream-mode launch groups in flight
+constexpr int kSlots = 8;  // stream-mode launch groups in flight (at most)
 
 // Device / pinned-host arrays that grow on demand and free themselves with
 // their owner (not copyable).
@@ -149,11 +149,11 @@ struct sdbfg_ctx {
         bool used = false;
         DevBuf data, chunks, tiles, files, order, tile_out, features, work, redo;
         HostBuf h_tables;
-    } slot[3];
+    } slot[kSlots];
     int depth = 3;  // launch groups in flight
     DevBuf d_binfo, d_boff, d_total, d_phase;
-    cudaEvent_t ev_scan[3] = {nullptr, nullptr, nullptr};
-    cudaEvent_t ev_tiles[3] = {nullptr, nullptr, nullptr};  // a group's tile kernels done
+    cudaEvent_t ev_scan[kSlots] = {};
+    cudaEvent_t ev_tiles[kSlots] = {};  // a group's tile kernels done
     cudaEvent_t ev_start = nullptr;
     // comparison engine: tuning and cached plans (work units + CUDA graph)
     int mat_variant = kMatVariantTc;  // tensor-core counting

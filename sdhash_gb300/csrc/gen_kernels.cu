@@ -153,77 +153,148 @@ __device__ inline void load_bytes(const uint8_t* __restrict__ chunk, const TileG
 // dtab[c] = T[c+1] - T[c] (c = 0..63): entropy change when a byte value's
 // count in the window goes from c to c+1 (entr64_inc_int, entr64.cc:47-71,
 // written as differences of the table of entr64_table_init_int).
+//
+// Each of kRankThreads threads owns a run of positions starting at a
+// multiple of 8 and keeps the byte counts of its window in its own
+// histogram.  The counts are the only thing carried from step to step, so
+// everything else is moved out of that chain: bytes are read as words a
+// group ahead, two steps share one round of count loads (the second step's
+// counts corrected for the first step in registers), and the eight ranks of
+// a group are stored together as four words.
+__device__ __forceinline__ uint32_t byte_of(uint32_t w, uint32_t k) { return __byte_perm(w, 0, 0x4440u | k); }
+
+// Two window steps: bytes a0, a1 leave, b0, b1 enter; e0 / e1 receive the
+// entropy after each step.
+__device__ __forceinline__ void rank_pair(uint8_t* h, uint32_t hbase, const int32_t* dtab, int32_t& e, uint32_t a0,
+                                          uint32_t b0, uint32_t a1, uint32_t b1, int32_t& e0, int32_t& e1) {
+    const uint32_t ha0 = hbase + ((a0 >> 2) << 7) + (a0 & 3), hb0 = hbase + ((b0 >> 2) << 7) + (b0 & 3);
+    const uint32_t ha1 = hbase + ((a1 >> 2) << 7) + (a1 & 3), hb1 = hbase + ((b1 >> 2) << 7) + (b1 & 3);
+    const int32_t ca0 = h[ha0], cb0 = h[hb0];
+    int32_t ca1 = h[ha1], cb1 = h[hb1];
+    const bool d0 = a0 != b0, d1 = a1 != b1;
+    if (d0) {
+        e += dtab[cb0] - dtab[ca0 - 1];
+        ca1 += (int32_t)(a1 == b0) - (int32_t)(a1 == a0);
+        cb1 += (int32_t)(b1 == b0) - (int32_t)(b1 == a0);
+    }
+    e0 = e;
+    if (d1) e += dtab[cb1] - dtab[ca1 - 1];
+    e1 = e;
+    // later stores win where both steps touch the same byte value
+    if (d0) {
+        h[ha0] = (uint8_t)(ca0 - 1);
+        h[hb0] = (uint8_t)(cb0 + 1);
+    }
+    if (d1) {
+        h[ha1] = (uint8_t)(ca1 - 1);
+        h[hb1] = (uint8_t)(cb1 + 1);
+    }
+}
+
+// One window step: byte a leaves, byte b enters.
+__device__ __forceinline__ void rank_single(uint8_t* h, uint32_t hbase, const int32_t* dtab, int32_t& e, uint32_t a,
+                                            uint32_t b) {
+    if (a != b) {
+        const uint32_t ha = hbase + ((a >> 2) << 7) + (a & 3);
+        const uint32_t hb = hbase + ((b >> 2) << 7) + (b & 3);
+        const uint32_t ca = h[ha], cb = h[hb];
+        h[ha] = (uint8_t)(ca - 1);
+        h[hb] = (uint8_t)(cb + 1);
+        e += dtab[cb] - dtab[ca - 1];
+    }
+}
+
 __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const uint16_t* rank_tab,
                                      const int32_t* dtab) {
     const uint8_t* b8 = reinterpret_cast<const uint8_t*>(s.bytes32);
+    const uint32_t* b32 = s.bytes32;
     const uint32_t np = g.RE - g.Q0;
-    const uint32_t per = (np + kRankThreads - 1) / kRankThreads;
+    const uint32_t per = ((np + kRankThreads - 1) / kRankThreads + 7) & ~7u;
     const uint32_t tid = threadIdx.x;
     if (tid >= (uint32_t)kRankThreads) return;
     uint8_t* h = s.hist;  // counts at hist_off(tid, v) (cleared by the caller)
-    const uint32_t lo = tid * per, hi = min(np, lo + per);
+    const uint32_t lo = min(np, tid * per), hi = min(np, lo + per);
     const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
+    const uint32_t vend = last > g.Q0 ? min(hi, last - g.Q0) : lo;  // [lo, vend): entropy ranks
     const uint32_t hbase = hist_off(tid, 0);
     int32_t e = 0;
     uint32_t r = lo;
-    if (r < hi && g.Q0 + r < last) {
-        // entr64_init_int (entr64.cc:27-41) built incrementally
-        for (int k = 0; k < kWin; k++) {
-            const uint32_t v = b8[r + k];
-            const uint32_t off = hbase + ((v >> 2) << 7) + (v & 3);
-            const uint32_t c = h[off];
-            e += dtab[c];
-            h[off] = (uint8_t)(c + 1);
+    if (r < vend) {
+        // entr64_init_int (entr64.cc:27-41) built incrementally, two bytes
+        // per round of count loads; lo is a multiple of 8, so the window's 64
+        // bytes are 16 aligned words, read four at a time
+#pragma unroll 1
+        for (int q = 0; q < 16; q += 4) {
+            uint32_t w[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) w[k] = b32[(lo >> 2) + q + k];
+#pragma unroll
+            for (int k = 0; k < 16; k += 2) {
+                const uint32_t v0 = byte_of(w[k >> 2], k & 3), v1 = byte_of(w[k >> 2], (k & 3) + 1);
+                const uint32_t o0 = hbase + ((v0 >> 2) << 7) + (v0 & 3), o1 = hbase + ((v1 >> 2) << 7) + (v1 & 3);
+                const int32_t c0 = h[o0];
+                const int32_t c1 = h[o1] + (int32_t)(v0 == v1);
+                e += dtab[c0] + dtab[c1];
+                h[o0] = (uint8_t)(c0 + 1);
+                h[o1] = (uint8_t)(c1 + 1);  // the same counter when v0 == v1: this store wins
+            }
         }
-        s.ranks[pidx(r)] = __ldg(rank_tab + (e >> 10));
+        s.ranks[pidx(r)] = rank_tab[e >> 10];
         r++;
     }
-    // two steps per iteration: the second step's counts are loaded together
-    // with the first's and corrected for the first step's update in registers
-    // (later stores win where both steps touch the same byte value)
-    for (; r + 1 < hi && g.Q0 + r + 1 < last; r += 2) {
-        const uint32_t a0 = b8[r - 1], b0 = b8[r + 63], a1 = b8[r], b1 = b8[r + 64];
-        const uint32_t ha0 = hbase + ((a0 >> 2) << 7) + (a0 & 3), hb0 = hbase + ((b0 >> 2) << 7) + (b0 & 3);
-        const uint32_t ha1 = hbase + ((a1 >> 2) << 7) + (a1 & 3), hb1 = hbase + ((b1 >> 2) << 7) + (b1 & 3);
-        const int32_t ca0 = h[ha0], cb0 = h[hb0];
-        int32_t ca1 = h[ha1], cb1 = h[hb1];
-        const bool d0 = a0 != b0, d1 = a1 != b1;
-        if (d0) {
-            e += dtab[cb0] - dtab[ca0 - 1];
-            ca1 += (int32_t)(a1 == b0) - (int32_t)(a1 == a0);
-            cb1 += (int32_t)(b1 == b0) - (int32_t)(b1 == a0);
-        }
-        const uint16_t rk0 = __ldg(rank_tab + (e >> 10));
-        if (d1) e += dtab[cb1] - dtab[ca1 - 1];
-        const uint16_t rk1 = __ldg(rank_tab + (e >> 10));
-        if (d0) {
-            h[ha0] = (uint8_t)(ca0 - 1);
-            h[hb0] = (uint8_t)(cb0 + 1);
-        }
-        if (d1) {
-            h[ha1] = (uint8_t)(ca1 - 1);
-            h[hb1] = (uint8_t)(cb1 + 1);
-        }
-        s.ranks[pidx(r)] = rk0;
-        s.ranks[pidx(r + 1)] = rk1;
+    // single steps up to the next multiple of 8
+    for (; r < vend && (r & 7u); r++) {
+        rank_single(h, hbase, dtab, e, b8[r - 1], b8[r + 63]);
+        s.ranks[pidx(r)] = rank_tab[e >> 10];
     }
-    for (; r < hi; r++) {
-        if (g.Q0 + r >= last) {
-            s.ranks[pidx(r)] = 0;
-            continue;
+    // groups of eight: leaving bytes r-1..r+6, entering r+63..r+70 (three
+    // aligned words each, the next group's words loaded ahead)
+    if (r + 8 <= vend) {
+        uint32_t lw0 = b32[(r - 4) >> 2], lw1 = b32[r >> 2], lw2 = b32[(r + 4) >> 2];
+        uint32_t ew0 = b32[(r + 60) >> 2], ew1 = b32[(r + 64) >> 2], ew2 = b32[(r + 68) >> 2];
+        for (; r + 8 <= vend; r += 8) {
+            uint32_t nl0 = 0, nl1 = 0, nl2 = 0, ne0 = 0, ne1 = 0, ne2 = 0;
+            if (r + 16 <= vend) {
+                nl0 = b32[(r + 4) >> 2];
+                nl1 = b32[(r + 8) >> 2];
+                nl2 = b32[(r + 12) >> 2];
+                ne0 = b32[(r + 68) >> 2];
+                ne1 = b32[(r + 72) >> 2];
+                ne2 = b32[(r + 76) >> 2];
+            }
+            uint32_t a[8], b[8];
+            a[0] = byte_of(lw0, 3);
+            b[0] = byte_of(ew0, 3);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                a[1 + k] = byte_of(lw1, k);
+                b[1 + k] = byte_of(ew1, k);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                a[5 + k] = byte_of(lw2, k);
+                b[5 + k] = byte_of(ew2, k);
+            }
+            int32_t ev[8];
+#pragma unroll
+            for (int k = 0; k < 8; k += 2) rank_pair(h, hbase, dtab, e, a[k], b[k], a[k + 1], b[k + 1], ev[k], ev[k + 1]);
+            uint32_t* rk = reinterpret_cast<uint32_t*>(s.ranks + pidx(r));
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                rk[k] = (uint32_t)rank_tab[ev[2 * k] >> 10] | ((uint32_t)rank_tab[ev[2 * k + 1] >> 10] << 16);
+            lw0 = nl0;
+            lw1 = nl1;
+            lw2 = nl2;
+            ew0 = ne0;
+            ew1 = ne1;
+            ew2 = ne2;
         }
-        // byte r-1 leaves, byte r+63 enters
-        const uint32_t a = b8[r - 1], b = b8[r + 63];
-        if (a != b) {
-            const uint32_t ha = hbase + ((a >> 2) << 7) + (a & 3);
-            const uint32_t hb = hbase + ((b >> 2) << 7) + (b & 3);
-            const uint32_t ca = h[ha], cb = h[hb];
-            h[ha] = (uint8_t)(ca - 1);
-            h[hb] = (uint8_t)(cb + 1);
-            e += dtab[cb] - dtab[ca - 1];
-        }
-        s.ranks[pidx(r)] = __ldg(rank_tab + (e >> 10));
     }
+    for (; r < vend; r++) {
+        rank_single(h, hbase, dtab, e, b8[r - 1], b8[r + 63]);  // byte r-1 leaves, byte r+63 enters
+        s.ranks[pidx(r)] = rank_tab[e >> 10];
+    }
+    for (; r < hi; r++) s.ranks[pidx(r)] = 0;  // the last 64 positions of a chunk
 }
 
 // ------------------------------------- phase 3: full-rescan result per step
@@ -244,51 +315,102 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
 //    run; step u = v+1 takes A's minimum on ties (leftmost), continuing its
 //    run into B when it reaches A's last position and B starts with the
 //    same rank.  Both run ends stay within the window, so no cap is needed.
-// Positions past the ranks (the last block's B) count as rank 0.
+// Positions past the tile's last step are read but only feed steps that no
+// walk uses (every array extends past them).
+//
+// Both passes move eight steps at a time: the next group's ranks (two per
+// 32-bit word; pidx keeps a block contiguous and 4-byte aligned) are loaded
+// before the current group's results are stored, so no load waits behind a
+// store.
 __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
-    const uint32_t np = g.RE - g.Q0;
     const uint32_t nsteps = g.SE - g.Q0;
     const uint32_t nblk = (nsteps + 63) / 64;
-    const uint16_t* __restrict__ R = s.ranks;
-    uint16_t* __restrict__ Fr = s.fres;
     for (uint32_t j = threadIdx.x; j < nblk; j += blockDim.x) {
         const uint32_t base = j * 64;
-        const uint32_t ulim = min(64u, nsteps - base);
-        const uint16_t* Ra = R + pidx(base);   // block A (pidx is contiguous inside a block)
-        const uint16_t* Rb = R + pidx(base + 64);
-        uint16_t* Fa = Fr + pidx(base);
+        const uint32_t* __restrict__ Ra = reinterpret_cast<const uint32_t*>(s.ranks + pidx(base));
+        const uint32_t* __restrict__ Rb = reinterpret_cast<const uint32_t*>(s.ranks + pidx(base + 64));
+        uint32_t* __restrict__ Fa = reinterpret_cast<uint32_t*>(s.fres + pidx(base));
+        // pass 1: suffix states of A, steps 63..0
         uint32_t m = 1023, e = 63, rn = 0;
-#pragma unroll 8
-        for (int u = 63; u >= 0; u--) {
-            const uint32_t r = (base + u < np) ? Ra[u] : 0u;
-            const bool take = r != 0 && (r < m || (r == m && rn != m));
-            m = take ? r : m;
-            e = take ? (uint32_t)u : e;
-            rn = r;
-            if ((uint32_t)u < ulim) Fa[u] = r == 0 ? (uint16_t)0 : (uint16_t)((m << 6) | e);
-        }
-        uint32_t pm = 1023, pe = 0, lead_end = 0;
-        const uint32_t rb0 = (base + 64 < np) ? Rb[0] : 0u;
-#pragma unroll 4
-        for (uint32_t v = 0; v + 1 < ulim; v++) {
-            const uint32_t r = (base + 64 + v < np) ? Rb[v] : 0u;
-            lead_end = (v != 0 && r == rb0 && lead_end + 1 == v) ? v : lead_end;
-            const bool lower = r != 0 && r < pm;
-            const bool cont = r != 0 && r == pm && pe + 1 == v;
-            pm = lower ? r : pm;
-            pe = (lower || cont) ? v : pe;
-            const uint32_t u = v + 1;
-            const uint32_t sv = Fa[u];
-            const uint32_t sm = sv >> 6, se = sv & 63;
-            uint32_t mm, p;
-            if (sm <= pm) {
-                mm = sm;
-                p = (se == 63 && rb0 == sm) ? 64 + lead_end : se;
-            } else {
-                mm = pm;
-                p = 64 + pe;
+        uint32_t cur[4], nxt[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < 4; q++) cur[q] = Ra[28 + q];
+        uint32_t first = 0;  // result of step 0 (final after pass 1)
+#pragma unroll 1
+        for (int gi = 7; gi >= 0; gi--) {
+            if (gi > 0) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) nxt[q] = Ra[4 * (gi - 1) + q];
             }
-            Fa[u] = sv == 0 ? (uint16_t)0 : (uint16_t)((mm << 6) | (p - u));
+            uint32_t out[4];
+#pragma unroll
+            for (int q = 3; q >= 0; q--) {
+                uint32_t o2 = 0;
+#pragma unroll
+                for (int h = 1; h >= 0; h--) {
+                    const uint32_t u = 8u * gi + 2 * q + h;
+                    const uint32_t r = h ? (cur[q] >> 16) : (cur[q] & 0xFFFFu);
+                    const bool take = r != 0 && (r < m || (r == m && rn != m));
+                    m = take ? r : m;
+                    e = take ? u : e;
+                    rn = r;
+                    o2 |= (r == 0 ? 0u : ((m << 6) | e)) << (16 * h);
+                }
+                out[q] = o2;
+            }
+            first = out[0] & 0xFFFFu;
+#pragma unroll
+            for (int q = 0; q < 4; q++) Fa[4 * gi + q] = out[q];
+#pragma unroll
+            for (int q = 0; q < 4; q++) cur[q] = nxt[q];
+        }
+        // pass 2: prefix states of B, steps u = v + 1 = 1..63; results are
+        // packed into aligned words with the previous group's last one
+        uint32_t rb[4], fa[5], nrb[4] = {0, 0, 0, 0}, nfa[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < 4; q++) rb[q] = Rb[q];
+#pragma unroll
+        for (int q = 0; q < 5; q++) fa[q] = Fa[q];
+        const uint32_t rb0 = rb[0] & 0xFFFFu;
+        uint32_t pm = 1023, pe = 0, lead_end = 0;
+        uint32_t carry = first;
+#pragma unroll 1
+        for (uint32_t gi = 0; gi < 8; gi++) {
+            if (gi < 7) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) nrb[q] = Rb[4 * (gi + 1) + q];
+#pragma unroll
+                for (int q = 0; q < 4; q++) nfa[q] = Fa[4 * (gi + 1) + q];
+                nfa[4] = gi < 6 ? Fa[4 * (gi + 1) + 4] : 0u;
+            }
+            uint32_t res[8];
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const uint32_t v = 8 * gi + t;
+                const uint32_t r = (t & 1) ? (rb[t >> 1] >> 16) : (rb[t >> 1] & 0xFFFFu);
+                lead_end = (v != 0 && r == rb0 && lead_end + 1 == v) ? v : lead_end;
+                const bool lower = r != 0 && r < pm;
+                const bool cont = r != 0 && r == pm && pe + 1 == v;
+                pm = lower ? r : pm;
+                pe = (lower || cont) ? v : pe;
+                const uint32_t u = v + 1;  // its suffix state is halfword t + 1 of fa
+                const uint32_t sv = ((t + 1) & 1) ? (fa[(t + 1) >> 1] >> 16) : (fa[(t + 1) >> 1] & 0xFFFFu);
+                const uint32_t sm = sv >> 6, se = sv & 63;
+                const bool a_wins = sm <= pm;
+                const uint32_t mm = a_wins ? sm : pm;
+                const uint32_t p = a_wins ? ((se == 63 && rb0 == sm) ? 64 + lead_end : se) : 64 + pe;
+                res[t] = sv == 0 ? 0u : ((mm << 6) | (p - u));
+            }
+            // steps 8gi .. 8gi+7 as words 4gi .. 4gi+3 (step 8gi from the carry)
+            Fa[4 * gi] = carry | (res[0] << 16);
+            Fa[4 * gi + 1] = res[1] | (res[2] << 16);
+            Fa[4 * gi + 2] = res[3] | (res[4] << 16);
+            Fa[4 * gi + 3] = res[5] | (res[6] << 16);
+            carry = res[7];  // step 8gi + 8 (the next block's step 0 when gi == 7: dropped)
+#pragma unroll
+            for (int q = 0; q < 4; q++) rb[q] = nrb[q];
+#pragma unroll
+            for (int q = 0; q < 5; q++) fa[q] = nfa[q];
         }
     }
 }
@@ -311,36 +433,80 @@ struct Credit {
         }
         cnt = 0;
     }
-    __device__ __forceinline__ void add(uint32_t p) {
-        if (p != cur) {
-            flush();
-            cur = p;
+    // one step's credit to p when act (the step's min rank is not 0)
+    __device__ __forceinline__ void add(uint32_t p, bool act) {
+        const bool chg = act && p != cur;
+        const uint32_t o = cur - lo;
+        if (chg && cnt && o < hi - lo) {
+            const uint32_t inc = cnt << (8 * (o & 3));
+            if (kSign > 0) atomicAdd(&score32[o >> 2], inc);
+            else atomicSub(&score32[o >> 2], inc);
         }
-        cnt++;
+        cnt = chg ? 0u : cnt;
+        cur = chg ? p : cur;
+        cnt += act ? 1u : 0u;
     }
 };
 
+// One step of gen_chunk_scores (sdbf_core.cc:59-80) from state st, given
+// rank[i+64] and the full-rescan result of step i.
+template <typename CR>
+__device__ __forceinline__ void walk_step(ChainState& st, uint32_t i, uint32_t r64, uint32_t f, CR* cr) {
+    const bool cheap = (st.M != 0) & (r64 >= st.M) & (i < st.P);
+    const uint32_t cheapP = (r64 == st.M) ? i + 64 : st.P;
+    st.P = cheap ? cheapP : i + (f & 63);
+    st.M = cheap ? st.M : (f >> 6);
+    if (cr) cr->add(st.P, st.M != 0);
+}
+
+// Eight consecutive 16-bit entries starting at an 8-aligned index (inside
+// one 64-block of the padded layout, 4-byte aligned) as four words.
+__device__ __forceinline__ void load8(const uint16_t* p, uint32_t* w) {
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+#pragma unroll
+    for (int k = 0; k < 4; k++) w[k] = q[k];
+}
+__device__ __forceinline__ uint32_t half16(const uint32_t* w, int k) {
+    return (k & 1) ? (w[k >> 1] >> 16) : (w[k >> 1] & 0xFFFFu);
+}
+
 // Walk steps [a, b) of gen_chunk_scores from state `st` (st.M == 0 makes step
-// a a full rescan: the speculative start, or step 0).  The operands of step
-// i+1 are loaded while step i is processed; both arrays extend past the last
-// step, so those loads stay in bounds.
+// a a full rescan: the speculative start, or step 0).  Single steps up to an
+// 8-aligned step (Q0 is a multiple of 64, so tile offsets are aligned too),
+// then groups of eight whose operands (rank[i+64..], fres[i..]) are loaded
+// one group ahead.  With rec set, the state entering step chk is stored
+// there (the steps before chk then run one at a time).
 template <typename CR>
 __device__ __forceinline__ ChainState walk(const TileGeom& g, const TileSmem& s, uint32_t a, uint32_t b,
-                                           ChainState st, CR* cr) {
-    if (a >= b) return st;
+                                           ChainState st, CR* cr, uint32_t chk = 0, uint64_t* rec = nullptr) {
     const uint16_t* __restrict__ R = s.ranks;
     const uint16_t* __restrict__ Fr = s.fres;
-    uint32_t r64 = R[pidx(a + 64 - g.Q0)], f = Fr[pidx(a - g.Q0)];
-    for (uint32_t i = a; i < b; i++) {
-        const uint32_t r64n = R[pidx(i + 65 - g.Q0)], fn = Fr[pidx(i + 1 - g.Q0)];
-        const bool cheap = (st.M != 0) & (r64 >= st.M) & (i < st.P);
-        const uint32_t cheapP = (r64 == st.M) ? i + 64 : st.P;
-        st.P = cheap ? cheapP : i + (f & 63);
-        st.M = cheap ? st.M : (f >> 6);
-        if (cr && st.M != 0) cr->add(st.P);
-        r64 = r64n;
-        f = fn;
+    uint32_t i = a;
+    if (rec && chk >= a && chk < b) {
+        for (; i < chk; i++) walk_step(st, i, R[pidx(i + 64 - g.Q0)], Fr[pidx(i - g.Q0)], cr);
+        *rec = pack_state(st);
     }
+    for (; i < b && (i & 7u); i++) walk_step(st, i, R[pidx(i + 64 - g.Q0)], Fr[pidx(i - g.Q0)], cr);
+    if (i + 8 <= b) {
+        uint32_t rw[4], fw[4];
+        load8(R + pidx(i + 64 - g.Q0), rw);
+        load8(Fr + pidx(i - g.Q0), fw);
+        for (; i + 8 <= b; i += 8) {
+            uint32_t nrw[4] = {0, 0, 0, 0}, nfw[4] = {0, 0, 0, 0};
+            if (i + 16 <= b) {
+                load8(R + pidx(i + 72 - g.Q0), nrw);
+                load8(Fr + pidx(i + 8 - g.Q0), nfw);
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) walk_step(st, i + k, half16(rw, k), half16(fw, k), cr);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                rw[k] = nrw[k];
+                fw[k] = nfw[k];
+            }
+        }
+    }
+    for (; i < b; i++) walk_step(st, i, R[pidx(i + 64 - g.Q0)], Fr[pidx(i - g.Q0)], cr);
     return st;
 }
 
@@ -362,8 +528,9 @@ __device__ uint64_t relink_segment(const TileGeom& g, const TileSmem& s, uint32_
     for (; i < Et; i++) {
         if (pack_state(old) == pack_state(nw)) break;
         if (i == chk) *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(nw);
-        old = walk(g, s, i, i + 1, old, &un);
-        nw = walk(g, s, i, i + 1, nw, &re);
+        const uint32_t r64 = s.ranks[pidx(i + 64 - g.Q0)], f = s.fres[pidx(i - g.Q0)];
+        walk_step(old, i, r64, f, &un);
+        walk_step(nw, i, r64, f, &re);
     }
     un.flush();
     re.flush();
@@ -381,13 +548,7 @@ template <int kSign>
 __device__ __forceinline__ ChainState walk_segment(const TileGeom& g, const TileSmem& s, uint32_t St, uint32_t Et,
                                                    ChainState st, uint32_t chk) {
     Credit<kSign> cr{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0};
-    if (chk >= St && chk < Et) {
-        st = walk(g, s, St, chk, st, &cr);
-        if (kSign > 0) *reinterpret_cast<uint64_t*>(&s.misc[10]) = pack_state(st);
-        st = walk(g, s, chk, Et, st, &cr);
-    } else {
-        st = walk(g, s, St, Et, st, &cr);
-    }
+    st = walk(g, s, St, Et, st, &cr, chk, kSign > 0 ? reinterpret_cast<uint64_t*>(&s.misc[10]) : nullptr);
     cr.flush();
     return st;
 }
@@ -481,17 +642,20 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
 // Writes the positions (relative to t0) with score > thr (or >= thr when
 // ge) among [t0, t0+nown) into s.list in ascending order; returns count.
 // Each warp owns a contiguous run of score words; lanes read consecutive
-// 32-bit words (4 positions each), so the reads are conflict-free.
+// 32-bit words (4 positions each), so the reads are conflict-free.  A
+// position's place in the list comes from four ballots (one per byte of
+// the word): the selected positions of earlier lanes, plus those earlier in
+// the lane's own word.
 __device__ __forceinline__ uint32_t word_flags(const uint32_t* sc32, uint32_t wd, uint32_t nown, uint32_t thr,
                                                bool ge) {
     const uint32_t w = sc32[wd];
-    uint32_t f = 0;
-#pragma unroll
-    for (int b = 0; b < 4; b++) {
-        const uint32_t v = (w >> (8 * b)) & 0xFFu;
-        const bool sel = ge ? (v >= thr) : (v > thr);
-        if (sel && 4 * wd + b < nown) f |= 1u << b;
-    }
+    // per byte: bit 7 set when selected (bytes are scores <= 65 and the
+    // threshold byte is <= 66, so no byte borrows from its neighbour)
+    const uint32_t t4 = (ge ? thr : thr + 1) * 0x01010101u;
+    const uint32_t hb = ((w | 0x80808080u) - t4) & 0x80808080u;
+    uint32_t f = (hb >> 7 | hb >> 14 | hb >> 21 | hb >> 28) & 0xFu;
+    const uint32_t p0 = 4 * wd;
+    if (p0 + 4 > nown) f &= (p0 >= nown) ? 0u : ((1u << (nown - p0)) - 1u);
     return f;
 }
 
@@ -502,8 +666,7 @@ __device__ uint32_t compact(const TileSmem& s, uint32_t nown, uint32_t thr, bool
     const uint32_t w0 = min(nwords, wid * per), w1 = min(nwords, w0 + per);
     uint32_t c = 0;
     for (uint32_t wd = w0 + lane; wd < w1; wd += 32) c += __popc(word_flags(s.score32, wd, nown, thr, ge));
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+    c = __reduce_add_sync(0xffffffffu, c);
     if (lane == 0) tmp_counts[wid] = c;
     __syncthreads();
     uint32_t base = 0, total = 0;
@@ -511,24 +674,52 @@ __device__ uint32_t compact(const TileSmem& s, uint32_t nown, uint32_t thr, bool
         if (w < wid) base += tmp_counts[w];
         total += tmp_counts[w];
     }
+    const uint32_t lt = (1u << lane) - 1u;
     for (uint32_t wd0 = w0; wd0 < w1; wd0 += 32) {
         const uint32_t wd = wd0 + lane;
         const uint32_t f = wd < w1 ? word_flags(s.score32, wd, nown, thr, ge) : 0u;
-        const uint32_t k = __popc(f);
-        uint32_t incl = k;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-            if (lane >= (uint32_t)d) incl += y;
-        }
-        uint32_t pos = base + incl - k;
+        const uint32_t m0 = __ballot_sync(0xffffffffu, f & 1u), m1 = __ballot_sync(0xffffffffu, f & 2u);
+        const uint32_t m2 = __ballot_sync(0xffffffffu, f & 4u), m3 = __ballot_sync(0xffffffffu, f & 8u);
+        uint32_t pos = base + __popc(m0 & lt) + __popc(m1 & lt) + __popc(m2 & lt) + __popc(m3 & lt);
 #pragma unroll
         for (int b = 0; b < 4; b++)
             if ((f >> b) & 1u) s.list[pos++] = 4 * wd + b;
-        base += __shfl_sync(0xffffffffu, incl, 31);
+        base += __popc(m0) + __popc(m1) + __popc(m2) + __popc(m3);
     }
     __syncthreads();
     return total;
+}
+
+// Stream tiles (threshold 16): one pass.  Warp w writes its selected
+// positions to its own list s.list[w * kWarpList ..] and their number to
+// counts[w]; feature f of the tile is entry f - (the counts of earlier
+// warps) of the first warp list that reaches it.  A warp's range holds at
+// most 2,048 positions, so at most (2048 + 64) / 17 = 124 of them reach a
+// score of 17 (each step credits one position in [i, i+64]).
+constexpr uint32_t kWarpList = 128;
+__device__ void compact_stream(const TileSmem& s, uint32_t nown, uint32_t* counts) {
+    const uint32_t nwords = (nown + 3) / 4;
+    const uint32_t nwarps = blockDim.x / 32, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t per = ((nwords + nwarps - 1) / nwarps + 31) / 32 * 32;
+    const uint32_t w0 = min(nwords, wid * per), w1 = min(nwords, w0 + per);
+    uint32_t* list = s.list + wid * kWarpList;
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t n = 0;
+    for (uint32_t wd0 = w0; wd0 < w1; wd0 += 32) {
+        const uint32_t wd = wd0 + lane;
+        const uint32_t f = wd < w1 ? word_flags(s.score32, wd, nown, kThreshold, false) : 0u;
+        const uint32_t m0 = __ballot_sync(0xffffffffu, f & 1u), m1 = __ballot_sync(0xffffffffu, f & 2u);
+        const uint32_t m2 = __ballot_sync(0xffffffffu, f & 4u), m3 = __ballot_sync(0xffffffffu, f & 8u);
+        if (f) {
+            uint32_t pos = n + __popc(m0 & lt) + __popc(m1 & lt) + __popc(m2 & lt) + __popc(m3 & lt);
+#pragma unroll
+            for (int b = 0; b < 4; b++)
+                if ((f >> b) & 1u) list[pos++] = 4 * wd + b;
+        }
+        n += __popc(m0) + __popc(m1) + __popc(m2) + __popc(m3);
+    }
+    if (lane == 0) counts[wid] = n;
+    __syncthreads();
 }
 
 // ---------------------------------------------------------- stream tiles
@@ -554,20 +745,28 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
     __shared__ int32_t dtab[64];
     for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
     __syncthreads();
-    const uint16_t* rank_tab = P.rank_tab;  // 2 KB, read through the read-only cache
+    // the rank table (2 KB) in shared memory: a lookup is one shared-memory read
+    __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
+    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];
+    __syncthreads();
+    const uint16_t* rank_tab = s_rank;
     TileOut* out = P.tile_out + tile;
     long long tm[9];
     tile_pipeline(P.data + C.data_off, g, s, rank_tab, dtab, entry, &out->sig_in, &out->tau_out, P.lead,
                   P.phase ? tm : nullptr);
     const uint32_t nown = g.SE > g.t0 ? g.SE - g.t0 : 0;
     __shared__ uint32_t counts[kGenThreads / 32];
-    const uint32_t nf = compact(s, nown, kThreshold, false, counts);
+    static_assert(kGenThreads / 32 == 4 && 4 * kWarpList <= (kTileL + 64) / 15 + 8, "stream list layout");
+    compact_stream(s, nown, counts);
+    const uint32_t c1 = counts[0], c2 = c1 + counts[1], c3 = c2 + counts[2], nf = c3 + counts[3];
     stamp(P.phase ? tm : nullptr, 6);
     // SHA-1 of each selected feature (sdbf_core.cc:103-105)
     uint32_t* feat = P.features + (size_t)tile * 5 * kTileCap;
     const uint32_t off = g.t0 - g.Q0;
     for (uint32_t f = threadIdx.x; f < nf; f += blockDim.x) {
-        const uint32_t p = s.list[f] + off;
+        const uint32_t wl = (f >= c1) + (f >= c2) + (f >= c3);
+        const uint32_t before = wl == 0 ? 0u : wl == 1 ? c1 : wl == 2 ? c2 : c3;
+        const uint32_t p = s.list[wl * kWarpList + (f - before)] + off;
         uint32_t w[16], h[5];
         load_be16(s.bytes32, p, w);
         sha1_feature(w, h);
@@ -1142,7 +1341,10 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
     __shared__ int state[4];  // k, allowed, hashed, done
     for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
     __syncthreads();
-    const uint16_t* rank_tab = P.rank_tab;  // read through the read-only cache
+    __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
+    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];
+    __syncthreads();
+    const uint16_t* rank_tab = s_rank;
     TileSmem s = carve(smem, P.block_lmax);
     for (uint32_t b = blockIdx.x; b < P.nchunks; b += gridDim.x) {
         const GenChunk C = P.chunks[b];
