@@ -213,6 +213,36 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def compare_roofline(pairs_per_s: float, variant: int, sm_mhz=None):
+    """Roofline of the comparison kernel.  The tensor-core variant counts
+    popcount(a & b) of two 2,048-bit filters as an e4m3 dot product of length
+    2,048 (4,096 fp8 FLOPs per filter pair) against the fp8 dense rate, taken
+    as twice the measured bf16 rate (MEASURED_PEAKS.json has no fp8 figure;
+    nominal dense fp8 is 4.5 PFLOP/s).  The CUDA-core variants are integer
+    issue bound: 64 AND + 64 POPC + 63 adds per filter pair against 128
+    integer lanes per SM per clock."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        bf16, src = float(pk["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        bf16, src = 1900.0, "fallback"
+    if variant == 5:
+        peak = 2 * bf16
+        ach = pairs_per_s * 4096 / 1e12
+        return {"bound": "tensor", "kernel": "k_matrix_tc", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                "frac": ach / peak, "traffic": None,
+                "work_per_filter_pair": "4096 fp8 FLOPs (2048-bit AND-popcount as an e4m3 0/1 dot product)",
+                "peak_source": f"2 x {src} bf16 burst (MEASURED_PEAKS.json bf16_tflops; fp8 dense = 2 x bf16)",
+                "mma_bound_filter_pairs_per_s": peak * 1e12 / 4096}
+    mhz = sm_mhz or 2070.0
+    peak = 152 * 128 * mhz * 1e6 / 1e12
+    ach = pairs_per_s * 191 / 1e12
+    return {"bound": "int", "kernel": "k_matrix", "achieved": ach, "peak": peak, "unit": "Tops/s", "frac": ach / peak,
+            "traffic": None, "work_per_filter_pair": "191 integer lane ops (64 AND, 64 POPC, 63 adds)",
+            "peak_source": f"152 SMs x 128 integer lanes x {mhz:.0f} MHz"}
+
+
 def profiled_traffic(kernel: str):
     """dram bytes per input byte of `kernel` from the committed ncu summary."""
     path = os.path.join(REPO, "profiles", f"{kernel}_ncu.md")
@@ -491,6 +521,7 @@ def main_allpairs(args):
                        "autotune_sample_rate": tuned_rate, "build_s": round(t_build, 1),
                        "l2": "filters 5x larger than L2"},
             "gpu_launches": launches, "clocks": clocks.summary(),
+            "roofline": compare_roofline(value, variant, clocks.summary().get("sm_mhz")),
             "plain_per_call": {"value": plain_rate, "unit": AP_UNIT, "pairs": len(pi), "filter_pairs": plain_work,
                                "seconds": round(t_plain, 3),
                                "path": "sdbfg_score_pairs with one pair per call (one launch + sync each)"},
@@ -680,6 +711,7 @@ def main_image(args):
             "top_match": {"cut_queries_best_segment_found": int(found.sum()), "cut_queries": int(cut.sum()),
                           "queries_with_score_ge_1": int((scores.max(1) >= 1).sum())},
             "gpu_launches": launches, "clocks": clocks.summary(),
+            "roofline": compare_roofline(value, variant, clocks.summary().get("sm_mhz")),
             "plain_per_call": {"value": plain_work / t_plain, "unit": AP_UNIT, "queries": len(pick),
                                "seconds": round(t_plain, 3),
                                "path": "one query per call: upload + compare_to + scores back"},
@@ -885,6 +917,7 @@ def main_serve(args):
             "filter_pairs_per_s": served_fp,
             "served_over_plain_per_pair": served_fp / pair_rate,
             "server_stats": stats, "clocks": clocks.summary(), "gpu_launches": int(stats["launches"]),
+            "roofline": compare_roofline(served_fp, tuned[0] if tuned else 5, clocks.summary().get("sm_mhz")),
             "plain_per_call": {"value": plain_qps, "unit": "queries/s", "queries": len(svc),
                                "mean_service_ms": float(svc.mean() * 1e3),
                                "latency_at_70pct_of_served_capacity": fifo(rate_b, 5),

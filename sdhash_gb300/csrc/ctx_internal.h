@@ -26,6 +26,16 @@ constexpr uint64_t kFirstHostGroupBytes = 256ull << 20;  // first group of a hos
 constexpr uint32_t kMinFile = 512;                 // MIN_FILE_SIZE (sdbf_defines.h:56)
 constexpr uint64_t kPairsPerLaunch = 1ull << 22;
 constexpr int kSlots = 8;  // stream-mode launch groups in flight (at most)
+// pinned host-input stream batches up to this size (and half the free
+// device memory) are staged whole on the device
+constexpr uint64_t kStageMaxBytes = 64ull << 30;
+constexpr uint64_t kStagePiece = 1ull << 20;  // work item of the staging gather
+struct StagePiece {
+    uint64_t dst;  // staging offset (16-byte aligned)
+    uint64_t src;  // device address of the pinned host bytes
+    uint64_t len;
+};
+
 
 // Device / pinned-host arrays that grow on demand and free themselves with
 // their owner (not copyable).
@@ -152,6 +162,12 @@ struct sdbfg_ctx {
     } slot[kSlots];
     int depth = 3;  // launch groups in flight
     DevBuf d_binfo, d_boff, d_total, d_phase;
+    // host-input stream batches staged whole on the device: per-file copies
+    // in launch-group order on their own stream, one event per group
+    DevBuf d_stage_in, d_stage_items;
+    HostBuf h_stage_items;
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> ev_copy;
     cudaEvent_t ev_scan[kSlots] = {};
     cudaEvent_t ev_tiles[kSlots] = {};  // a group's tile kernels done
     cudaEvent_t ev_start = nullptr;

@@ -336,8 +336,10 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 #pragma unroll
         for (int q = 0; q < 4; q++) cur[q] = Ra[28 + q];
         uint32_t first = 0;  // result of step 0 (final after pass 1)
+        uint32_t any = 0;    // OR of block A's ranks
 #pragma unroll 1
         for (int gi = 7; gi >= 0; gi--) {
+            any |= cur[0] | cur[1] | cur[2] | cur[3];
             if (gi > 0) {
 #pragma unroll
                 for (int q = 0; q < 4; q++) nxt[q] = Ra[4 * (gi - 1) + q];
@@ -364,6 +366,9 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 #pragma unroll
             for (int q = 0; q < 4; q++) cur[q] = nxt[q];
         }
+        // a block whose ranks are all 0 (low-entropy content) is done: every
+        // step's result is 0, as pass 1 wrote
+        if (any == 0) continue;
         // pass 2: prefix states of B, steps u = v + 1 = 1..63; results are
         // packed into aligned words with the previous group's last one
         uint32_t rb[4], fa[5], nrb[4] = {0, 0, 0, 0}, nfa[5] = {0, 0, 0, 0, 0};

@@ -78,6 +78,12 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : c->ev_tiles)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->ev_copy)
+        if (e) cudaEventDestroy(e);
+    c->d_stage_in.release();
+    c->d_stage_items.release();
+    c->h_stage_items.release();
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->ev_start) cudaEventDestroy(c->ev_start);
     c->h_stage.release();
     timer_collect(c);
@@ -349,6 +355,46 @@ __global__ void k_pack_group(const uint32_t* __restrict__ work, const GenFile* _
     }
 }
 
+// Staging of pinned host inputs: each piece (at most kStagePiece bytes of
+// one input) is read straight from host memory through the device's mapping
+// of the pinned buffer and written to its 16-byte aligned staging offset;
+// 16-byte loads where the source allows them, else 4-byte or single bytes.
+// kGatherThreads threads and few registers, so a CTA fits on an SM beside
+// the tile kernel's four.
+constexpr int kGatherThreads = 128;
+__global__ void __launch_bounds__(kGatherThreads) k_stage_gather(const StagePiece* __restrict__ items, uint32_t n,
+                                                                  uint8_t* __restrict__ dst) {
+    for (uint32_t f = blockIdx.x; f < n; f += gridDim.x) {
+        const StagePiece it = items[f];
+        const uint8_t* s = reinterpret_cast<const uint8_t*>(it.src);
+        uint8_t* d = dst + it.dst;
+        uint64_t done = 0;
+        if ((it.src & 15) == 0) {
+            const uint4* s4 = reinterpret_cast<const uint4*>(s);
+            uint4* d4 = reinterpret_cast<uint4*>(d);
+            const uint64_t n4 = it.len / 16;
+            uint64_t q = threadIdx.x;
+            for (; q + 3 * kGatherThreads < n4; q += 4 * kGatherThreads) {
+                const uint4 a = s4[q], b = s4[q + kGatherThreads], c = s4[q + 2 * kGatherThreads],
+                            e = s4[q + 3 * kGatherThreads];
+                d4[q] = a;
+                d4[q + kGatherThreads] = b;
+                d4[q + 2 * kGatherThreads] = c;
+                d4[q + 3 * kGatherThreads] = e;
+            }
+            for (; q < n4; q += kGatherThreads) d4[q] = s4[q];
+            done = n4 * 16;
+        } else if ((it.src & 3) == 0) {
+            const uint32_t* s1 = reinterpret_cast<const uint32_t*>(s);
+            uint32_t* d1 = reinterpret_cast<uint32_t*>(d);
+            const uint64_t n1 = it.len / 4;
+            for (uint64_t q = threadIdx.x; q < n1; q += kGatherThreads) d1[q] = s1[q];
+            done = n1 * 4;
+        }
+        for (uint64_t q = done + threadIdx.x; q < it.len; q += kGatherThreads) d[q] = s[q];
+    }
+}
+
 static int ensure_pipeline(sdbfg_ctx* c) {
     for (int k = 0; k < kSlots; k++) {
         if (!c->slot[k].stream) {
@@ -462,6 +508,38 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
     // results[] records where each input's filters are.
     // (an index build keeps input order: every file's digest depends on the
     // index inserts of the files before it)
+    // Pinned host inputs are staged whole on the device when they fit.  A
+    // gather kernel per launch group reads the group's inputs straight from
+    // host memory (the device's mapping of the pinned buffer) on a
+    // high-priority stream of its own, one event per group: the copies cost
+    // one launch per group instead of one API call per input (tens of
+    // microseconds each), and no copy waits behind an earlier group's commit
+    // or a slot's reuse.  Its small CTAs fit beside the tile kernel's.
+    bool staged = false;
+    const uint8_t* host_dev = nullptr;  // the device's view of the pinned input
+    if (host_data && !ib && n) {
+        cudaPointerAttributes attr{};
+        const bool pinned = cudaPointerGetAttributes(&attr, host_data) == cudaSuccess &&
+                            attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr;
+        cudaGetLastError();
+        if (pinned)
+            host_dev = static_cast<const uint8_t*>(attr.devicePointer) +
+                       (host_data - static_cast<const uint8_t*>(attr.hostPointer));
+        uint64_t tot = 0;
+        for (uint32_t i = 0; i < n; i++) tot += (lens_in[i] + 15) & ~15ull;
+        size_t freeb = 0, totb = 0;
+        if (pinned && tot <= kStageMaxBytes && cudaMemGetInfo(&freeb, &totb) == cudaSuccess &&
+            (c->d_stage_in.cap >= tot || tot <= freeb / 2)) {
+            CUDA_TRY(c, c->d_stage_in.ensure(std::max<uint64_t>(16, tot)));
+            if (!c->copy_stream) {
+                int lo = 0, hi = 0;
+                CUDA_TRY(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+                CUDA_TRY(c, cudaStreamCreateWithPriority(&c->copy_stream, cudaStreamNonBlocking, hi));
+            }
+            staged = true;
+        }
+        cudaGetLastError();
+    }
     std::vector<uint32_t> perm(n);
     std::iota(perm.begin(), perm.end(), 0u);
     if (!ib)
@@ -480,6 +558,61 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
     CUDA_TRY(c, cudaMemsetAsync(c->d_total.p, 0, 64, c->stream));
     CUDA_TRY(c, cudaEventRecord(c->ev_start, c->stream));
     const std::vector<Group> groups = make_groups(lens, n, 0, host_data ? kFirstHostGroupBytes : kMaxBytesPerLaunch);
+    std::vector<uint64_t> stage_off;
+    if (staged) {
+        stage_off.resize(n);
+        uint64_t tot = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            stage_off[i] = tot;
+            tot += (lens[i] + 15) & ~15ull;
+        }
+        while (c->ev_copy.size() < groups.size()) {
+            cudaEvent_t e;
+            CUDA_TRY(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            c->ev_copy.push_back(e);
+        }
+        // after the previous batch's work on the caller's stream
+        CUDA_TRY(c, cudaStreamWaitEvent(c->copy_stream, c->ev_start, 0));
+    }
+    if (staged) {
+        // pieces of at most kStagePiece bytes; the item tables of all groups
+        // go over in one copy, then one gather launch per group
+        std::vector<uint32_t> first_item(groups.size() + 1, 0);
+        uint64_t nitems = 0;
+        for (size_t gi = 0; gi < groups.size(); gi++) {
+            first_item[gi] = (uint32_t)nitems;
+            for (uint32_t k = 0; k < groups[gi].count; k++) {
+                const uint64_t len = lens[groups[gi].first + k];
+                if (len >= kMinFile) nitems += (len + kStagePiece - 1) / kStagePiece;
+            }
+        }
+        first_item[groups.size()] = (uint32_t)nitems;
+        CUDA_TRY(c, c->h_stage_items.ensure(std::max<uint64_t>(1, nitems) * sizeof(StagePiece)));
+        CUDA_TRY(c, c->d_stage_items.ensure(std::max<uint64_t>(1, nitems) * sizeof(StagePiece)));
+        // the previous batch's table copy has finished (its call synchronised
+        // at its end); the host table may be rewritten
+        StagePiece* it = reinterpret_cast<StagePiece*>(c->h_stage_items.p);
+        uint64_t q = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            if (lens[i] < kMinFile) continue;
+            for (uint64_t pos = 0; pos < lens[i]; pos += kStagePiece)
+                it[q++] = StagePiece{stage_off[i] + pos, reinterpret_cast<uint64_t>(host_dev + offsets[i] + pos),
+                                     std::min<uint64_t>(kStagePiece, lens[i] - pos)};
+        }
+        if (nitems)
+            CUDA_TRY(c, cudaMemcpyAsync(c->d_stage_items.p, it, nitems * sizeof(StagePiece), cudaMemcpyHostToDevice,
+                                        c->copy_stream));
+        for (size_t gi = 0; gi < groups.size(); gi++) {
+            const uint32_t ni = first_item[gi + 1] - first_item[gi];
+            if (ni)
+                TIMED_LAUNCH_ON(c, "k_stage_gather", c->copy_stream,
+                                (k_stage_gather<<<std::min<uint32_t>(ni, (uint32_t)c->sms), kGatherThreads, 0,
+                                                  c->copy_stream>>>(c->d_stage_items.as<StagePiece>() + first_item[gi],
+                                                                    ni, c->d_stage_in.as<uint8_t>()),
+                                 cudaGetLastError()));
+            CUDA_TRY(c, cudaEventRecord(c->ev_copy[gi], c->copy_stream));
+        }
+    }
     cudaEvent_t prev_scan = c->ev_start, prev_tiles = c->ev_start;
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
@@ -513,6 +646,10 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         if (dev_data) {
             gdata = dev_data;
             for (uint32_t k = 0; k < g.count; k++) doff[k] = offsets[g.first + k];
+        } else if (staged) {
+            gdata = c->d_stage_in.as<uint8_t>();
+            for (uint32_t k = 0; k < g.count; k++) doff[k] = stage_off[g.first + k];
+            CUDA_TRY(c, cudaStreamWaitEvent(st, c->ev_copy[gi], 0));
         } else {
             CUDA_TRY(c, S.data.ensure(std::max<uint64_t>(16, bytes)));
             gdata = S.data.as<uint8_t>();

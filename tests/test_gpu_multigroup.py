@@ -76,3 +76,34 @@ def test_multi_group_batch_matches_oracle(ctx, oracle):
     # the 64 MiB files carry filters from both of their chunks
     big = [i for i in range(n) if int(sizes[i]) == 64 * MiB]
     assert all(res_host[i].bf_count > 1 for i in big)
+
+
+def test_pinned_inputs_at_unaligned_offsets(ctx, oracle):
+    """Pinned host inputs at offsets that are not multiples of 16 or 4 (the
+    staging copy then reads them with narrower loads), as one batch with a
+    file of more than one 1 MiB staging piece."""
+    import torch
+    from sdhash_gb300 import DigestResult, _ptr, _u64, lib
+
+    sizes = [700, 1 << 20, 3 * MiB + 5, 5000, 2 * MiB + 1, 600, 100000]
+    offs, pos = [], 0
+    for k, n in enumerate(sizes):
+        pos += (1, 6, 3, 16, 2, 5, 7)[k]  # gaps that leave odd, even and aligned starts
+        offs.append(pos)
+        pos += n
+    pinned = torch.empty(pos + 64, dtype=torch.uint8, pin_memory=True)
+    data = pinned.numpy()
+    for k, (o, n) in enumerate(zip(offs, sizes)):
+        data[o:o + n] = synth.mixture_bytes(43, k, n)
+    o64, l64 = _u64(offs), _u64(sizes)
+    cap = ctx.capacity(l64, 0)
+    out = torch.empty(cap * 256, dtype=torch.uint8, pin_memory=True).numpy()
+    res = (DigestResult * len(sizes))()
+    for _ in range(2):  # twice: the staging buffers are reused
+        ctx._check(lib().sdbfg_digest_batch(ctx.h, data.ctypes.data, _ptr(o64), _ptr(l64), len(sizes), 0,
+                                            out.ctypes.data, cap, None, res))
+        for k, (o, n) in enumerate(zip(offs, sizes)):
+            od = oracle.digest(f"u{k}", data[o:o + n].tobytes(), 0)
+            r = res[k]
+            assert (r.bf_count, r.last_count) == (od.bf_count, od.last_count), k
+            assert out[r.filter_offset * 256:(r.filter_offset + r.bf_count) * 256].tobytes() == od.filters(), k
