@@ -587,7 +587,9 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
     stamp(tm, 3);
     // segments over steps [S0, SE)
     const uint32_t total = g.SE > g.S0 ? g.SE - g.S0 : 0;
-    const uint32_t SL = (total + kSegs - 1) / kSegs;
+    // segment length a multiple of 8 (S0 is a multiple of 64): every walk then
+    // starts and ends on a group of eight steps (trailing threads may idle)
+    const uint32_t SL = ((total + kSegs - 1) / kSegs + 7) & ~7u;
     const uint32_t chk = g.t0 + g.L - 64;  // next tile's S0
     const uint32_t t = threadIdx.x;
     const uint32_t St = g.S0 + t * SL;
