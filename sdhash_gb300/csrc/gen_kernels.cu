@@ -700,30 +700,47 @@ __device__ uint32_t compact(const TileSmem& s, uint32_t nown, uint32_t thr, bool
 // Stream tiles (threshold 16): one pass.  Warp w writes its selected
 // positions to its own list s.list[w * kWarpList ..] and their number to
 // counts[w]; feature f of the tile is entry f - (the counts of earlier
-// warps) of the first warp list that reaches it.  A warp's range holds at
-// most 2,048 positions, so at most (2048 + 64) / 17 = 124 of them reach a
-// score of 17 (each step credits one position in [i, i+64]).
+// warps) of the first warp list that reaches it.  A lane reads 16 scores
+// (one 16-byte load; a warp's 32 loads are one contiguous 512-byte run) and
+// gets their selection bits from four byte-parallel compares; a shuffle scan
+// of the lanes' counts places them.  A warp's range holds at most 2,048
+// positions, so at most (2048 + 64) / 17 = 124 of them reach a score of 17
+// (each step credits one position in [i, i+64]).
 constexpr uint32_t kWarpList = 128;
+__device__ __forceinline__ uint32_t sel4(uint32_t w, uint32_t t4) {
+    const uint32_t hb = ((w | 0x80808080u) - t4) & 0x80808080u;
+    return (hb >> 7 | hb >> 14 | hb >> 21 | hb >> 28) & 0xFu;
+}
 __device__ void compact_stream(const TileSmem& s, uint32_t nown, uint32_t* counts) {
-    const uint32_t nwords = (nown + 3) / 4;
+    const uint32_t nq = (nown + 15) / 16;  // 16-position quads
     const uint32_t nwarps = blockDim.x / 32, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint32_t per = ((nwords + nwarps - 1) / nwarps + 31) / 32 * 32;
-    const uint32_t w0 = min(nwords, wid * per), w1 = min(nwords, w0 + per);
+    const uint32_t per = ((nq + nwarps - 1) / nwarps + 31) / 32 * 32;
+    const uint32_t q0 = min(nq, wid * per), q1 = min(nq, q0 + per);
     uint32_t* list = s.list + wid * kWarpList;
-    const uint32_t lt = (1u << lane) - 1u;
+    const uint4* sc4 = reinterpret_cast<const uint4*>(s.score32);
+    const uint32_t t4 = (kThreshold + 1) * 0x01010101u;
     uint32_t n = 0;
-    for (uint32_t wd0 = w0; wd0 < w1; wd0 += 32) {
-        const uint32_t wd = wd0 + lane;
-        const uint32_t f = wd < w1 ? word_flags(s.score32, wd, nown, kThreshold, false) : 0u;
-        const uint32_t m0 = __ballot_sync(0xffffffffu, f & 1u), m1 = __ballot_sync(0xffffffffu, f & 2u);
-        const uint32_t m2 = __ballot_sync(0xffffffffu, f & 4u), m3 = __ballot_sync(0xffffffffu, f & 8u);
-        if (f) {
-            uint32_t pos = n + __popc(m0 & lt) + __popc(m1 & lt) + __popc(m2 & lt) + __popc(m3 & lt);
-#pragma unroll
-            for (int b = 0; b < 4; b++)
-                if ((f >> b) & 1u) list[pos++] = 4 * wd + b;
+    for (uint32_t qb = q0; qb < q1; qb += 32) {
+        const uint32_t q = qb + lane;
+        uint32_t m = 0;
+        if (q < q1) {
+            const uint4 w = sc4[q];
+            m = sel4(w.x, t4) | (sel4(w.y, t4) << 4) | (sel4(w.z, t4) << 8) | (sel4(w.w, t4) << 12);
+            if (16 * q + 16 > nown) m &= (1u << (nown - 16 * q)) - 1u;
         }
-        n += __popc(m0) + __popc(m1) + __popc(m2) + __popc(m3);
+        const uint32_t c = __popc(m);
+        uint32_t incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += y;
+        }
+        uint32_t pos = n + incl - c;
+        while (m) {
+            list[pos++] = 16 * q + (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+        }
+        n += __shfl_sync(0xffffffffu, incl, 31);
     }
     if (lane == 0) counts[wid] = n;
     __syncthreads();
