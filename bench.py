@@ -1404,6 +1404,7 @@ def main():
     # One more step, outside the timed region, with launch groups run one
     # after another and per-kernel CUDA events on the launch stream: the
     # kernels do not overlap, so each event pair brackets one kernel alone.
+    depth0 = ctx.pipeline_depth
     ctx.set_pipeline_depth(1)
     ctx.profile(True)
     step_device()
@@ -1414,7 +1415,7 @@ def main():
               for k in ("load", "ranks", "fres", "walk", "link", "compact", "sha1", "fixups")}
     commit_ph = {k: ctx.kernel_time("k_stream_commit." + k)[0] for k in ("wait", "busy", "groups", "loops", "max_file")}
     ctx.profile(False)
-    ctx.set_pipeline_depth(3)
+    ctx.set_pipeline_depth(depth0)
     tiles_ms, tiles_n = kern["k_stream_tiles"]
     ms_per_step = allmax(world, dev_ms / args.steps)
     bytes_all = allsum(world, total_bytes)

@@ -73,11 +73,13 @@ int sdbfg_ctx_kernel_time(sdbfg_ctx *ctx, const char *kernel, double *total_ms, 
  * exercise it.  No counterpart in the reference (its walk is sequential). */
 int sdbfg_ctx_set_lead(sdbfg_ctx *ctx, uint32_t steps);
 /* Stream-mode launch groups (<= 2 GiB of input each) kept in flight on
- * separate streams, 1..8 (default 3): the ordered commit of one group
+ * separate streams, 1..8 (default 4): the ordered commit of one group
  * overlaps the next groups' tile kernels.  Depth 1 runs groups one after
  * another (used to time kernels without overlap).  Tuning knob without a
  * counterpart in the reference. */
 int sdbfg_ctx_set_pipeline_depth(sdbfg_ctx *ctx, int depth);
+/* The current pipeline depth (no counterpart in the reference). */
+int sdbfg_ctx_pipeline_depth(const sdbfg_ctx *ctx);
 /* Tiles whose speculative popularity chain was re-walked (instrumentation). */
 uint64_t sdbfg_ctx_relinked_tiles(sdbfg_ctx *ctx);
 /* Stream-mode index build (sdbfg_digest_batch_index with dd == 0): the

@@ -92,6 +92,7 @@ def lib() -> C.CDLL:
         L.sdbfg_ctx_launch_count.restype = C.c_uint64
         L.sdbfg_ctx_set_lead.argtypes = [vp, C.c_uint32]
         L.sdbfg_ctx_set_pipeline_depth.argtypes = [vp, C.c_int]
+        L.sdbfg_ctx_pipeline_depth.argtypes = [vp]
         L.sdbfg_ctx_profile.argtypes = [vp, C.c_int]
         L.sdbfg_ctx_kernel_time.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
         L.sdbfg_ctx_relinked_tiles.argtypes = [vp]
@@ -374,6 +375,11 @@ class Context:
     def set_lead(self, steps: int):
         """Speculative lead-in of the parallel score walk (exact for any value)."""
         self._check(lib().sdbfg_ctx_set_lead(self.h, steps))
+
+    @property
+    def pipeline_depth(self) -> int:
+        """Stream-mode launch groups kept in flight."""
+        return int(lib().sdbfg_ctx_pipeline_depth(self.h))
 
     def set_pipeline_depth(self, depth: int):
         """Stream-mode launch groups in flight (1..8); 1 = no overlap."""

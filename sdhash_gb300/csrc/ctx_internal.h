@@ -160,7 +160,7 @@ struct sdbfg_ctx {
         DevBuf data, chunks, tiles, files, order, tile_out, features, work, redo;
         HostBuf h_tables;
     } slot[kSlots];
-    int depth = 3;  // launch groups in flight
+    int depth = 4;  // launch groups in flight
     DevBuf d_binfo, d_boff, d_total, d_phase;
     // host-input stream batches staged whole on the device: per-file copies
     // in launch-group order on their own stream, one event per group

@@ -23,7 +23,8 @@ constexpr uint32_t kTileL = 7936;
 // at most one selected feature per 17 credited steps (score > 16), and a
 // tile's positions are credited by kTileL + 64 steps
 constexpr uint32_t kTileCap = ((kTileL + 64) / 17 + 2 + 3) / 4 * 4;  // rows 16-byte aligned
-constexpr int kCommitWarps = 2;      // files per commit CTA
+constexpr int kCommitWarps = 1;      // files per commit CTA (one: its 44 KB of shared memory then
+                                     // displaces a single tile CTA on its SM)
 constexpr uint32_t kMaxBlockBytes = 16384;  // dd block size limit (sdhash.cc:215-219)
 constexpr uint64_t kChunkBytes = 32ull << 20;  // stream chunk (sdbf_class.cc:43)
 

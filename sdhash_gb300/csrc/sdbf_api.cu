@@ -161,6 +161,8 @@ extern "C" int sdbfg_ctx_kernel_time(sdbfg_ctx* c, const char* name, double* tot
     return SDBFG_OK;
 }
 
+extern "C" int sdbfg_ctx_pipeline_depth(const sdbfg_ctx* c) { return c ? c->depth : 0; }
+
 extern "C" int sdbfg_ctx_set_pipeline_depth(sdbfg_ctx* c, int depth) {
     if (!c || depth < 1 || depth > kSlots) return SDBFG_ERR_ARG;
     c->depth = depth;
