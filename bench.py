@@ -243,16 +243,21 @@ def compare_roofline(pairs_per_s: float, variant: int, sm_mhz=None):
             "peak_source": f"152 SMs x 128 integer lanes x {mhz:.0f} MHz"}
 
 
-def profiled_traffic(kernel: str):
-    """dram bytes per input byte of `kernel` from the committed ncu summary."""
+def profiled_value(kernel: str, key: str):
+    """A per-input-byte figure of `kernel` from its committed ncu summary."""
     path = os.path.join(REPO, "profiles", f"{kernel}_ncu.md")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_input_byte:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def profiled_traffic(kernel: str):
+    """dram bytes per input byte of `kernel` from the committed ncu summary."""
+    return profiled_value(kernel, "dram_bytes_per_input_byte")
 
 
 def sample_files(sizes, gib: float, seed: int):
@@ -1466,7 +1471,21 @@ def main():
     tile_ms = tiles_ms / max(1, tiles_n)
     achieved = per_launch_bytes / (tile_ms / 1e3) / 1e9 if tile_ms > 0 else None
     tpb = profiled_traffic("k_stream_tiles")
+    # the bound that holds: integer issue (warp instructions per input byte
+    # from the committed ncu capture x achieved bytes/s, against one warp
+    # instruction per scheduler per clock)
+    wipb = profiled_value("k_stream_tiles", "warp_inst_per_input_byte")
+    sm_mhz = clocks.summary().get("sm_mhz") or 2070.0
+    issue_peak = 152 * 4 * sm_mhz * 1e6
+    issue = None
+    if wipb and achieved:
+        issue = {"unit": "warp instructions/s", "warp_inst_per_input_byte": wipb,
+                 "achieved": wipb * achieved * 1e9, "peak": issue_peak, "frac": wipb * achieved * 1e9 / issue_peak,
+                 "ceiling_GBs_at_full_issue": issue_peak / wipb / 1e9,
+                 "source": "profiles/k_stream_tiles_ncu.md (smsp__inst_executed per input byte); peak = 152 SMs x "
+                           "4 schedulers x median SM clock"}
     roofline = {"bound": "hbm", "kernel": "k_stream_tiles", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "issue": issue,
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": (tpb * per_launch_bytes) if tpb else None,
                 "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",
