@@ -377,7 +377,14 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 #pragma unroll
         for (int q = 0; q < 5; q++) fa[q] = Fa[q];
         const uint32_t rb0 = rb[0] & 0xFFFFu;
-        uint32_t pm = 1023, pe = 0, lead_end = 0;
+        // A's leftmost minimum whose run reaches A's last position has A's
+        // last rank, so it continues into B iff B starts with that rank
+        const uint32_t r63 = Ra[31] >> 16;
+        const bool contB = r63 != 0 && r63 == rb0;
+        // pm / pe64: minimum of B[0..v] and 64 + the end of its leftmost run;
+        // open: that run ends at v; lead64: 64 + the end of B's leading run
+        uint32_t pm = 1023, pe64 = 64, lead64 = 64;
+        bool open = false, lead_open = true;
         uint32_t carry = first;
 #pragma unroll 1
         for (uint32_t gi = 0; gi < 8; gi++) {
@@ -393,17 +400,19 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
             for (int t = 0; t < 8; t++) {
                 const uint32_t v = 8 * gi + t;
                 const uint32_t r = (t & 1) ? (rb[t >> 1] >> 16) : (rb[t >> 1] & 0xFFFFu);
-                lead_end = (v != 0 && r == rb0 && lead_end + 1 == v) ? v : lead_end;
+                lead_open = lead_open && r == rb0;
+                lead64 = lead_open ? 64 + v : lead64;
                 const bool lower = r != 0 && r < pm;
-                const bool cont = r != 0 && r == pm && pe + 1 == v;
+                const bool cont = open && r == pm;  // pm > 0, so r != 0
                 pm = lower ? r : pm;
-                pe = (lower || cont) ? v : pe;
+                open = lower || cont;
+                pe64 = open ? 64 + v : pe64;
                 const uint32_t u = v + 1;  // its suffix state is halfword t + 1 of fa
                 const uint32_t sv = ((t + 1) & 1) ? (fa[(t + 1) >> 1] >> 16) : (fa[(t + 1) >> 1] & 0xFFFFu);
                 const uint32_t sm = sv >> 6, se = sv & 63;
                 const bool a_wins = sm <= pm;
                 const uint32_t mm = a_wins ? sm : pm;
-                const uint32_t p = a_wins ? ((se == 63 && rb0 == sm) ? 64 + lead_end : se) : 64 + pe;
+                const uint32_t p = a_wins ? ((se == 63 && contB) ? lead64 : se) : pe64;
                 res[t] = sv == 0 ? 0u : ((mm << 6) | (p - u));
             }
             // steps 8gi .. 8gi+7 as words 4gi .. 4gi+3 (step 8gi from the carry)
@@ -427,29 +436,25 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
 template <int kSign>
 struct Credit {
     uint32_t* score32;
-    uint32_t lo, hi;  // credited positions [lo, hi) (chunk-relative)
-    uint32_t cur, cnt;
-    __device__ __forceinline__ void flush() {
-        if (cnt && cur - lo < hi - lo) {
-            const uint32_t o = cur - lo;
-            const uint32_t inc = cnt << (8 * (o & 3));
-            if (kSign > 0) atomicAdd(&score32[o >> 2], inc);
-            else atomicSub(&score32[o >> 2], inc);
-        }
-        cnt = 0;
-    }
-    // one step's credit to p when act (the step's min rank is not 0)
-    __device__ __forceinline__ void add(uint32_t p, bool act) {
-        const bool chg = act && p != cur;
+    uint32_t lo, hi;      // credited positions [lo, hi) (chunk-relative)
+    uint32_t cur, start;  // position credited by the open run of steps (~0u: none) and its first step
+    // closes the open run at step i (its steps [start, i) all credited cur)
+    __device__ __forceinline__ void flush(uint32_t i) {
         const uint32_t o = cur - lo;
-        if (chg && cnt && o < hi - lo) {
-            const uint32_t inc = cnt << (8 * (o & 3));
+        if (o < hi - lo && i > start) {
+            const uint32_t inc = (i - start) << (8 * (o & 3));
             if (kSign > 0) atomicAdd(&score32[o >> 2], inc);
             else atomicSub(&score32[o >> 2], inc);
         }
-        cnt = chg ? 0u : cnt;
-        cur = chg ? p : cur;
-        cnt += act ? 1u : 0u;
+    }
+    // step i credits p when act (its min rank is not 0); a step that
+    // credits nothing opens a run of ~0u, which is never added
+    __device__ __forceinline__ void add(uint32_t i, uint32_t p, bool act) {
+        const uint32_t key = act ? p : ~0u;
+        const bool chg = key != cur;
+        if (chg) flush(i);
+        cur = chg ? key : cur;
+        start = chg ? i : start;
     }
 };
 
@@ -461,7 +466,7 @@ __device__ __forceinline__ void walk_step(ChainState& st, uint32_t i, uint32_t r
     const uint32_t cheapP = (r64 == st.M) ? i + 64 : st.P;
     st.P = cheap ? cheapP : i + (f & 63);
     st.M = cheap ? st.M : (f >> 6);
-    if (cr) cr->add(st.P, st.M != 0);
+    if (cr) cr->add(i, st.P, st.M != 0);
 }
 
 // Eight consecutive 16-bit entries starting at an 8-aligned index (inside
@@ -527,8 +532,8 @@ __host__ __device__ inline uint32_t tile_lead(uint32_t lead) { return lead >= kF
 // segment's exit state.
 __device__ uint64_t relink_segment(const TileGeom& g, const TileSmem& s, uint32_t St, uint32_t Et, ChainState old,
                                    ChainState nw, uint32_t chk, uint64_t old_exit) {
-    Credit<-1> un{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0};
-    Credit<1> re{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0};
+    Credit<-1> un{s.score32, g.t0, g.t0 + g.L, ~0u, St};
+    Credit<1> re{s.score32, g.t0, g.t0 + g.L, ~0u, St};
     uint32_t i = St;
     for (; i < Et; i++) {
         if (pack_state(old) == pack_state(nw)) break;
@@ -537,8 +542,8 @@ __device__ uint64_t relink_segment(const TileGeom& g, const TileSmem& s, uint32_
         walk_step(old, i, r64, f, &un);
         walk_step(nw, i, r64, f, &re);
     }
-    un.flush();
-    re.flush();
+    un.flush(i);
+    re.flush(i);
     return i < Et ? old_exit : pack_state(nw);
 }
 
@@ -552,9 +557,9 @@ __device__ __forceinline__ void stamp(long long* tm, int k) {
 template <int kSign>
 __device__ __forceinline__ ChainState walk_segment(const TileGeom& g, const TileSmem& s, uint32_t St, uint32_t Et,
                                                    ChainState st, uint32_t chk) {
-    Credit<kSign> cr{s.score32, g.t0, g.t0 + g.L, 0xFFFFFFFFu, 0};
+    Credit<kSign> cr{s.score32, g.t0, g.t0 + g.L, ~0u, St};
     st = walk(g, s, St, Et, st, &cr, chk, kSign > 0 ? reinterpret_cast<uint64_t*>(&s.misc[10]) : nullptr);
-    cr.flush();
+    cr.flush(Et);
     return st;
 }
 
