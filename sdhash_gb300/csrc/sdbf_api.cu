@@ -224,14 +224,16 @@ struct Group {  // consecutive inputs processed by one launch sequence
 
 // Splits inputs into launch groups bounded by tiles (stream) or bytes.
 // Launch groups of consecutive inputs, each at most kMaxTilesPerLaunch tiles
-// and kMaxBytesPerLaunch bytes; the first group at most first_cap bytes
-// (host inputs: a short first copy lets the kernels start early while the
-// later groups' copies overlap them).
+// and kMaxBytesPerLaunch bytes; the first group at most first_cap bytes and
+// each later one at most twice its predecessor's cap (host inputs: a short
+// first copy lets the kernels start early, and the ramp keeps each later
+// group's copy shorter than the kernels of the groups before it).
 std::vector<Group> make_groups(const uint64_t* lens, uint32_t n, uint32_t dd,
                                uint64_t first_cap = kMaxBytesPerLaunch) {
     std::vector<Group> gs;
     uint32_t start = 0;
     uint64_t tiles = 0, bytes = 0;
+    uint64_t cap_bytes = std::min(first_cap, kMaxBytesPerLaunch);
     for (uint32_t i = 0; i < n; i++) {
         uint64_t t = 0;
         if (!dd && lens[i] >= kMinFile) {
@@ -241,12 +243,12 @@ std::vector<Group> make_groups(const uint64_t* lens, uint32_t n, uint32_t dd,
             }
         }
         const uint64_t b = (lens[i] + 15) & ~15ull;
-        const uint64_t cap_bytes = gs.empty() ? std::min(first_cap, kMaxBytesPerLaunch) : kMaxBytesPerLaunch;
         if (i > start && (tiles + t > kMaxTilesPerLaunch || bytes + b > cap_bytes)) {
             gs.push_back({start, i - start});
             start = i;
             tiles = 0;
             bytes = 0;
+            cap_bytes = std::min(2 * cap_bytes, kMaxBytesPerLaunch);
         }
         tiles += t;
         bytes += b;

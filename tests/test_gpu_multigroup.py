@@ -1,13 +1,14 @@
 """The digest path at the scale the bulk-generation benchmark runs it.
 
-Smaller tests fit one launch group.  Here about 4.7 GiB of mixture content
-(forty 64 MiB files of two 32 MiB chunks each, files just over one chunk, a
+Smaller tests fit one launch group.  Here about 6 GiB of mixture content
+(sixty 64 MiB files of two 32 MiB chunks each, files just over one chunk, a
 log-uniform spread of 4 KiB..64 MiB files and a few below the 512-byte
 minimum) goes through the C ABI twice:
 
-* host buffers (sdbfg_digest_batch): a 256 MiB first launch group, then
-  2 GiB groups, three in flight on their own streams, tile kernels chained
-  by events across the streams;
+* host buffers (sdbfg_digest_batch): the pinned input staged on the device
+  by a gather kernel per launch group; launch groups of 256 MiB, 512 MiB,
+  1 GiB, then 2 GiB, four in flight on their own streams, tile kernels
+  chained by events across the streams;
 * device-resident input (sdbfg_digest_batch_device): 2 GiB groups.
 
 Every file of both runs is checked against the oracle (filters, bf_count,
@@ -28,7 +29,7 @@ MiB = 1 << 20
 def _sizes():
     spread = [int(s) for s in synth.log_uniform_sizes(31, 300, 4096, 64 * MiB)]
     edges = [32 * MiB + 65, 32 * MiB + 1000, 64 * MiB - 1, 64 * MiB - 63, 33 * MiB + 7, 100, 511, 512, 4097]
-    sizes = [64 * MiB] * 40 + spread + edges
+    sizes = [64 * MiB] * 60 + spread + edges
     rng = np.random.default_rng(5)
     return np.array([sizes[i] for i in rng.permutation(len(sizes))], dtype=np.uint64)
 
@@ -39,7 +40,8 @@ def test_multi_group_batch_matches_oracle(ctx, oracle):
 
     sizes = _sizes()
     offs, total = synth.packed_layout(sizes)
-    assert total > (256 * MiB) + 2 * (2 << 30)  # a 256 MiB first group and at least two full 2 GiB groups
+    # host path: groups of 256 MiB, 512 MiB, 1 GiB, then at least two full 2 GiB groups
+    assert total > (256 + 512 + 1024) * MiB + 2 * (2 << 30)
     pinned = torch.empty(total, dtype=torch.uint8, pin_memory=True)
     data = pinned.numpy()
     synth.fill_many(41, "mixture", sizes, out=data)
@@ -47,7 +49,7 @@ def test_multi_group_batch_matches_oracle(ctx, oracle):
     n = len(sizes)
     cap = ctx.capacity(l64, 0)
 
-    ctx.set_pipeline_depth(3)
+    ctx.set_pipeline_depth(4)
     out_host = torch.empty(cap * 256, dtype=torch.uint8, pin_memory=True).numpy()
     res_host = (DigestResult * n)()
     ctx._check(lib().sdbfg_digest_batch(ctx.h, data.ctypes.data, _ptr(o64), _ptr(l64), n, 0, out_host.ctypes.data,
