@@ -144,6 +144,8 @@ struct sdbfg_ctx {
     uint64_t launches = 0;
     int sms = 152;
     uint32_t lead = kDefaultLead;
+    bool pre_ranks = true;  // stream mode: ranks by k_stream_ranks ahead of the tile kernel
+    DevBuf d_ranks;         // their ranks (one buffer: groups' rank kernels run one after another)
     // constant tables
     DevBuf d_rank, d_ent, d_cut, d_cut64;
     // generation buffers
@@ -158,6 +160,7 @@ struct sdbfg_ctx {
         cudaEvent_t done = nullptr;
         bool used = false;
         DevBuf data, chunks, tiles, files, order, tile_out, features, work, redo;
+        DevBuf rk_items;  // stretches of the group's chunks for k_stream_ranks
         HostBuf h_tables;
     } slot[kSlots];
     int depth = 4;  // launch groups in flight

@@ -133,6 +133,49 @@ __device__ inline TileSmem carve(uint8_t* base, uint32_t Lmax) {
     return s;
 }
 
+// Layout of a stream tile whose ranks come precomputed (k_stream_ranks):
+// ranks | fres (the compaction list reuses it) | scores | sig | tau | misc.
+// No bytes or histograms: 42.9 KB, so five tiles fit on an SM.
+__host__ __device__ inline uint32_t fres_bytes(uint32_t Lmax) { return align_up(padded_len(Lmax + 64 + kLead) * 2, 16); }
+__host__ __device__ inline uint32_t tile_smem_bytes_pre(uint32_t Lmax) {
+    const uint32_t span = Lmax + 64 + kLead + 64;
+    return align_up(padded_len(span) * 2, 16) + fres_bytes(Lmax) + align_up(Lmax + 16, 16) + 2 * kSegs * 8 + 64 * 4;
+}
+__device__ inline TileSmem carve_pre(uint8_t* base, uint32_t Lmax) {
+    TileSmem s;
+    const uint32_t span = Lmax + 64 + kLead + 64;
+    uint8_t* p = base;
+    s.bytes32 = nullptr;
+    s.hist = nullptr;
+    s.own = nullptr;
+    s.ranks = reinterpret_cast<uint16_t*>(p); p += align_up(padded_len(span) * 2, 16);
+    s.fres = reinterpret_cast<uint16_t*>(p);
+    s.list = reinterpret_cast<uint32_t*>(p); p += fres_bytes(Lmax);
+    s.score32 = reinterpret_cast<uint32_t*>(p); p += align_up(Lmax + 16, 16);
+    s.sig = reinterpret_cast<uint64_t*>(p); p += kSegs * 8;
+    s.tau = reinterpret_cast<uint64_t*>(p); p += kSegs * 8;
+    s.misc = reinterpret_cast<uint32_t*>(p);
+    return s;
+}
+static_assert(((kTileL + 64) / 15 + 8) * 4 <= (kTileL + 64 + kLead) * 2, "the list fits in the fres area");
+
+// Ranks [Q0, RE) of a tile from the chunk's precomputed ranks (src = the
+// chunk's first rank, 16-byte aligned; Q0 is a multiple of 64, and the
+// chunk's ranks extend to a multiple of 8), eight per 16-byte load.
+__device__ inline void load_ranks(const uint16_t* __restrict__ src, const TileGeom& g, uint16_t* dst) {
+    const uint32_t n8 = (g.RE - g.Q0 + 7) / 8;
+    const uint4* s4 = reinterpret_cast<const uint4*>(src + g.Q0);
+#pragma unroll 4
+    for (uint32_t i = threadIdx.x; i < n8; i += blockDim.x) {
+        const uint4 v = __ldg(s4 + i);
+        uint32_t* d = reinterpret_cast<uint32_t*>(dst + pidx(8 * i));
+        d[0] = v.x;
+        d[1] = v.y;
+        d[2] = v.z;
+        d[3] = v.w;
+    }
+}
+
 // ------------------------------------------------------- phase 1: bytes
 __device__ inline void load_bytes(const uint8_t* __restrict__ chunk, const TileGeom& g, uint32_t* dst32) {
     // [Q0, BE) -> dst; Q0 is a multiple of 64 relative to the chunk start and
@@ -204,19 +247,34 @@ __device__ __forceinline__ void rank_single(uint8_t* h, uint32_t hbase, const in
     }
 }
 
-__device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const uint16_t* rank_tab,
-                                     const int32_t* dtab) {
-    const uint8_t* b8 = reinterpret_cast<const uint8_t*>(s.bytes32);
-    const uint32_t* b32 = s.bytes32;
-    const uint32_t np = g.RE - g.Q0;
-    const uint32_t per = ((np + kRankThreads - 1) / kRankThreads + 7) & ~7u;
-    const uint32_t tid = threadIdx.x;
-    if (tid >= (uint32_t)kRankThreads) return;
-    uint8_t* h = s.hist;  // counts at hist_off(tid, v) (cleared by the caller)
-    const uint32_t lo = min(np, tid * per), hi = min(np, lo + per);
-    const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
-    const uint32_t vend = last > g.Q0 ? min(hi, last - g.Q0) : lo;  // [lo, vend): entropy ranks
-    const uint32_t hbase = hist_off(tid, 0);
+// Where a run of ranks goes: the tile's padded shared-memory array, or a
+// chunk's ranks in global memory (a group of eight as one 16-byte store).
+struct SmemRanks {
+    uint16_t* r;
+    __device__ __forceinline__ void one(uint32_t o, uint16_t v) const { r[pidx(o)] = v; }
+    __device__ __forceinline__ void eight(uint32_t o, const uint32_t (&w)[4]) const {
+        uint32_t* p = reinterpret_cast<uint32_t*>(r + pidx(o));
+#pragma unroll
+        for (int k = 0; k < 4; k++) p[k] = w[k];
+    }
+};
+struct GlobalRanks {
+    uint16_t* r;  // 16-byte aligned
+    __device__ __forceinline__ void one(uint32_t o, uint16_t v) const { r[o] = v; }
+    __device__ __forceinline__ void eight(uint32_t o, const uint32_t (&w)[4]) const {
+        *reinterpret_cast<uint4*>(r + o) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+};
+
+// Ranks of positions [lo, hi) of the bytes at b32 (lo a multiple of 8):
+// entropy ranks for [lo, vend), 0 for [vend, hi).  Bytes up to vend+62
+// must be present, plus 8 bytes of padding; h + hbase is the thread's
+// cleared histogram (hist_off layout).
+template <class Out>
+__device__ __forceinline__ void rank_run(const uint32_t* b32, uint8_t* h, uint32_t hbase, const uint16_t* rank_tab,
+                                         const int32_t* dtab, uint32_t lo, uint32_t vend, uint32_t hi,
+                                         const Out& out) {
+    const uint8_t* b8 = reinterpret_cast<const uint8_t*>(b32);
     int32_t e = 0;
     uint32_t r = lo;
     if (r < vend) {
@@ -239,13 +297,13 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
                 h[o1] = (uint8_t)(c1 + 1);  // the same counter when v0 == v1: this store wins
             }
         }
-        s.ranks[pidx(r)] = rank_tab[e >> 10];
+        out.one(r, rank_tab[e >> 10]);
         r++;
     }
     // single steps up to the next multiple of 8
     for (; r < vend && (r & 7u); r++) {
         rank_single(h, hbase, dtab, e, b8[r - 1], b8[r + 63]);
-        s.ranks[pidx(r)] = rank_tab[e >> 10];
+        out.one(r, rank_tab[e >> 10]);
     }
     // groups of eight: leaving bytes r-1..r+6, entering r+63..r+70 (three
     // aligned words each, the next group's words loaded ahead)
@@ -278,10 +336,11 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
             int32_t ev[8];
 #pragma unroll
             for (int k = 0; k < 8; k += 2) rank_pair(h, hbase, dtab, e, a[k], b[k], a[k + 1], b[k + 1], ev[k], ev[k + 1]);
-            uint32_t* rk = reinterpret_cast<uint32_t*>(s.ranks + pidx(r));
+            uint32_t rk[4];
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 rk[k] = (uint32_t)rank_tab[ev[2 * k] >> 10] | ((uint32_t)rank_tab[ev[2 * k + 1] >> 10] << 16);
+            out.eight(r, rk);
             lw0 = nl0;
             lw1 = nl1;
             lw2 = nl2;
@@ -292,9 +351,21 @@ __device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const
     }
     for (; r < vend; r++) {
         rank_single(h, hbase, dtab, e, b8[r - 1], b8[r + 63]);  // byte r-1 leaves, byte r+63 enters
-        s.ranks[pidx(r)] = rank_tab[e >> 10];
+        out.one(r, rank_tab[e >> 10]);
     }
-    for (; r < hi; r++) s.ranks[pidx(r)] = 0;  // the last 64 positions of a chunk
+    for (; r < hi; r++) out.one(r, 0);  // the last 64 positions of a chunk
+}
+
+__device__ inline void compute_ranks(const TileGeom& g, const TileSmem& s, const uint16_t* rank_tab,
+                                     const int32_t* dtab) {
+    const uint32_t np = g.RE - g.Q0;
+    const uint32_t per = ((np + kRankThreads - 1) / kRankThreads + 7) & ~7u;
+    const uint32_t tid = threadIdx.x;
+    if (tid >= (uint32_t)kRankThreads) return;
+    const uint32_t lo = min(np, tid * per), hi = min(np, lo + per);
+    const uint32_t last = g.n - kWin;  // ranks exist for o < n-64 only
+    const uint32_t vend = last > g.Q0 ? min(hi, last - g.Q0) : lo;  // [lo, vend): entropy ranks
+    rank_run(s.bytes32, s.hist, hist_off(tid, 0), rank_tab, dtab, lo, vend, hi, SmemRanks{s.ranks});
 }
 
 // ------------------------------------- phase 3: full-rescan result per step
@@ -566,22 +637,33 @@ __device__ __forceinline__ ChainState walk_segment(const TileGeom& g, const Tile
 // Runs all phases for one tile.  entry != nullptr: the state entering step
 // S0 is known (re-computation after a failed link check); otherwise thread 0
 // starts speculatively `lead` steps early.  Writes sig_in / tau_out.
+// kPre: the ranks come from pre_ranks (the chunk's precomputed ranks)
+// instead of the chunk bytes.
+template <bool kPre = false>
 __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom& g, const TileSmem& s,
                               const uint16_t* rank_tab, const int32_t* dtab, const uint64_t* entry,
-                              uint64_t* sig_in, uint64_t* tau_out, uint32_t lead, long long* tm) {
+                              uint64_t* sig_in, uint64_t* tau_out, uint32_t lead, long long* tm,
+                              const uint16_t* pre_ranks = nullptr) {
     stamp(tm, 0);
-    load_bytes(chunk, g, s.bytes32);
-    {
-        uint4* h4 = reinterpret_cast<uint4*>(s.hist);
-        for (uint32_t i = threadIdx.x; i < 256 * kRankThreads / 16; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
+    if constexpr (kPre) {
+        load_ranks(pre_ranks, g, s.ranks);
+        __syncthreads();
+        stamp(tm, 1);
+    } else {
+        load_bytes(chunk, g, s.bytes32);
+        {
+            uint4* h4 = reinterpret_cast<uint4*>(s.hist);
+            for (uint32_t i = threadIdx.x; i < 256 * kRankThreads / 16; i += blockDim.x)
+                h4[i] = make_uint4(0, 0, 0, 0);
+        }
+        __syncthreads();
+        stamp(tm, 1);
+        compute_ranks(g, s, rank_tab, dtab);
+        __syncthreads();
     }
-    __syncthreads();
-    stamp(tm, 1);
-    compute_ranks(g, s, rank_tab, dtab);
-    __syncthreads();
     stamp(tm, 2);
     compute_fres(g, s);
-    // clear scores (aliases the histogram area, free after phase 2)
+    // clear scores (in-tile ranks: aliases the histogram area, free after phase 2)
     for (uint32_t i = threadIdx.x; i < (g.L + 3) / 4 + 1; i += blockDim.x) s.score32[i] = 0;
     if (threadIdx.x == 0) {
         s.misc[9] = 0;
@@ -766,23 +848,32 @@ __device__ inline TileGeom stream_geom(uint32_t n, uint32_t t0) {
     return g;
 }
 
+// kPre: ranks precomputed in P.ranks (tile_smem_bytes_pre layout); the
+// SHA-1 phase then reads the feature bytes from global memory.
+template <bool kPre>
 __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64_t* entry, uint8_t* smem) {
     const GenTile T = P.tiles[tile];
     const GenChunk C = P.chunks[T.chunk];
     const TileGeom g = stream_geom(C.n, T.t0);
-    TileSmem s = carve(smem, kTileL);
-    __shared__ int32_t dtab[64];
-    for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
-    __syncthreads();
-    // the rank table (2 KB) in shared memory: a lookup is one shared-memory read
-    __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
-    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];
-    __syncthreads();
-    const uint16_t* rank_tab = s_rank;
+    TileSmem s = kPre ? carve_pre(smem, kTileL) : carve(smem, kTileL);
+    const uint16_t* rank_tab = nullptr;
+    const int32_t* dt = nullptr;
+    if constexpr (!kPre) {
+        __shared__ int32_t dtab[64];
+        for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x)
+            dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
+        // the rank table (2 KB) in shared memory: a lookup is one shared-memory read
+        __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
+        for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];
+        __syncthreads();
+        rank_tab = s_rank;
+        dt = dtab;
+    }
     TileOut* out = P.tile_out + tile;
     long long tm[9];
-    tile_pipeline(P.data + C.data_off, g, s, rank_tab, dtab, entry, &out->sig_in, &out->tau_out, P.lead,
-                  P.phase ? tm : nullptr);
+    const uint8_t* chunk = P.data + C.data_off;
+    tile_pipeline<kPre>(chunk, g, s, rank_tab, dt, entry, &out->sig_in, &out->tau_out, P.lead,
+                        P.phase ? tm : nullptr, kPre ? P.ranks + (size_t)C.rank_off8 * 8 : nullptr);
     const uint32_t nown = g.SE > g.t0 ? g.SE - g.t0 : 0;
     __shared__ uint32_t counts[kGenThreads / 32];
     static_assert(kGenThreads / 32 == 4 && 4 * kWarpList <= (kTileL + 64) / 15 + 8, "stream list layout");
@@ -797,7 +888,10 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
         const uint32_t before = wl == 0 ? 0u : wl == 1 ? c1 : wl == 2 ? c2 : c3;
         const uint32_t p = s.list[wl * kWarpList + (f - before)] + off;
         uint32_t w[16], h[5];
-        load_be16(s.bytes32, p, w);
+        if constexpr (kPre)
+            load_be16_global(chunk + g.Q0 + p, w);
+        else
+            load_be16(s.bytes32, p, w);
         sha1_feature(w, h);
 #pragma unroll
         for (int k = 0; k < 5; k++) feat[k * kTileCap + f] = h[k];
@@ -820,7 +914,15 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
 __global__ void __launch_bounds__(kGenThreads, 4) k_stream_tiles(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     for (uint32_t tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
-        stream_tile_body(P, tile, nullptr, smem);
+        stream_tile_body<false>(P, tile, nullptr, smem);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kGenThreads, 5) k_stream_tiles_pre(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    for (uint32_t tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+        stream_tile_body<true>(P, tile, nullptr, smem);
         __syncthreads();
     }
 }
@@ -854,6 +956,7 @@ __global__ void __launch_bounds__(128) k_stream_check(GenParams P) {
     }
 }
 
+template <bool kPre>
 __global__ void __launch_bounds__(kGenThreads) k_stream_fix(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t entry;
@@ -870,11 +973,56 @@ __global__ void __launch_bounds__(kGenThreads) k_stream_fix(GenParams P) {
             }
             __syncthreads();
             if (redo) {
-                stream_tile_body(P, tile, &entry, smem);
+                stream_tile_body<kPre>(P, tile, &entry, smem);
                 if (threadIdx.x == 0) atomicAdd(P.counters + 0, 1u);
             }
             __syncthreads();
         }
+    }
+}
+
+// ------------------------------------------------ precomputed ranks
+// Entropy ranks of a stream launch group ahead of its tile kernel.  One CTA
+// item is a stretch of kRkSpan positions of a chunk, its bytes staged in
+// shared memory with 16-byte loads; each thread ranks kRkPer consecutive
+// positions with its own histogram (rank_run, the tile kernel's rank loop),
+// so a thread's 64-byte window set-up is spread over 264 positions instead
+// of a tile thread's 88.  Ranks of positions >= n-64 are 0; the chunk's
+// ranks run to a multiple of 8 (GenChunk::rank_off8).
+constexpr uint32_t kRkBytes = align_up(kRkSpan + 64 + 16, 16);  // staged bytes + zero padding
+constexpr uint32_t kRkSmem = 256 * kRkThreads + kRkBytes;
+
+__global__ void __launch_bounds__(kRkThreads, 3) k_stream_ranks(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint8_t* hist = smem;
+    uint32_t* b32 = reinterpret_cast<uint32_t*>(smem + 256 * kRkThreads);
+    __shared__ int32_t dtab[64];
+    __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
+    for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
+    for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t item = blockIdx.x; item < P.nrk_items; item += gridDim.x) {
+        const uint2 it = P.rk_items[item];
+        const GenChunk C = P.chunks[it.x];
+        const uint32_t s0 = it.y, n = C.n;
+        const uint32_t np = min(kRkSpan, align_up(n, 8) - s0);  // positions [s0, s0+np)
+        const uint32_t nb = min(kRkSpan + 64, n - s0);          // bytes [s0, s0+nb)
+        __syncthreads();  // the previous stretch is done with the bytes and histograms
+        const uint8_t* src = P.data + C.data_off + s0;
+        const uint32_t nvec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0) ? nb / 16 : 0;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(b32);
+        for (uint32_t i = tid; i < nvec; i += blockDim.x) d4[i] = __ldg(s4 + i);
+        uint8_t* d8 = reinterpret_cast<uint8_t*>(b32);
+        for (uint32_t i = nvec * 16 + tid; i < nb + 8; i += blockDim.x) d8[i] = (i < nb) ? src[i] : 0;
+        uint4* h4 = reinterpret_cast<uint4*>(hist);
+        for (uint32_t i = tid; i < 256 * kRkThreads / 16; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        const uint32_t lo = min(np, tid * kRkPer), hi = min(np, lo + kRkPer);
+        const uint32_t last = n > kWin ? n - kWin : 0;  // ranks exist for o < n-64 only
+        const uint32_t vend = last > s0 ? min(hi, last - s0) : lo;
+        rank_run(b32, hist, hist_off(tid, 0), s_rank, dtab, lo, vend, hi,
+                 GlobalRanks{P.ranks + (size_t)C.rank_off8 * 8 + s0});
     }
 }
 
@@ -1530,22 +1678,35 @@ __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
 
 // ---------------------------------------------------------------- launch
 size_t stream_tile_smem() { return tile_smem_bytes(kTileL); }
+size_t stream_tile_smem_pre() { return tile_smem_bytes_pre(kTileL); }
 size_t block_smem(uint32_t lmax) { return tile_smem_bytes(lmax); }
 
 static void set_stream_attrs() {
     static bool done = false;
     if (done) return;
-    const int sm = (int)stream_tile_smem();
+    const int sm = (int)stream_tile_smem(), smp = (int)stream_tile_smem_pre();
     cudaFuncSetAttribute(k_stream_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    cudaFuncSetAttribute(k_stream_fix, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(k_stream_fix<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(k_stream_tiles_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
+    cudaFuncSetAttribute(k_stream_fix<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
+    cudaFuncSetAttribute(k_stream_ranks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRkSmem);
     cudaFuncSetAttribute(k_stream_commit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(CommitSmem) * kCommitWarps));
     done = true;
 }
 
+cudaError_t launch_stream_ranks(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    set_stream_attrs();
+    if (grid) k_stream_ranks<<<grid, kRkThreads, kRkSmem, st>>>(P);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t st) {
     set_stream_attrs();
-    k_stream_tiles<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
+    if (P.ranks)
+        k_stream_tiles_pre<<<grid, kGenThreads, stream_tile_smem_pre(), st>>>(P);
+    else
+        k_stream_tiles<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
     return cudaGetLastError();
 }
 
@@ -1556,7 +1717,10 @@ cudaError_t launch_stream_check(const GenParams& P, uint32_t grid, cudaStream_t 
 
 cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st) {
     set_stream_attrs();
-    k_stream_fix<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
+    if (P.ranks)
+        k_stream_fix<true><<<grid, kGenThreads, stream_tile_smem_pre(), st>>>(P);
+    else
+        k_stream_fix<false><<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
     return cudaGetLastError();
 }
 

@@ -37,7 +37,16 @@ struct GenChunk {
     uint32_t ntiles;      // stream: tiles of this chunk
     uint32_t filter;      // block: output filter index
     uint32_t kind;        // block: 0 full block (histogram threshold), 1 tail (16 / 192)
+    uint32_t rank_off8;   // stream, ranks precomputed: the chunk's first rank in GenParams::ranks / 8
 };
+
+// Precomputed ranks of a stream launch group: k_stream_ranks gives each CTA
+// kRkThreads x kRkPer consecutive positions of one chunk (a "stretch"); one
+// work item (chunk, first position) per stretch.
+constexpr int kRkThreads = 128;
+constexpr uint32_t kRkPer = 264;  // positions per thread: a multiple of 8 whose word count (66) is
+                                  // 2 mod 4, so a warp's byte-word reads are at most 2-way bank conflicts
+constexpr uint32_t kRkSpan = kRkThreads * kRkPer;
 
 struct GenTile {
     uint32_t chunk;
@@ -111,6 +120,12 @@ struct GenParams {
     const uint8_t* commit_dirty;
     const uint32_t* commit_from;
     uint32_t* commit_ckpt;
+    // stream mode with ranks precomputed by k_stream_ranks (null: the tile
+    // kernel computes them itself): ranks of every chunk position, 16-byte
+    // aligned per chunk (GenChunk::rank_off8), and the stretches to compute
+    uint16_t* ranks;
+    const uint2* rk_items;
+    uint32_t nrk_items;
 };
 
 // Index search samples counted features 0, 4, 8, ... of a block
@@ -128,6 +143,10 @@ enum : int {
 
 size_t stream_tile_smem();
 size_t block_smem(uint32_t lmax);
+// Ranks of every position of the group's chunks into P.ranks (P.rk_items stretches).
+cudaError_t launch_stream_ranks(const GenParams& P, uint32_t grid, cudaStream_t st);
+// Tile kernels: with P.ranks set they read the precomputed ranks (and the
+// feature bytes from the input in global memory), else they compute ranks.
 cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t st);
 cudaError_t launch_stream_check(const GenParams& P, uint32_t grid, cudaStream_t st);  // 4 chunks per CTA
 cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st);

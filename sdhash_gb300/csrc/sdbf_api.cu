@@ -64,11 +64,11 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
                       &c->d_match_counts, &c->d_match_offs, &c->d_matches, &c->d_mphase, &c->d_probes,
                       &c->d_nprobes, &c->d_hits, &c->d_index_tab, &c->d_feats, &c->d_idx_bits, &c->d_idx_first,
                       &c->d_idx_count, &c->d_seen[0], &c->d_seen[1], &c->d_pred, &c->d_diff, &c->d_ckpt,
-                      &c->d_from})
+                      &c->d_from, &c->d_ranks})
         b->release();
     for (auto& S : c->slot) {
         for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work,
-                          &S.redo})
+                          &S.redo, &S.rk_items})
             b->release();
         S.h_tables.release();
         if (S.stream) cudaStreamDestroy(S.stream);
@@ -617,6 +617,27 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             CUDA_TRY(c, cudaEventRecord(c->ev_copy[gi], c->copy_stream));
         }
     }
+    // Precomputed ranks (2 bytes per input byte) in one buffer for all
+    // groups: a group's rank kernel runs after the previous group's tile and
+    // fix kernels, its only readers.  Sized once for the largest group;
+    // without the room the tile kernels compute the ranks themselves.
+    bool pre_ranks = c->pre_ranks;
+    if (pre_ranks) {
+        uint64_t most = 0;
+        for (const Group& g : groups) {
+            uint64_t r8 = 0;
+            for (uint32_t k = 0; k < g.count; k++) {
+                const uint64_t len = lens[g.first + k];
+                if (len >= kMinFile) r8 += (len + 7) / 8 + len / kChunkBytes + 1;  // per chunk, to a multiple of 8
+            }
+            most = std::max(most, r8);
+        }
+        if (c->d_ranks.ensure(most * 16 + 16) != cudaSuccess) {
+            cudaGetLastError();
+            c->d_ranks.release();
+            pre_ranks = false;
+        }
+    }
     cudaEvent_t prev_scan = c->ev_start, prev_tiles = c->ev_start;
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
@@ -627,7 +648,8 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         S.used = true;
         CUDA_TRY(c, cudaStreamWaitEvent(st, c->ev_start, 0));
         // ---- work lists (pinned host staging, copied asynchronously)
-        uint64_t nchunks = 0, ntiles = 0, bytes = 0;
+        // rank stretches: every chunk position (to a multiple of 8), kRkSpan at a time
+        uint64_t nchunks = 0, ntiles = 0, bytes = 0, nrk = 0;
         for (uint32_t k = 0; k < g.count; k++) {
             const uint64_t len = lens[g.first + k];
             bytes += (len + 15) & ~15ull;
@@ -636,15 +658,24 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
                 const uint64_t m = std::min<uint64_t>(kChunkBytes, len - pos);
                 nchunks++;
                 if (m > 64) ntiles += (m - 64 + kTileL - 1) / kTileL;
+                nrk += ((m + 7) / 8 * 8 + kRkSpan - 1) / kRkSpan;
             }
+        }
+        bool pre = pre_ranks && ntiles;
+        if (pre && S.rk_items.ensure(nrk * sizeof(uint2)) != cudaSuccess) {
+            cudaGetLastError();
+            S.rk_items.release();
+            pre = false;
         }
         const size_t tb_chunks = nchunks * sizeof(GenChunk), tb_tiles = ntiles * sizeof(GenTile);
         const size_t tb_files = g.count * sizeof(GenFile), tb_order = g.count * sizeof(uint32_t);
-        CUDA_TRY(c, S.h_tables.ensure(tb_chunks + tb_tiles + tb_files + tb_order + 64));
+        const size_t tb_rk = pre ? nrk * sizeof(uint2) : 0;
+        CUDA_TRY(c, S.h_tables.ensure(tb_chunks + tb_tiles + tb_files + tb_order + tb_rk + 64));
         GenChunk* hc = reinterpret_cast<GenChunk*>(S.h_tables.p);
         GenTile* ht = reinterpret_cast<GenTile*>(reinterpret_cast<uint8_t*>(S.h_tables.p) + tb_chunks);
         GenFile* hf = reinterpret_cast<GenFile*>(reinterpret_cast<uint8_t*>(ht) + tb_tiles);
         uint32_t* ho = reinterpret_cast<uint32_t*>(reinterpret_cast<uint8_t*>(hf) + tb_files);
+        uint2* hr = reinterpret_cast<uint2*>(reinterpret_cast<uint8_t*>(ho) + tb_order);
         const uint8_t* gdata;
         std::vector<uint64_t> doff(g.count);
         if (dev_data) {
@@ -676,7 +707,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
                 }
             }
         }
-        uint32_t ci = 0, ti = 0;
+        uint32_t ci = 0, ti = 0, ri = 0, r8 = 0;
         uint64_t work = 0;
         for (uint32_t k = 0; k < g.count; k++) {
             const uint32_t i = g.first + k;
@@ -684,10 +715,13 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             if (lens[i] >= kMinFile) {
                 for (uint64_t pos = 0; pos < lens[i]; pos += kChunkBytes) {
                     const uint32_t m = (uint32_t)std::min<uint64_t>(kChunkBytes, lens[i] - pos);
-                    GenChunk ch{doff[k] + pos, m, k, ti, 0, 0, 0};
+                    GenChunk ch{doff[k] + pos, m, k, ti, 0, 0, 0, r8};
                     if (m > 64)
                         for (uint32_t t0 = 0; t0 < m - 64; t0 += kTileL) ht[ti++] = GenTile{ci, t0};
                     ch.ntiles = ti - ch.first_tile;
+                    if (pre)
+                        for (uint32_t s0 = 0; s0 < (m + 7) / 8 * 8; s0 += kRkSpan) hr[ri++] = make_uint2(ci, s0);
+                    r8 += (m + 7) / 8;
                     hc[ci++] = ch;
                     f.nchunks++;
                 }
@@ -712,6 +746,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         if (tb_tiles) CUDA_TRY(c, cudaMemcpyAsync(S.tiles.p, ht, tb_tiles, cudaMemcpyHostToDevice, st));
         CUDA_TRY(c, cudaMemcpyAsync(S.files.p, hf, tb_files, cudaMemcpyHostToDevice, st));
         CUDA_TRY(c, cudaMemcpyAsync(S.order.p, ho, tb_order, cudaMemcpyHostToDevice, st));
+        if (tb_rk) CUDA_TRY(c, cudaMemcpyAsync(S.rk_items.p, hr, tb_rk, cudaMemcpyHostToDevice, st));
         GenParams P{};
         P.data = gdata;
         P.rank_tab = c->d_rank.as<uint16_t>();
@@ -731,12 +766,20 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         P.out_filters = S.work.as<uint32_t>();
         P.out_info = c->d_binfo.as<FileInfoDev>() + g.first;
         P.chunk_redo = S.redo.as<uint32_t>();
+        if (pre) {
+            P.ranks = c->d_ranks.as<uint16_t>();
+            P.rk_items = S.rk_items.as<uint2>();
+            P.nrk_items = (uint32_t)nrk;
+        }
         const uint32_t cap_grid = (uint32_t)c->sms * 3 * 16;
         // the groups' tile kernels run one after another (each fills the GPU),
         // so a group's commit overlaps the next group's tiles instead of all
         // groups in flight finishing their tiles together and then waiting
         // on their commits
         CUDA_TRY(c, cudaStreamWaitEvent(st, prev_tiles, 0));
+        if (pre)
+            TIMED_LAUNCH_ON(c, "k_stream_ranks", st,
+                            launch_stream_ranks(P, std::min<uint32_t>(P.nrk_items, cap_grid), st));
         if (P.ntiles)
             TIMED_LAUNCH_ON(c, "k_stream_tiles", st, launch_stream_tiles(P, std::min<uint32_t>(P.ntiles, cap_grid), st));
         if (P.nchunks) {

@@ -80,6 +80,21 @@ __device__ __forceinline__ void load_be16(const uint32_t* sm32, uint32_t p, uint
     }
 }
 
+// The same 16 words for 64 bytes at any global address: aligned word loads
+// (none past the word holding the last byte) joined by byte permutes.
+__device__ __forceinline__ void load_be16_global(const uint8_t* src, uint32_t (&w)[16]) {
+    const uintptr_t ad = reinterpret_cast<uintptr_t>(src);
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(ad & ~(uintptr_t)3);
+    const uint32_t a = (uint32_t)(ad & 3);
+    const uint32_t sel = (a << 12) | ((a + 1) << 8) | ((a + 2) << 4) | (a + 3);
+    uint32_t v[17];
+#pragma unroll
+    for (int k = 0; k < 16; k++) v[k] = __ldg(q + k);
+    v[16] = a ? __ldg(q + 16) : 0u;
+#pragma unroll
+    for (int k = 0; k < 16; k++) w[k] = __byte_perm(v[k], v[k + 1], sel);
+}
+
 // ------------------------------------------------- popularity-chain state
 // State entering a window step i of gen_chunk_scores (sdbf_core.cc:58-82):
 // (P, M) = current (min_pos, min_rank).  M == 0 means the next step is a
