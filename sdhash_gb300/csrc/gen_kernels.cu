@@ -981,6 +981,18 @@ __global__ void __launch_bounds__(kGenThreads) k_stream_fix(GenParams P) {
     }
 }
 
+// ------------------------------------------------------ async copies
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+// The L2 prefetch of [gmem, gmem+bytes) (16-byte aligned, a multiple of 16 bytes).
+__device__ __forceinline__ void prefetch_l2(const void* gmem, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(gmem), "r"(bytes) : "memory");
+}
+
 // ------------------------------------------------ precomputed ranks
 // Entropy ranks of a stream launch group ahead of its tile kernel.  One CTA
 // item is a stretch of kRkSpan positions of a chunk, its bytes staged in
@@ -1008,15 +1020,26 @@ __global__ void __launch_bounds__(kRkThreads, 3) k_stream_ranks(GenParams P) {
         const uint32_t np = min(kRkSpan, align_up(n, 8) - s0);  // positions [s0, s0+np)
         const uint32_t nb = min(kRkSpan + 64, n - s0);          // bytes [s0, s0+nb)
         __syncthreads();  // the previous stretch is done with the bytes and histograms
+        // the stretch's bytes: 16-byte asynchronous copies, all in flight at once
         const uint8_t* src = P.data + C.data_off + s0;
         const uint32_t nvec = ((reinterpret_cast<uintptr_t>(src) & 15) == 0) ? nb / 16 : 0;
         const uint4* s4 = reinterpret_cast<const uint4*>(src);
         uint4* d4 = reinterpret_cast<uint4*>(b32);
-        for (uint32_t i = tid; i < nvec; i += blockDim.x) d4[i] = __ldg(s4 + i);
+        for (uint32_t i = tid; i < nvec; i += blockDim.x) cp_async16(d4 + i, s4 + i);
+        cp_async_commit();
         uint8_t* d8 = reinterpret_cast<uint8_t*>(b32);
         for (uint32_t i = nvec * 16 + tid; i < nb + 8; i += blockDim.x) d8[i] = (i < nb) ? src[i] : 0;
         uint4* h4 = reinterpret_cast<uint4*>(hist);
         for (uint32_t i = tid; i < 256 * kRkThreads / 16; i += blockDim.x) h4[i] = make_uint4(0, 0, 0, 0);
+        // the CTA's next stretch into L2 while this one is ranked
+        if (tid == 0 && item + gridDim.x < P.nrk_items) {
+            const uint2 nx = P.rk_items[item + gridDim.x];
+            const GenChunk Cn = P.chunks[nx.x];
+            const uint8_t* ns = P.data + Cn.data_off + nx.y;
+            const uint32_t nnb = min(kRkSpan + 64, Cn.n - nx.y) & ~15u;
+            if ((reinterpret_cast<uintptr_t>(ns) & 15) == 0 && nnb) prefetch_l2(ns, nnb);
+        }
+        cp_async_wait_all();
         __syncthreads();
         const uint32_t lo = min(np, tid * kRkPer), hi = min(np, lo + kRkPer);
         const uint32_t last = n > kWin ? n - kWin : 0;  // ranks exist for o < n-64 only
@@ -1046,12 +1069,6 @@ __device__ inline uint32_t lanemask_lt() {
     return m;
 }
 
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
 // Stage the first `nf` features of a tile (5 rows of kTileCap words) into buf.
 __device__ __forceinline__ void stage_tile(uint32_t (*buf)[kTileCap], const uint32_t* feat, uint32_t nf,
