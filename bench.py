@@ -47,8 +47,8 @@ CONFIG_BASE = {"workload": "bulk stream-mode digest generation", "files": 4096, 
                "mode": "stream (-b 0)", "l2": "inputs larger than L2 (no flush needed)"}
 
 
-KERNELS = ("k_stream_ranks", "k_stream_tiles", "k_stream_check", "k_stream_fix", "k_stream_commit", "k_pack_filters",
-           "k_scan_offsets")
+KERNELS = ("k_stream_ranks", "k_stream_tiles", "k_stream_fails", "k_stream_fix_list", "k_stream_check", "k_stream_fix",
+           "k_stream_commit", "k_pack_filters", "k_scan_offsets")
 
 
 def parse():

@@ -159,7 +159,7 @@ struct sdbfg_ctx {
         cudaStream_t stream = nullptr;
         cudaEvent_t done = nullptr;
         bool used = false;
-        DevBuf data, chunks, tiles, files, order, tile_out, features, work, redo;
+        DevBuf data, chunks, tiles, files, order, tile_out, features, work, redo, fix_list;
         DevBuf rk_items;  // stretches of the group's chunks for k_stream_ranks
         HostBuf h_tables;
     } slot[kSlots];

@@ -591,11 +591,6 @@ __device__ __forceinline__ ChainState walk(const TileGeom& g, const TileSmem& s,
     return st;
 }
 
-// Lead-in of a tile's first segment: the maximum for leads from
-// kFullTileLead on (a failed link between tiles recomputes a whole tile),
-// the configured lead below it (so tests can drive the cross-tile path).
-__host__ __device__ inline uint32_t tile_lead(uint32_t lead) { return lead >= kFullTileLead ? kLead : lead; }
-
 // Re-walk segment [St, Et) from its true entry state `nw` next to the chain
 // it was credited with (`old`, from its speculative entry).  Both walks run
 // in lockstep; credits differ only until the two states coincide, after
@@ -690,9 +685,10 @@ __device__ void tile_pipeline(const uint8_t* __restrict__ chunk, const TileGeom&
             } else {
                 // lead-in (never below Q0, since every lead <= kLead); a lead-in
                 // from step 0 makes the walk exact.  The tile's first segment
-                // uses tile_lead: its mis-speculation costs a tile recompute.
-                const uint32_t ld = t == 0 ? tile_lead(lead) : lead;
-                const uint32_t Ls = St > ld ? St - ld : 0;
+                // has the same lead as the others (a longer one would hold up
+                // its warp): its rare mis-speculation costs a tile recompute
+                // in k_stream_fix.
+                const uint32_t Ls = St > lead ? St - lead : 0;
                 st = walk(g, s, Ls, St, st, (Credit<1>*)nullptr);
             }
             s.sig[t] = pack_state(st);
@@ -932,11 +928,13 @@ __global__ void __launch_bounds__(kGenThreads, 5) k_stream_tiles_pre(GenParams P
 // k_stream_check (one warp per chunk, no shared memory) finds the first
 // tile of each chunk whose link fails; k_stream_fix (one CTA per chunk,
 // normally exiting at once) recomputes that tile from the true entry state
-// and walks on through the chunk, recomputing every later tile whose link
-// still fails.
+// and moves on through the chunk: its threads check the links of the next
+// kGenThreads tiles at once, and the first failing one (a later tile whose
+// entry no longer matches, or an unrelated mis-speculation) is recomputed
+// next.
 __device__ __forceinline__ bool link_fails(const GenParams& P, const GenChunk& C, uint32_t tile) {
     const TileGeom g = stream_geom(C.n, P.tiles[tile].t0);
-    return g.S0 > tile_lead(P.lead) && P.tile_out[tile - 1].tau_out != P.tile_out[tile].sig_in;
+    return g.S0 > P.lead && P.tile_out[tile - 1].tau_out != P.tile_out[tile].sig_in;
 }
 
 __global__ void __launch_bounds__(128) k_stream_check(GenParams P) {
@@ -956,27 +954,64 @@ __global__ void __launch_bounds__(128) k_stream_check(GenParams P) {
     }
 }
 
+// Before k_stream_check / k_stream_fix: every tile whose link fails goes
+// to P.fix_list (fix_list[0] = their number, zeroed by the host), and
+// k_stream_fix_list recomputes them all at once, one CTA each, from their
+// predecessors' exit states as they stand.  A tile whose predecessor is
+// recomputed in the same launch may start from the stale state; the
+// serial pass that follows finds and redoes it (normally nothing is left).
+__global__ void __launch_bounds__(256) k_stream_fails(GenParams P) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < P.ntiles; t += gridDim.x * blockDim.x) {
+        const GenChunk C = P.chunks[P.tiles[t].chunk];
+        if (t > C.first_tile && link_fails(P, C, t)) P.fix_list[1 + atomicAdd(P.fix_list, 1u)] = t;
+    }
+}
+
+template <bool kPre>
+__global__ void __launch_bounds__(kGenThreads) k_stream_fix_list(GenParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint64_t entry;
+    const uint32_t n = P.fix_list[0];
+    for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
+        const uint32_t tile = P.fix_list[1 + k];
+        if (threadIdx.x == 0) entry = P.tile_out[tile - 1].tau_out;
+        __syncthreads();
+        stream_tile_body<kPre>(P, tile, &entry, smem);
+        if (threadIdx.x == 0) atomicAdd(P.counters + 0, 1u);
+        __syncthreads();
+    }
+}
+
 template <bool kPre>
 __global__ void __launch_bounds__(kGenThreads) k_stream_fix(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ uint64_t entry;
-    __shared__ int redo;
+    __shared__ uint32_t bad_first;
     for (uint32_t c = blockIdx.x; c < P.nchunks; c += gridDim.x) {
         const uint32_t first = P.chunk_redo[c];
         if (first == 0xFFFFFFFFu) continue;
         const GenChunk C = P.chunks[c];
-        for (uint32_t j = first; j < C.ntiles; j++) {
-            const uint32_t tile = C.first_tile + j;
-            if (threadIdx.x == 0) {
-                redo = link_fails(P, C, tile);
-                entry = P.tile_out[tile - 1].tau_out;
-            }
+        uint32_t j = first;
+        while (j < C.ntiles) {
+            // the first failing link among tiles [j, j + blockDim.x); tiles
+            // recomputed before it are visible here (same CTA, after a barrier)
+            if (threadIdx.x == 0) bad_first = 0xFFFFFFFFu;
             __syncthreads();
-            if (redo) {
-                stream_tile_body<kPre>(P, tile, &entry, smem);
-                if (threadIdx.x == 0) atomicAdd(P.counters + 0, 1u);
-            }
+            const uint32_t jj = j + threadIdx.x;
+            if (jj < C.ntiles && link_fails(P, C, C.first_tile + jj)) atomicMin(&bad_first, jj);
             __syncthreads();
+            const uint32_t f = bad_first;
+            if (f == 0xFFFFFFFFu) {
+                j += blockDim.x;
+                continue;
+            }
+            const uint32_t tile = C.first_tile + f;
+            if (threadIdx.x == 0) entry = P.tile_out[tile - 1].tau_out;
+            __syncthreads();
+            stream_tile_body<kPre>(P, tile, &entry, smem);
+            if (threadIdx.x == 0) atomicAdd(P.counters + 0, 1u);
+            __syncthreads();
+            j = f + 1;
         }
     }
 }
@@ -1706,6 +1741,8 @@ static void set_stream_attrs() {
     cudaFuncSetAttribute(k_stream_fix<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     cudaFuncSetAttribute(k_stream_tiles_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
     cudaFuncSetAttribute(k_stream_fix<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
+    cudaFuncSetAttribute(k_stream_fix_list<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    cudaFuncSetAttribute(k_stream_fix_list<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
     cudaFuncSetAttribute(k_stream_ranks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRkSmem);
     cudaFuncSetAttribute(k_stream_commit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(CommitSmem) * kCommitWarps));
@@ -1724,6 +1761,20 @@ cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t 
         k_stream_tiles_pre<<<grid, kGenThreads, stream_tile_smem_pre(), st>>>(P);
     else
         k_stream_tiles<<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_fails(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    if (grid) k_stream_fails<<<grid, 256, 0, st>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stream_fix_list(const GenParams& P, uint32_t grid, cudaStream_t st) {
+    set_stream_attrs();
+    if (P.ranks)
+        k_stream_fix_list<true><<<grid, kGenThreads, stream_tile_smem_pre(), st>>>(P);
+    else
+        k_stream_fix_list<false><<<grid, kGenThreads, stream_tile_smem(), st>>>(P);
     return cudaGetLastError();
 }
 

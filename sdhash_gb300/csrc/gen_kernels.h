@@ -15,7 +15,6 @@ constexpr uint32_t kLead = 128;      // maximum speculative lead-in steps per se
 constexpr uint32_t kDefaultLead = 64; // default lead-in (measured best of 16..128 on the bulk stream
                                      // workload); mis-speculated segments are re-walked only until
                                      // their chain meets the speculative one
-constexpr uint32_t kFullTileLead = 48;  // leads from here on give a tile's first segment kLead
 // window steps owned by a stream tile: with the 64-step credit halo and the
 // 128-step maximum lead-in a tile simulates 8128 steps (127 aligned 64-step
 // blocks, one per thread of the full-rescan table)
@@ -93,6 +92,7 @@ struct GenParams {
     uint32_t lead;               // speculative lead-in steps (<= kLead)
     unsigned long long* phase;   // optional phase cycle counters (kPhase*), null = off
     uint32_t* chunk_redo;        // per chunk: first tile whose link failed (stream)
+    uint32_t* fix_list;          // stream: [0] = n, then the n tiles whose link failed
     // block mode with index search: SHA-1 words of every fourth counted
     // feature of each block ([slot][kProbeWords]) and their number per slot;
     // null = no search
@@ -148,6 +148,10 @@ cudaError_t launch_stream_ranks(const GenParams& P, uint32_t grid, cudaStream_t 
 // Tile kernels: with P.ranks set they read the precomputed ranks (and the
 // feature bytes from the input in global memory), else they compute ranks.
 cudaError_t launch_stream_tiles(const GenParams& P, uint32_t grid, cudaStream_t st);
+// Tiles whose link fails into P.fix_list (zeroed count first), then all of
+// them recomputed in parallel; k_stream_check / k_stream_fix finish the job.
+cudaError_t launch_stream_fails(const GenParams& P, uint32_t grid, cudaStream_t st);
+cudaError_t launch_stream_fix_list(const GenParams& P, uint32_t grid, cudaStream_t st);
 cudaError_t launch_stream_check(const GenParams& P, uint32_t grid, cudaStream_t st);  // 4 chunks per CTA
 cudaError_t launch_stream_fix(const GenParams& P, uint32_t grid, cudaStream_t st);
 cudaError_t launch_stream_commit(const GenParams& P, uint32_t grid, cudaStream_t st);

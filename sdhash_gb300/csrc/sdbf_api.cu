@@ -68,7 +68,7 @@ extern "C" void sdbfg_ctx_destroy(sdbfg_ctx* c) {
         b->release();
     for (auto& S : c->slot) {
         for (DevBuf* b : {&S.data, &S.chunks, &S.tiles, &S.files, &S.order, &S.tile_out, &S.features, &S.work,
-                          &S.redo, &S.rk_items})
+                          &S.redo, &S.rk_items, &S.fix_list})
             b->release();
         S.h_tables.release();
         if (S.stream) cudaStreamDestroy(S.stream);
@@ -742,6 +742,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         CUDA_TRY(c, S.features.ensure(std::max<uint64_t>(1, ntiles) * 5ull * kTileCap * 4));
         CUDA_TRY(c, S.work.ensure(std::max<uint64_t>(1, work) * 256));
         CUDA_TRY(c, S.redo.ensure(std::max<uint64_t>(1, nchunks) * 4));
+        CUDA_TRY(c, S.fix_list.ensure((ntiles + 1) * 4));
         if (tb_chunks) CUDA_TRY(c, cudaMemcpyAsync(S.chunks.p, hc, tb_chunks, cudaMemcpyHostToDevice, st));
         if (tb_tiles) CUDA_TRY(c, cudaMemcpyAsync(S.tiles.p, ht, tb_tiles, cudaMemcpyHostToDevice, st));
         CUDA_TRY(c, cudaMemcpyAsync(S.files.p, hf, tb_files, cudaMemcpyHostToDevice, st));
@@ -766,6 +767,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         P.out_filters = S.work.as<uint32_t>();
         P.out_info = c->d_binfo.as<FileInfoDev>() + g.first;
         P.chunk_redo = S.redo.as<uint32_t>();
+        P.fix_list = S.fix_list.as<uint32_t>();
         if (pre) {
             P.ranks = c->d_ranks.as<uint16_t>();
             P.rk_items = S.rk_items.as<uint2>();
@@ -783,6 +785,13 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         if (P.ntiles)
             TIMED_LAUNCH_ON(c, "k_stream_tiles", st, launch_stream_tiles(P, std::min<uint32_t>(P.ntiles, cap_grid), st));
         if (P.nchunks) {
+            if (P.ntiles) {
+                CUDA_TRY(c, cudaMemsetAsync(P.fix_list, 0, 4, st));
+                TIMED_LAUNCH_ON(c, "k_stream_fails", st,
+                                launch_stream_fails(P, std::min<uint32_t>((P.ntiles + 255) / 256, cap_grid), st));
+                TIMED_LAUNCH_ON(c, "k_stream_fix_list", st,
+                                launch_stream_fix_list(P, std::min<uint32_t>(P.ntiles, (uint32_t)c->sms * 5), st));
+            }
             TIMED_LAUNCH_ON(c, "k_stream_check", st, launch_stream_check(P, (P.nchunks + 3) / 4, st));
             TIMED_LAUNCH_ON(c, "k_stream_fix", st,
                             launch_stream_fix(P, std::min<uint32_t>(P.nchunks, cap_grid), st));
