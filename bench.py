@@ -1484,8 +1484,21 @@ def main():
                  "ceiling_GBs_at_full_issue": issue_peak / wipb / 1e9,
                  "source": "profiles/k_stream_tiles_ncu.md (smsp__inst_executed per input byte); peak = 152 SMs x "
                            "4 schedulers x median SM clock"}
-    roofline = {"bound": "hbm", "kernel": "k_stream_tiles", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "issue": issue,
+    # the rank kernel that runs ahead of each tile launch: input bytes per
+    # second of its launches, and the same issue arithmetic
+    ranks_ms, ranks_n = kern.get("k_stream_ranks", (0.0, 0))
+    ranks = None
+    if ranks_ms > 0:
+        r_ach = total_bytes / (ranks_ms / 1e3) / 1e9
+        r_wipb = profiled_value("k_stream_ranks", "warp_inst_per_input_byte")
+        r_tpb = profiled_traffic("k_stream_ranks")
+        ranks = {"kernel": "k_stream_ranks", "launches": ranks_n, "achieved_GBs": r_ach,
+                 "frac_of_hbm": r_ach / peak if peak else None,
+                 "traffic": (r_tpb * per_launch_bytes) if r_tpb else None,
+                 "issue_frac": (r_wipb * r_ach * 1e9 / issue_peak) if r_wipb else None,
+                 "warp_inst_per_input_byte": r_wipb}
+    roofline = {"bound": "hbm", "kernel": "k_stream_tiles_pre", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "issue": issue, "ranks_kernel": ranks,
                 "frac": (achieved / peak) if achieved else None,
                 "traffic": (tpb * per_launch_bytes) if tpb else None,
                 "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)",

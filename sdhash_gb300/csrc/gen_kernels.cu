@@ -520,10 +520,16 @@ struct Credit {
     }
     // step i credits p when act (its min rank is not 0); a step that
     // credits nothing opens a run of ~0u, which is never added
+    // (the open run is closed inline: one predicate for "changed and in range")
     __device__ __forceinline__ void add(uint32_t i, uint32_t p, bool act) {
         const uint32_t key = act ? p : ~0u;
         const bool chg = key != cur;
-        if (chg) flush(i);
+        const uint32_t o = cur - lo;
+        if (chg && o < hi - lo) {
+            const uint32_t inc = (i - start) << (8 * (o & 3));
+            if (kSign > 0) atomicAdd(&score32[o >> 2], inc);
+            else atomicSub(&score32[o >> 2], inc);
+        }
         cur = chg ? key : cur;
         start = chg ? i : start;
     }
