@@ -1752,6 +1752,16 @@ static void set_stream_attrs() {
     cudaFuncSetAttribute(k_stream_ranks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRkSmem);
     cudaFuncSetAttribute(k_stream_commit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(CommitSmem) * kCommitWarps));
+    // one shared-memory / L1 split for every kernel of the stream pipeline
+    // (the largest shared memory): CTAs of different kernels can then share
+    // an SM
+    for (const void* f : {(const void*)k_stream_ranks, (const void*)k_stream_tiles, (const void*)k_stream_tiles_pre,
+                          (const void*)k_stream_fails, (const void*)k_stream_fix_list<false>,
+                          (const void*)k_stream_fix_list<true>, (const void*)k_stream_check,
+                          (const void*)k_stream_fix<false>, (const void*)k_stream_fix<true>,
+                          (const void*)k_stream_commit, (const void*)k_stream_commit_round,
+                          (const void*)k_stream_commit_index})
+        cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
     done = true;
 }
 

@@ -409,6 +409,11 @@ static int ensure_pipeline(sdbfg_ctx* c) {
         }
     }
     if (!c->ev_start) CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming));
+    // the pipeline's small kernels take the tile kernels' shared-memory / L1
+    // split, so their CTAs can share an SM with them
+    for (const void* f : {(const void*)k_stage_gather, (const void*)k_scan_offsets, (const void*)k_pack_group})
+        cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+    cudaGetLastError();
     return SDBFG_OK;
 }
 
