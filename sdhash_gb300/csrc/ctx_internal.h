@@ -145,7 +145,7 @@ struct sdbfg_ctx {
     int sms = 152;
     uint32_t lead = kDefaultLead;
     bool pre_ranks = true;  // stream mode: ranks by k_stream_ranks ahead of the tile kernel
-    DevBuf d_ranks;         // their ranks (one buffer: groups' rank kernels run one after another)
+    DevBuf d_ranks;         // their ranks (two halves, by launch-group parity)
     // constant tables
     DevBuf d_rank, d_ent, d_cut, d_cut64;
     // generation buffers

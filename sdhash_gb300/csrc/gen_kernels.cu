@@ -423,7 +423,9 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
                 for (int h = 1; h >= 0; h--) {
                     const uint32_t u = 8u * gi + 2 * q + h;
                     const uint32_t r = h ? (cur[q] >> 16) : (cur[q] & 0xFFFFu);
-                    const bool take = r != 0 && (r < m || (r == m && rn != m));
+                    // r != 0 and (r < m, or r == m after a run break), as one
+                    // unsigned compare (m >= 1): r - 1 < m - (rn == m)
+                    const bool take = (r - 1u) < (m - (uint32_t)(rn == m));
                     m = take ? r : m;
                     e = take ? u : e;
                     rn = r;
@@ -473,7 +475,7 @@ __device__ inline void compute_fres(const TileGeom& g, const TileSmem& s) {
                 const uint32_t r = (t & 1) ? (rb[t >> 1] >> 16) : (rb[t >> 1] & 0xFFFFu);
                 lead_open = lead_open && r == rb0;
                 lead64 = lead_open ? 64 + v : lead64;
-                const bool lower = r != 0 && r < pm;
+                const bool lower = (r - 1u) < (pm - 1u);  // r != 0 && r < pm (pm >= 1)
                 const bool cont = open && r == pm;  // pm > 0, so r != 0
                 pm = lower ? r : pm;
                 open = lower || cont;

@@ -622,9 +622,10 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             CUDA_TRY(c, cudaEventRecord(c->ev_copy[gi], c->copy_stream));
         }
     }
-    // Precomputed ranks (2 bytes per input byte) in one buffer for all
-    // groups: a group's rank kernel runs after the previous group's tile and
-    // fix kernels, its only readers.  Sized once for the largest group;
+    // Precomputed ranks (2 bytes per input byte) in two halves, by group
+    // parity: a group's rank kernel waits for the tile and fix kernels of the
+    // group two back (the last readers of its half) and runs beside the
+    // previous group's tile kernel.  Sized once for the largest group;
     // without the room the tile kernels compute the ranks themselves.
     bool pre_ranks = c->pre_ranks;
     if (pre_ranks) {
@@ -637,13 +638,14 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
             }
             most = std::max(most, r8);
         }
-        if (c->d_ranks.ensure(most * 16 + 16) != cudaSuccess) {
+        if (c->d_ranks.ensure(2 * (most * 16 + 16)) != cudaSuccess) {
             cudaGetLastError();
             c->d_ranks.release();
             pre_ranks = false;
         }
     }
-    cudaEvent_t prev_scan = c->ev_start, prev_tiles = c->ev_start;
+    cudaEvent_t prev_scan = c->ev_start, prev_tiles = c->ev_start, prev2_tiles = c->ev_start;
+    const uint64_t rank_half = c->d_ranks.cap / 2 / 16 * 16;  // bytes per half, 16-byte aligned
     for (size_t gi = 0; gi < groups.size(); gi++) {
         const Group& g = groups[gi];
         const int depth = ib ? 1 : std::max(1, std::min(c->depth, kSlots));
@@ -774,7 +776,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         P.chunk_redo = S.redo.as<uint32_t>();
         P.fix_list = S.fix_list.as<uint32_t>();
         if (pre) {
-            P.ranks = c->d_ranks.as<uint16_t>();
+            P.ranks = c->d_ranks.as<uint16_t>() + (gi & 1) * (rank_half / 2);
             P.rk_items = S.rk_items.as<uint2>();
             P.nrk_items = (uint32_t)nrk;
         }
@@ -783,10 +785,12 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
         // so a group's commit overlaps the next group's tiles instead of all
         // groups in flight finishing their tiles together and then waiting
         // on their commits
-        CUDA_TRY(c, cudaStreamWaitEvent(st, prev_tiles, 0));
-        if (pre)
+        if (pre) {
+            CUDA_TRY(c, cudaStreamWaitEvent(st, prev2_tiles, 0));
             TIMED_LAUNCH_ON(c, "k_stream_ranks", st,
                             launch_stream_ranks(P, std::min<uint32_t>(P.nrk_items, cap_grid), st));
+        }
+        CUDA_TRY(c, cudaStreamWaitEvent(st, prev_tiles, 0));
         if (P.ntiles)
             TIMED_LAUNCH_ON(c, "k_stream_tiles", st, launch_stream_tiles(P, std::min<uint32_t>(P.ntiles, cap_grid), st));
         if (P.nchunks) {
@@ -802,6 +806,7 @@ static int digest_stream_pipelined(sdbfg_ctx* c, const uint8_t* host_data, const
                             launch_stream_fix(P, std::min<uint32_t>(P.nchunks, cap_grid), st));
         }
         CUDA_TRY(c, cudaEventRecord(c->ev_tiles[gi % depth], st));
+        prev2_tiles = prev_tiles;
         prev_tiles = c->ev_tiles[gi % depth];
         if (ib) {
             P.index_bits = ib->bits;
