@@ -195,7 +195,8 @@ __device__ inline void load_bytes(const uint8_t* __restrict__ chunk, const TileG
 // ------------------------------------------------------- phase 2: ranks
 // dtab[c] = T[c+1] - T[c] (c = 0..63): entropy change when a byte value's
 // count in the window goes from c to c+1 (entr64_inc_int, entr64.cc:47-71,
-// written as differences of the table of entr64_table_init_int).
+// written as differences of the table of entr64_table_init_int); dtab[64]
+// = 0 pads the table for the branch-free step pair.
 //
 // Each of kRankThreads threads owns a run of positions starting at a
 // multiple of 8 and keeps the byte counts of its window in its own
@@ -214,24 +215,23 @@ __device__ __forceinline__ void rank_pair(uint8_t* h, uint32_t hbase, const int3
     const uint32_t ha1 = hbase + ((a1 >> 2) << 7) + (a1 & 3), hb1 = hbase + ((b1 >> 2) << 7) + (b1 & 3);
     const int32_t ca0 = h[ha0], cb0 = h[hb0];
     int32_t ca1 = h[ha1], cb1 = h[hb1];
-    const bool d0 = a0 != b0, d1 = a1 != b1;
-    if (d0) {
-        e += dtab[cb0] - dtab[ca0 - 1];
-        ca1 += (int32_t)(a1 == b0) - (int32_t)(a1 == a0);
-        cb1 += (int32_t)(b1 == b0) - (int32_t)(b1 == a0);
-    }
+    // no branches: when a step's leaving and entering bytes are equal, its
+    // two counters are one, the stores below write that count back
+    // unchanged, its entropy change is dropped, and the second step's
+    // corrections are 0 (dtab has a 0 at index 64 for a count of 64 there)
+    const int32_t d0 = (int32_t)(a0 != b0), d1 = (int32_t)(a1 != b1);
+    const int32_t x0 = dtab[cb0] - dtab[ca0 - 1];
+    ca1 += (int32_t)(a1 == b0) - (int32_t)(a1 == a0);
+    cb1 += (int32_t)(b1 == b0) - (int32_t)(b1 == a0);
+    e += d0 ? x0 : 0;
     e0 = e;
-    if (d1) e += dtab[cb1] - dtab[ca1 - 1];
+    const int32_t x1 = dtab[cb1] - dtab[ca1 - 1];
+    e += d1 ? x1 : 0;
     e1 = e;
-    // later stores win where both steps touch the same byte value
-    if (d0) {
-        h[ha0] = (uint8_t)(ca0 - 1);
-        h[hb0] = (uint8_t)(cb0 + 1);
-    }
-    if (d1) {
-        h[ha1] = (uint8_t)(ca1 - 1);
-        h[hb1] = (uint8_t)(cb1 + 1);
-    }
+    h[ha0] = (uint8_t)(ca0 - d0);
+    h[hb0] = (uint8_t)(cb0 + d0);
+    h[ha1] = (uint8_t)(ca1 - d1);
+    h[hb1] = (uint8_t)(cb1 + d1);
 }
 
 // One window step: byte a leaves, byte b enters.
@@ -863,9 +863,9 @@ __device__ void stream_tile_body(const GenParams& P, uint32_t tile, const uint64
     const uint16_t* rank_tab = nullptr;
     const int32_t* dt = nullptr;
     if constexpr (!kPre) {
-        __shared__ int32_t dtab[64];
-        for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x)
-            dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
+        __shared__ int32_t dtab[65];
+        for (uint32_t i = threadIdx.x; i < 65; i += blockDim.x)
+            dtab[i] = i < 64 ? (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i] : 0;
         // the rank table (2 KB) in shared memory: a lookup is one shared-memory read
         __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
         for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];
@@ -1041,7 +1041,7 @@ __device__ __forceinline__ void prefetch_l2(const void* gmem, uint32_t bytes) {
 // item is a stretch of kRkSpan positions of a chunk, its bytes staged in
 // shared memory with 16-byte loads; each thread ranks kRkPer consecutive
 // positions with its own histogram (rank_run, the tile kernel's rank loop),
-// so a thread's 64-byte window set-up is spread over 264 positions instead
+// so a thread's 64-byte window set-up is spread over 312 positions instead
 // of a tile thread's 88.  Ranks of positions >= n-64 are 0; the chunk's
 // ranks run to a multiple of 8 (GenChunk::rank_off8).
 constexpr uint32_t kRkBytes = align_up(kRkSpan + 64 + 16, 16);  // staged bytes + zero padding
@@ -1051,9 +1051,9 @@ __global__ void __launch_bounds__(kRkThreads, 3) k_stream_ranks(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint8_t* hist = smem;
     uint32_t* b32 = reinterpret_cast<uint32_t*>(smem + 256 * kRkThreads);
-    __shared__ int32_t dtab[64];
+    __shared__ int32_t dtab[65];
     __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
-    for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
+    for (uint32_t i = threadIdx.x; i < 65; i += blockDim.x) dtab[i] = i < 64 ? (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i] : 0;
     for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];
     const uint32_t tid = threadIdx.x;
     for (uint32_t item = blockIdx.x; item < P.nrk_items; item += gridDim.x) {
@@ -1570,13 +1570,13 @@ __device__ inline TileGeom block_geom(uint32_t n) {
 
 __global__ void __launch_bounds__(kGenThreads) k_block_digest(GenParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ int32_t dtab[64];
+    __shared__ int32_t dtab[65];
     __shared__ uint32_t histo[66];
     __shared__ uint32_t counts[kGenThreads / 32];
     __shared__ uint32_t filt[64];
     __shared__ uint32_t hsh[kGenThreads][5];
     __shared__ int state[4];  // k, allowed, hashed, done
-    for (uint32_t i = threadIdx.x; i < 64; i += blockDim.x) dtab[i] = (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i];
+    for (uint32_t i = threadIdx.x; i < 65; i += blockDim.x) dtab[i] = i < 64 ? (int32_t)P.ent_tab[i + 1] - (int32_t)P.ent_tab[i] : 0;
     __syncthreads();
     __shared__ uint16_t s_rank[(SDBF_RANK_BINS + 7) / 8 * 8];
     for (uint32_t i = threadIdx.x; i < SDBF_RANK_BINS; i += blockDim.x) s_rank[i] = P.rank_tab[i];

@@ -43,8 +43,9 @@ struct GenChunk {
 // kRkThreads x kRkPer consecutive positions of one chunk (a "stretch"); one
 // work item (chunk, first position) per stretch.
 constexpr int kRkThreads = 128;
-constexpr uint32_t kRkPer = 264;  // positions per thread: a multiple of 8 whose word count (66) is
-                                  // 2 mod 4, so a warp's byte-word reads are at most 2-way bank conflicts
+constexpr uint32_t kRkPer = 312;  // positions per thread: a multiple of 8 whose word count (78) is
+                                  // 2 mod 4, so a warp's byte-word reads are at most 2-way bank
+                                  // conflicts; 73.3 KB per CTA still fits three CTAs per SM
 constexpr uint32_t kRkSpan = kRkThreads * kRkPer;
 
 struct GenTile {
