@@ -1039,7 +1039,8 @@ __device__ __forceinline__ void prefetch_l2(const void* gmem, uint32_t bytes) {
 // ------------------------------------------------ precomputed ranks
 // Entropy ranks of a stream launch group ahead of its tile kernel.  One CTA
 // item is a stretch of kRkSpan positions of a chunk, its bytes staged in
-// shared memory with 16-byte loads; each thread ranks kRkPer consecutive
+// shared memory by 16-byte asynchronous copies (the CTA's next stretch
+// prefetched into L2 meanwhile); each thread ranks kRkPer consecutive
 // positions with its own histogram (rank_run, the tile kernel's rank loop),
 // so a thread's 64-byte window set-up is spread over 312 positions instead
 // of a tile thread's 88.  Ranks of positions >= n-64 are 0; the chunk's
